@@ -1,0 +1,149 @@
+/*
+ * mtcheck.h -- C ABI of the GB300 incremental-checkpoint deduplicator.
+ *
+ * Drop-in boundary for the deduplication path of TauferLab/MTCheck: each
+ * entry point replaces one member of BaseDeduplicator
+ * (include/deduplicator_interface.hpp:14-184) or one helper of the
+ * reference, cited beside it.  Plain pointers and sizes only; "device"
+ * pointers are CUDA device addresses on the current device.  Every call
+ * returns an MTC_* status; mtc_last_error() gives a message for the calling
+ * thread.  A handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef MTCHECK_H
+#define MTCHECK_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference reports errors only by printf) */
+#define MTC_OK 0
+#define MTC_EINVAL 1     /* bad argument, length change without baseline, short buffer */
+#define MTC_ECORRUPT 2   /* malformed incremental checkpoint */
+#define MTC_ENOMEM 3     /* device or host allocation failed, table full */
+#define MTC_ETIMEOUT 4   /* a bounded device wait expired */
+#define MTC_ECUDA 5      /* CUDA runtime error */
+#define MTC_EINTERNAL 6  /* internal invariant violated */
+#define MTC_ENOTSUP 7    /* outside the supported range */
+
+/* approaches: DedupMode values of include/utils.hpp:39-49 */
+#define MTC_FULL 1
+#define MTC_BASIC 2
+#define MTC_LIST 3
+#define MTC_TREE 4
+#define MTC_TREE_LOW_OFFSET_REF 5 /* tree with the serial labelling of include/reference_impl.hpp:16-132 */
+#define MTC_TREE_LOW_OFFSET 6     /* same as MTC_TREE (src/dedup_files.cpp:68-70) */
+
+/* chunk digest functions: include/hash_functions.hpp:16-20 selects one at build time */
+#define MTC_HASH_MURMUR3 0 /* include/kokkos_murmur3.hpp:213-292, 431-437 */
+#define MTC_HASH_MD5 1     /* include/kokkos_md5.hpp:287-323 */
+
+/* header_t, include/utils.hpp:29-37: the first 32 bytes of every .basic,
+ * .hashlist and .hashtree incremental checkpoint */
+typedef struct mtc_header {
+  uint32_t ref_id;
+  uint32_t chkpt_id;
+  uint64_t datalen;
+  uint32_t chunk_size;
+  uint32_t num_first_ocur;
+  uint32_t num_prior_chkpts;
+  uint32_t num_shift_dupl;
+} mtc_header_t;
+
+/* counters and timers of the last operation (BaseDeduplicator members
+ * current_id, baseline_id, datasizes, timers[4], restart_timers[2],
+ * include/deduplicator_interface.hpp:15-23; TreeDeduplicator::num_first_ocur /
+ * num_shift_dupl, include/tree_approach.hpp:52-58) */
+typedef struct mtc_info {
+  uint32_t current_id;
+  uint32_t baseline_id;
+  uint32_t chunk_size;
+  uint32_t num_first_ocur;
+  uint32_t num_shift_dupl;
+  uint32_t num_prior_chkpts;
+  uint64_t data_len;
+  uint64_t diff_len;
+  uint64_t data_size;      /* datasizes.first */
+  uint64_t metadata_size;  /* datasizes.second */
+  double timers[4];        /* setup, compare, gather, copy to host (s) */
+  double restart_timers[2];/* copy, total (s) */
+  uint32_t device_error;   /* last device error bits (0 = none) */
+  uint32_t reserved;
+} mtc_info_t;
+
+typedef struct mtc_dedup mtc_dedup_t;
+
+/* TreeDeduplicator(uint32_t) and siblings, src/tree_approach.cpp:5-9 */
+int mtc_create(int approach, int hash, uint32_t chunk_size, mtc_dedup_t** out);
+/* ~TreeDeduplicator(), src/tree_approach.cpp:11 */
+int mtc_destroy(mtc_dedup_t* h);
+/* CUDA stream for all work of the handle (0 = legacy default stream); the
+ * reference uses Kokkos' default execution space instance */
+int mtc_set_stream(mtc_dedup_t* h, void* cuda_stream);
+
+/* checkpoint(header_t&, uint8_t*, size_t, HostMirror&, bool),
+ * include/deduplicator_interface.hpp:52-57: deduplicates the device buffer and
+ * assembles the incremental checkpoint in device memory; current_id is NOT
+ * advanced.  *diff_len receives its size; fetch it with mtc_diff_copy. */
+int mtc_checkpoint_header(mtc_dedup_t* h, mtc_header_t* header, const void* dev_data, uint64_t len,
+                          int make_baseline, uint64_t* diff_len);
+/* checkpoint(uint8_t*, size_t, HostMirror&, bool), :93-96 (advances current_id) */
+int mtc_checkpoint(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_baseline, uint64_t* diff_len);
+/* the device->host copy of the diff, src/tree_approach.cpp:1677-1688 */
+int mtc_diff_copy(mtc_dedup_t* h, void* host_dst, uint64_t capacity);
+/* the diff of the last checkpoint in device memory (valid until the next call) */
+int mtc_diff_device(mtc_dedup_t* h, const void** dev_ptr, uint64_t* len);
+/* checkpoint + malloc'd host copy (release with mtc_free); advances current_id */
+int mtc_checkpoint_alloc(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_baseline, void** host_diff,
+                         uint64_t* diff_len);
+void mtc_free(void* p);
+/* checkpoint(uint8_t*, size_t, std::string& filename, std::string& logname, bool),
+ * :73-77: writes the diff to `filename` and the CSV logs under `logname`
+ * (logname NULL: no logs) */
+int mtc_checkpoint_file(mtc_dedup_t* h, const void* dev_data, uint64_t len, const char* filename,
+                        const char* logname, int make_baseline);
+
+/* restart(uint8_t*, size_t, std::vector<HostMirror>&, std::string&, uint32_t),
+ * :142-146: rebuilds checkpoint `chkpt_id` of the chain `host_diffs[0..n)` into
+ * the device buffer `dev_out` of `len` == header.datalen bytes */
+int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* host_diffs, const uint64_t* lens,
+                uint32_t n, uint32_t chkpt_id);
+/* same, with the chain already resident in device memory */
+int mtc_restart_device(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* dev_diffs,
+                       const uint64_t* lens, uint32_t n, uint32_t chkpt_id);
+/* restart(View, std::vector<std::string>& filenames, std::string&, uint32_t), :156-159;
+ * the names are complete paths of the incremental checkpoint files */
+int mtc_restart_files(mtc_dedup_t* h, void* dev_out, uint64_t len, const char* const* filenames, uint32_t n,
+                      uint32_t chkpt_id);
+
+/* counters and timers */
+int mtc_get_info(const mtc_dedup_t* h, mtc_info_t* out);
+/* write_chkpt_log(header_t&, HostMirror& diff_h, std::string& logname),
+ * include/deduplicator_interface.hpp:172-174: appends the three CSV logs
+ * <logname>.chunk_size.<c>{.csv,.size.csv,.timing.csv} for the last checkpoint */
+int mtc_write_chkpt_log(const mtc_dedup_t* h, const mtc_header_t* header, const void* host_diff, uint64_t len,
+                        const char* logname);
+/* write_restart_log(uint32_t select_chkpt, std::string& logname), :181-183 */
+int mtc_write_restart_log(const mtc_dedup_t* h, uint32_t select_chkpt, const char* logname);
+
+/* chunk digests of a device buffer into dev_digests (16 bytes per chunk, the
+ * last chunk may be short): the per-chunk hash() calls of the leaf loops,
+ * src/tree_approach.cpp:319-323 */
+int mtc_hash_chunks(int hash, const void* dev_data, uint64_t len, uint32_t chunk_size, void* dev_digests,
+                    void* cuda_stream);
+/* calculate_digest_host's digest, include/hash_functions.hpp:65-82 */
+int mtc_digest_host(int hash, const void* host_data, uint64_t len, uint8_t out[16]);
+/* its printable form: "XXXXXXXX XXXXXXXX XXXXXXXX XXXXXXXX " (37 bytes incl. NUL) */
+int mtc_digest_hex(const uint8_t digest[16], char out[37]);
+
+/* kernels launched by the library so far (all handles) */
+uint64_t mtc_launch_count(void);
+/* message for the last failing call on this thread */
+const char* mtc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MTCHECK_H */

@@ -1,0 +1,257 @@
+"""mtcheck_gb300 -- GB300 incremental-checkpoint deduplicator (Python binding).
+
+The product is the CUDA library ``_build/libmtcheck_gb300.so`` behind the C ABI
+of ``include/mtcheck.h``; this module binds it with ctypes and mirrors the
+reference's deduplicator classes (``TreeDeduplicator``, ``ListDeduplicator``,
+``BasicDeduplicator``, ``FullDeduplicator`` of TauferLab/MTCheck,
+include/deduplicator_interface.hpp:14-184).  Device buffers are torch CUDA
+tensors (uint8) or raw device addresses.  There is no CPU fallback: every
+call fails loudly when the library or a GPU is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libmtcheck_gb300.so")
+
+# approaches: DedupMode values (include/utils.hpp:39-49)
+FULL, BASIC, LIST, TREE, TREE_LOW_OFFSET_REF, TREE_LOW_OFFSET = 1, 2, 3, 4, 5, 6
+MURMUR3, MD5 = 0, 1
+STATUS = {0: "MTC_OK", 1: "MTC_EINVAL", 2: "MTC_ECORRUPT", 3: "MTC_ENOMEM", 4: "MTC_ETIMEOUT", 5: "MTC_ECUDA",
+          6: "MTC_EINTERNAL", 7: "MTC_ENOTSUP"}
+FILE_SUFFIX = {FULL: ".full_chkpt", BASIC: ".basic.incr_chkpt", LIST: ".hashlist.incr_chkpt",
+               TREE: ".hashtree.incr_chkpt", TREE_LOW_OFFSET_REF: ".hashtree.incr_chkpt",
+               TREE_LOW_OFFSET: ".hashtree.incr_chkpt"}
+
+
+class MtcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class Header(ctypes.Structure):
+    """header_t, include/utils.hpp:29-37."""
+    _fields_ = [("ref_id", ctypes.c_uint32), ("chkpt_id", ctypes.c_uint32), ("datalen", ctypes.c_uint64),
+                ("chunk_size", ctypes.c_uint32), ("num_first_ocur", ctypes.c_uint32),
+                ("num_prior_chkpts", ctypes.c_uint32), ("num_shift_dupl", ctypes.c_uint32)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("current_id", ctypes.c_uint32), ("baseline_id", ctypes.c_uint32), ("chunk_size", ctypes.c_uint32),
+                ("num_first_ocur", ctypes.c_uint32), ("num_shift_dupl", ctypes.c_uint32),
+                ("num_prior_chkpts", ctypes.c_uint32), ("data_len", ctypes.c_uint64),
+                ("diff_len", ctypes.c_uint64), ("data_size", ctypes.c_uint64), ("metadata_size", ctypes.c_uint64),
+                ("timers", ctypes.c_double * 4), ("restart_timers", ctypes.c_double * 2),
+                ("device_error", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+# every symbol of include/mtcheck.h with its ctypes signature
+_VP, _U32, _U64, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+SIGNATURES = {
+    "mtc_create": (_I, [_I, _I, _U32, ctypes.POINTER(_VP)]),
+    "mtc_destroy": (_I, [_VP]),
+    "mtc_set_stream": (_I, [_VP, _VP]),
+    "mtc_checkpoint_header": (_I, [_VP, ctypes.POINTER(Header), _VP, _U64, _I, ctypes.POINTER(_U64)]),
+    "mtc_checkpoint": (_I, [_VP, _VP, _U64, _I, ctypes.POINTER(_U64)]),
+    "mtc_diff_copy": (_I, [_VP, _VP, _U64]),
+    "mtc_diff_device": (_I, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(_U64)]),
+    "mtc_checkpoint_alloc": (_I, [_VP, _VP, _U64, _I, ctypes.POINTER(_VP), ctypes.POINTER(_U64)]),
+    "mtc_free": (None, [_VP]),
+    "mtc_checkpoint_file": (_I, [_VP, _VP, _U64, ctypes.c_char_p, ctypes.c_char_p, _I]),
+    "mtc_restart": (_I, [_VP, _VP, _U64, ctypes.POINTER(_VP), ctypes.POINTER(_U64), _U32, _U32]),
+    "mtc_restart_device": (_I, [_VP, _VP, _U64, ctypes.POINTER(_VP), ctypes.POINTER(_U64), _U32, _U32]),
+    "mtc_restart_files": (_I, [_VP, _VP, _U64, ctypes.POINTER(ctypes.c_char_p), _U32, _U32]),
+    "mtc_get_info": (_I, [_VP, ctypes.POINTER(Info)]),
+    "mtc_write_chkpt_log": (_I, [_VP, ctypes.POINTER(Header), _VP, _U64, ctypes.c_char_p]),
+    "mtc_write_restart_log": (_I, [_VP, _U32, ctypes.c_char_p]),
+    "mtc_hash_chunks": (_I, [_I, _VP, _U64, _U32, _VP, _VP]),
+    "mtc_digest_host": (_I, [_I, _VP, _U64, _VP]),
+    "mtc_digest_hex": (_I, [_VP, ctypes.c_char_p]),
+    "mtc_launch_count": (_U64, []),
+    "mtc_last_error": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise ImportError("mtcheck_gb300 CUDA library missing: %s (run __graft_entry__.build())" % path)
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise MtcError(rc, (load().mtc_last_error() or b"").decode())
+
+
+def _dev_ptr(buf):
+    """(address, nbytes) of a torch CUDA tensor, or pass (int address, nbytes)."""
+    if isinstance(buf, tuple):
+        return int(buf[0]), int(buf[1])
+    if not getattr(buf, "is_cuda", False):
+        raise TypeError("expected a CUDA tensor or an (address, nbytes) pair")
+    if not buf.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    return int(buf.data_ptr()), int(buf.numel() * buf.element_size())
+
+
+def launch_count():
+    return int(load().mtc_launch_count())
+
+
+def hash_chunks(kind, buf, chunk_size, out=None, stream=0):
+    """Digests of every chunk of a device buffer (16 bytes each)."""
+    import torch
+    ptr, n = _dev_ptr(buf)
+    nchunks = (n + chunk_size - 1) // chunk_size
+    if out is None:
+        out = torch.empty(nchunks * 16, dtype=torch.uint8, device="cuda")
+    _check(load().mtc_hash_chunks(kind, ptr, n, chunk_size, out.data_ptr(), stream))
+    return out
+
+
+def digest_host(data, kind=MURMUR3):
+    """calculate_digest_host's 16-byte digest of a host buffer."""
+    a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray)) else data,
+                             dtype=np.uint8)
+    out = (ctypes.c_uint8 * 16)()
+    _check(load().mtc_digest_host(kind, a.ctypes.data if a.size else None, a.size, out))
+    return bytes(out)
+
+
+def digest_hex(d):
+    out = ctypes.create_string_buffer(37)
+    _check(load().mtc_digest_hex(ctypes.c_char_p(d), out))
+    return out.value.decode()
+
+
+class Deduplicator:
+    """Common base: BaseDeduplicator (include/deduplicator_interface.hpp:14-184)."""
+    approach = TREE
+
+    def __init__(self, chunk_size, hash=MURMUR3, approach=None):
+        L = load()
+        if approach is not None:
+            self.approach = approach
+        self.chunk_size = chunk_size
+        h = _VP()
+        _check(L.mtc_create(self.approach, hash, chunk_size, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mtc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        _check(load().mtc_set_stream(self.h, int(stream)))
+
+    # -- checkpoint ------------------------------------------------------
+    def checkpoint_device(self, buf, make_baseline, advance=True):
+        """Deduplicate a device buffer; the diff stays in device memory.  Returns its size."""
+        ptr, n = _dev_ptr(buf)
+        out = _U64()
+        if advance:
+            _check(load().mtc_checkpoint(self.h, ptr, n, int(make_baseline), ctypes.byref(out)))
+        else:
+            _check(load().mtc_checkpoint_header(self.h, None, ptr, n, int(make_baseline), ctypes.byref(out)))
+        return int(out.value)
+
+    def checkpoint(self, buf, make_baseline, advance=True):
+        """checkpoint(uint8_t*, size_t, HostMirror& diff_h, bool): returns the diff as bytes."""
+        n = self.checkpoint_device(buf, make_baseline, advance)
+        host = np.empty(n, dtype=np.uint8)
+        _check(load().mtc_diff_copy(self.h, host.ctypes.data, n))
+        return host.tobytes()
+
+    def copy_diff(self, host_array):
+        _check(load().mtc_diff_copy(self.h, host_array.ctypes.data, host_array.nbytes))
+
+    def diff_device(self):
+        p, n = _VP(), _U64()
+        _check(load().mtc_diff_device(self.h, ctypes.byref(p), ctypes.byref(n)))
+        return int(p.value or 0), int(n.value)
+
+    def checkpoint_file(self, buf, filename, logname=None, make_baseline=False):
+        ptr, n = _dev_ptr(buf)
+        _check(load().mtc_checkpoint_file(self.h, ptr, n, filename.encode(),
+                                          logname.encode() if logname else None, int(make_baseline)))
+
+    # -- restart ---------------------------------------------------------
+    def restart(self, out, chkpts, chkpt_id):
+        """restart(View data, std::vector<HostMirror>& chkpts, logname, id) into device buffer `out`."""
+        ptr, n = _dev_ptr(out)
+        bufs = [np.frombuffer(c, dtype=np.uint8) for c in chkpts]
+        ptrs = (_VP * len(bufs))(*[b.ctypes.data if b.size else 0 for b in bufs])
+        lens = (_U64 * len(bufs))(*[b.size for b in bufs])
+        _check(load().mtc_restart(self.h, ptr, n, ptrs, lens, len(bufs), chkpt_id))
+
+    def restart_device(self, out, dev_chkpts, chkpt_id):
+        """Restart from a chain resident in device memory: list of (address, nbytes)."""
+        ptr, n = _dev_ptr(out)
+        ptrs = (_VP * len(dev_chkpts))(*[int(p) for p, _ in dev_chkpts])
+        lens = (_U64 * len(dev_chkpts))(*[int(l) for _, l in dev_chkpts])
+        _check(load().mtc_restart_device(self.h, ptr, n, ptrs, lens, len(dev_chkpts), chkpt_id))
+
+    def restart_files(self, out, filenames, chkpt_id):
+        ptr, n = _dev_ptr(out)
+        names = (ctypes.c_char_p * len(filenames))(*[f.encode() for f in filenames])
+        _check(load().mtc_restart_files(self.h, ptr, n, names, len(filenames), chkpt_id))
+
+    # -- counters ----------------------------------------------------------
+    def info(self):
+        i = Info()
+        _check(load().mtc_get_info(self.h, ctypes.byref(i)))
+        return i
+
+    def num_first_ocur(self):
+        return self.info().num_first_ocur
+
+    def num_shift_dupl(self):
+        return self.info().num_shift_dupl
+
+    @property
+    def current_id(self):
+        return self.info().current_id
+
+    def write_restart_log(self, select_chkpt, logname):
+        _check(load().mtc_write_restart_log(self.h, select_chkpt, logname.encode()))
+
+
+class TreeDeduplicator(Deduplicator):
+    approach = TREE
+
+
+class TreeLowOffsetRefDeduplicator(Deduplicator):
+    approach = TREE_LOW_OFFSET_REF
+
+
+class ListDeduplicator(Deduplicator):
+    approach = LIST
+
+
+class BasicDeduplicator(Deduplicator):
+    approach = BASIC
+
+
+class FullDeduplicator(Deduplicator):
+    approach = FULL

@@ -1,0 +1,291 @@
+// capi.cu -- the extern "C" boundary declared in include/mtcheck.h.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "../../include/mtcheck.h"
+#include "engine.hpp"
+#include "host_digest.hpp"
+#include "logs.hpp"
+
+struct mtc_dedup {
+  mtc::Engine* eng;
+};
+
+namespace {
+thread_local std::string t_err;
+
+int ret(int rc, const std::string& msg) {
+  if (rc != MTC_OK) t_err = msg;
+  return rc;
+}
+int ret_eng(int rc, mtc::Engine* e) { return ret(rc, e ? e->last_error : std::string("error")); }
+
+bool valid_mode(int a) { return a >= MTC_FULL && a <= MTC_TREE_LOW_OFFSET; }
+}  // namespace
+
+extern "C" {
+
+int mtc_create(int approach, int hash, uint32_t chunk_size, mtc_dedup_t** out) {
+  if (!out) return ret(MTC_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (!valid_mode(approach)) return ret(MTC_EINVAL, "unknown approach");
+  if (hash != MTC_HASH_MURMUR3 && hash != MTC_HASH_MD5) return ret(MTC_EINVAL, "unknown hash");
+  if (chunk_size == 0) return ret(MTC_EINVAL, "chunk size is 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ret(MTC_ECUDA, "no CUDA device");
+  auto* h = new (std::nothrow) mtc_dedup;
+  if (!h) return ret(MTC_ENOMEM, "out of host memory");
+  h->eng = new (std::nothrow) mtc::Engine(approach, hash, chunk_size);
+  if (!h->eng) { delete h; return ret(MTC_ENOMEM, "out of host memory"); }
+  *out = h;
+  return MTC_OK;
+}
+
+int mtc_destroy(mtc_dedup_t* h) {
+  if (!h) return MTC_OK;
+  delete h->eng;
+  delete h;
+  return MTC_OK;
+}
+
+int mtc_set_stream(mtc_dedup_t* h, void* s) {
+  if (!h) return ret(MTC_EINVAL, "NULL handle");
+  h->eng->set_stream(reinterpret_cast<cudaStream_t>(s));
+  return MTC_OK;
+}
+
+int mtc_checkpoint_header(mtc_dedup_t* h, mtc_header_t* header, const void* dev_data, uint64_t len,
+                          int make_baseline, uint64_t* diff_len) {
+  if (!h) return ret(MTC_EINVAL, "NULL handle");
+  mtc::HeaderHost hh{};
+  int rc = h->eng->checkpoint(static_cast<const uint8_t*>(dev_data), len, make_baseline != 0, &hh);
+  if (rc) return ret_eng(rc, h->eng);
+  if (header) std::memcpy(header, &hh, sizeof(hh));
+  if (diff_len) *diff_len = h->eng->diff_len();
+  return MTC_OK;
+}
+
+int mtc_checkpoint(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_baseline, uint64_t* diff_len) {
+  int rc = mtc_checkpoint_header(h, nullptr, dev_data, len, make_baseline, diff_len);
+  if (rc == MTC_OK) h->eng->current_id += 1;
+  return rc;
+}
+
+int mtc_diff_copy(mtc_dedup_t* h, void* host_dst, uint64_t capacity) {
+  if (!h || !host_dst) return ret(MTC_EINVAL, "NULL argument");
+  return ret_eng(h->eng->copy_diff(host_dst, capacity), h->eng);
+}
+
+int mtc_diff_device(mtc_dedup_t* h, const void** dev_ptr, uint64_t* len) {
+  if (!h || !dev_ptr || !len) return ret(MTC_EINVAL, "NULL argument");
+  *dev_ptr = h->eng->diff_device();
+  *len = h->eng->diff_len();
+  return *dev_ptr ? MTC_OK : ret(MTC_EINVAL, "no checkpoint staged");
+}
+
+int mtc_checkpoint_alloc(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_baseline, void** host_diff,
+                         uint64_t* diff_len) {
+  if (!h || !host_diff) return ret(MTC_EINVAL, "NULL argument");
+  *host_diff = nullptr;
+  uint64_t n = 0;
+  int rc = mtc_checkpoint_header(h, nullptr, dev_data, len, make_baseline, &n);
+  if (rc) return rc;
+  void* buf = std::malloc(n ? n : 1);
+  if (!buf) return ret(MTC_ENOMEM, "out of host memory");
+  rc = h->eng->copy_diff(buf, n);
+  if (rc) { std::free(buf); return ret_eng(rc, h->eng); }
+  h->eng->current_id += 1;
+  *host_diff = buf;
+  if (diff_len) *diff_len = n;
+  return MTC_OK;
+}
+
+void mtc_free(void* p) { std::free(p); }
+
+int mtc_checkpoint_file(mtc_dedup_t* h, const void* dev_data, uint64_t len, const char* filename,
+                        const char* logname, int make_baseline) {
+  if (!h || !filename) return ret(MTC_EINVAL, "NULL argument");
+  mtc::HeaderHost hh{};
+  int rc = h->eng->checkpoint(static_cast<const uint8_t*>(dev_data), len, make_baseline != 0, &hh);
+  if (rc) return ret_eng(rc, h->eng);
+  std::vector<uint8_t> buf(h->eng->diff_len());
+  rc = h->eng->copy_diff(buf.data(), buf.size());
+  if (rc) return ret_eng(rc, h->eng);
+  if (logname) mtc::write_chkpt_log(*h->eng, hh, buf.data(), buf.size(), logname);
+  std::ofstream f(filename, std::ios::out | std::ios::binary | std::ios::trunc);
+  if (!f) return ret(MTC_EINVAL, std::string("cannot open ") + filename);
+  f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
+  f.flush();
+  if (!f) return ret(MTC_EINVAL, std::string("cannot write ") + filename);
+  h->eng->current_id += 1;  // src/tree_approach.cpp:1723
+  return MTC_OK;
+}
+
+int mtc_restart_device(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* dev_diffs,
+                       const uint64_t* lens, uint32_t n, uint32_t chkpt_id) {
+  if (!h || !dev_out || !dev_diffs || !lens) return ret(MTC_EINVAL, "NULL argument");
+  if (chkpt_id >= n) return ret(MTC_EINVAL, "checkpoint id outside the chain");
+  std::vector<const uint8_t*> ptrs(n);
+  std::vector<uint64_t> l(lens, lens + n);
+  std::vector<mtc::HeaderHost> hdrs(n);
+  for (uint32_t i = 0; i < n; i++) {
+    ptrs[i] = static_cast<const uint8_t*>(dev_diffs[i]);
+    if (h->eng->mode() == MTC_FULL) continue;
+    if (l[i] < sizeof(mtc::HeaderHost)) { std::memset(&hdrs[i], 0, sizeof(hdrs[i])); continue; }
+    if (cudaMemcpy(&hdrs[i], ptrs[i], sizeof(mtc::HeaderHost), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return ret(MTC_ECUDA, "cannot read checkpoint header");
+  }
+  return ret_eng(h->eng->restart(static_cast<uint8_t*>(dev_out), len, ptrs, l, hdrs, chkpt_id), h->eng);
+}
+
+int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* host_diffs, const uint64_t* lens,
+                uint32_t n, uint32_t chkpt_id) {
+  if (!h || !dev_out || !host_diffs || !lens) return ret(MTC_EINVAL, "NULL argument");
+  if (chkpt_id >= n) return ret(MTC_EINVAL, "checkpoint id outside the chain");
+  // the reference copies each diff of the chain to the device as it walks it
+  // (src/tree_approach.cpp:756, :962); here the whole used part of the chain
+  // is staged once
+  std::vector<mtc::HeaderHost> hdrs(n);
+  std::vector<const uint8_t*> ptrs(n, nullptr);
+  std::vector<uint64_t> l(lens, lens + n);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (h->eng->mode() != MTC_FULL && l[i] >= sizeof(mtc::HeaderHost)) std::memcpy(&hdrs[i], host_diffs[i], sizeof(mtc::HeaderHost));
+    else std::memset(&hdrs[i], 0, sizeof(hdrs[i]));
+    if (i <= chkpt_id) total += (l[i] + 255) & ~uint64_t(255);
+  }
+  uint8_t* dev = nullptr;
+  if (cudaMalloc(&dev, total ? total : 1) != cudaSuccess) return ret(MTC_ENOMEM, "cannot stage the chain");
+  cudaStream_t s = h->eng->stream();
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, s);
+  uint64_t off = 0;
+  for (uint32_t i = 0; i <= chkpt_id; i++) {
+    ptrs[i] = dev + off;
+    if (l[i]) cudaMemcpyAsync(dev + off, host_diffs[i], l[i], cudaMemcpyHostToDevice, s);
+    off += (l[i] + 255) & ~uint64_t(255);
+  }
+  cudaEventRecord(b, s);
+  int rc = h->eng->restart(static_cast<uint8_t*>(dev_out), len, ptrs, l, hdrs, chkpt_id);
+  float ms = 0;
+  cudaEventSynchronize(b);
+  cudaEventElapsedTime(&ms, a, b);
+  if (rc == MTC_OK) {
+    h->eng->restart_timers[0] = ms * 1e-3;
+    h->eng->restart_timers[1] += ms * 1e-3;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(dev);
+  return ret_eng(rc, h->eng);
+}
+
+int mtc_restart_files(mtc_dedup_t* h, void* dev_out, uint64_t len, const char* const* filenames, uint32_t n,
+                      uint32_t chkpt_id) {
+  if (!h || !filenames) return ret(MTC_EINVAL, "NULL argument");
+  std::vector<std::vector<uint8_t>> bufs(n);
+  std::vector<const void*> ptrs(n);
+  std::vector<uint64_t> lens(n);
+  for (uint32_t i = 0; i < n; i++) {
+    std::ifstream f(filenames[i], std::ios::in | std::ios::binary | std::ios::ate);
+    if (!f) return ret(MTC_EINVAL, std::string("cannot open ") + filenames[i]);
+    std::streamsize sz = f.tellg();
+    f.seekg(0);
+    bufs[i].resize((size_t)sz);
+    if (sz && !f.read(reinterpret_cast<char*>(bufs[i].data()), sz)) return ret(MTC_EINVAL, std::string("cannot read ") + filenames[i]);
+    ptrs[i] = bufs[i].data();
+    lens[i] = (uint64_t)sz;
+  }
+  return mtc_restart(h, dev_out, len, ptrs.data(), lens.data(), n, chkpt_id);
+}
+
+int mtc_get_info(const mtc_dedup_t* h, mtc_info_t* o) {
+  if (!h || !o) return ret(MTC_EINVAL, "NULL argument");
+  const mtc::Engine& e = *h->eng;
+  std::memset(o, 0, sizeof(*o));
+  o->current_id = e.current_id;
+  o->baseline_id = e.baseline_id;
+  o->chunk_size = e.chunk_size();
+  o->num_first_ocur = e.num_first_ocur;
+  o->num_shift_dupl = e.num_shift_dupl;
+  o->num_prior_chkpts = e.num_prior_chkpts;
+  o->data_len = e.data_len;
+  o->diff_len = e.diff_len();
+  o->data_size = e.datasizes[0];
+  o->metadata_size = e.datasizes[1];
+  for (int i = 0; i < 4; i++) o->timers[i] = e.timers[i];
+  o->restart_timers[0] = e.restart_timers[0];
+  o->restart_timers[1] = e.restart_timers[1];
+  o->device_error = e.last_device_error;
+  return MTC_OK;
+}
+
+int mtc_write_chkpt_log(const mtc_dedup_t* h, const mtc_header_t* header, const void* host_diff, uint64_t len,
+                        const char* logname) {
+  if (!h || !header || !logname || (!host_diff && len)) return ret(MTC_EINVAL, "NULL argument");
+  mtc::HeaderHost hh;
+  std::memcpy(&hh, header, sizeof(hh));
+  mtc::write_chkpt_log(*h->eng, hh, static_cast<const uint8_t*>(host_diff), len, logname);
+  return MTC_OK;
+}
+
+int mtc_write_restart_log(const mtc_dedup_t* h, uint32_t select_chkpt, const char* logname) {
+  if (!h || !logname) return ret(MTC_EINVAL, "NULL argument");
+  mtc::write_restart_log(*h->eng, select_chkpt, logname);
+  return MTC_OK;
+}
+
+int mtc_hash_chunks(int hash, const void* dev_data, uint64_t len, uint32_t chunk_size, void* dev_digests,
+                    void* cuda_stream) {
+  if (!dev_data || !dev_digests || chunk_size == 0) return ret(MTC_EINVAL, "bad argument");
+  if (hash != MTC_HASH_MURMUR3 && hash != MTC_HASH_MD5) return ret(MTC_EINVAL, "unknown hash");
+  if (len == 0) return MTC_OK;
+  const uint64_t n = (len + chunk_size - 1) / chunk_size;
+  if (n >= (1ull << 31)) return ret(MTC_ENOTSUP, "more than 2^31 chunks");
+  mtc::LeafArgs a;
+  a.data = static_cast<const uint8_t*>(dev_data);
+  a.len = len;
+  a.cs = chunk_size;
+  a.n_chunks = (uint32_t)n;
+  a.out = static_cast<mtc::Digest*>(dev_digests);
+  a.hash_kind = hash;
+  a.epi = mtc::EPI_HASH;
+  mtc::TmaCache cache;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
+  cudaError_t e = mtc::launch_leaves(a, &cache, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return ret(MTC_ECUDA, cudaGetErrorString(e));
+  return MTC_OK;
+}
+
+int mtc_digest_host(int hash, const void* host_data, uint64_t len, uint8_t out[16]) {
+  if ((!host_data && len) || !out) return ret(MTC_EINVAL, "NULL argument");
+  if (hash != MTC_HASH_MURMUR3 && hash != MTC_HASH_MD5) return ret(MTC_EINVAL, "unknown hash");
+  mtc::digest_host(hash, static_cast<const uint8_t*>(host_data), len, out);
+  return MTC_OK;
+}
+
+int mtc_digest_hex(const uint8_t d[16], char out[37]) {
+  if (!d || !out) return ret(MTC_EINVAL, "NULL argument");
+  static const char hx[] = "0123456789ABCDEF";
+  char* c = out;
+  for (int k = 0; k < 16; k++) {
+    *c++ = hx[d[k] >> 4];
+    *c++ = hx[d[k] & 15];
+    if (k % 4 == 3) *c++ = ' ';
+  }
+  *c = 0;
+  return MTC_OK;
+}
+
+uint64_t mtc_launch_count(void) { return mtc::launch_count(); }
+
+const char* mtc_last_error(void) { return t_err.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// engine.cu -- host orchestration of one deduplicator: device state, map
+// growth, the per-checkpoint launch sequence and the readback of the diff
+// layout.  Mirrors TreeDeduplicator / ListDeduplicator / BasicDeduplicator /
+// FullDeduplicator::checkpoint(header_t&, ...) (src/tree_approach.cpp:1578-1689,
+// src/list_approach.cpp:843-931, src/basic_approach.cpp:468-549,
+// src/full_approach.cpp:14-77).
+#include <algorithm>
+#include <cstring>
+
+#include "engine.hpp"
+#include "mtc_scan.cuh"
+
+namespace mtc {
+
+template <class T>
+cudaError_t DevBuf<T>::ensure(size_t want, cudaStream_t s, bool keep) {
+  if (want <= n && p) return cudaSuccess;
+  T* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, sizeof(T) * std::max<size_t>(want, 1));
+  if (e != cudaSuccess) return e;
+  if (keep && p && n) cudaMemcpyAsync(q, p, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+  if (p) {
+    cudaStreamSynchronize(s);
+    cudaFree(p);
+  }
+  p = q;
+  n = want;
+  return cudaSuccess;
+}
+template <class T>
+void DevBuf<T>::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  n = 0;
+}
+
+static uint64_t next_pow2(uint64_t v) {
+  uint64_t c = 1;
+  while (c < v) c <<= 1;
+  return c;
+}
+
+Engine::Engine(int mode, int hash_kind, uint32_t chunk_size) : mode_(mode), hash_kind_(hash_kind), cs_(chunk_size) {
+  for (auto& e : ev_) cudaEventCreate(&e);
+  cudaMallocHost(&lay_host_, sizeof(Layout));
+  cudaMallocHost(&err_host_, 2 * sizeof(uint32_t));
+  std::memset(lay_host_, 0, sizeof(Layout));
+}
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_); else cudaDeviceSynchronize();
+  for (auto& e : ev_) if (e) cudaEventDestroy(e);
+  if (lay_host_) cudaFreeHost(lay_host_);
+  if (err_host_) cudaFreeHost(err_host_);
+}
+
+int Engine::fail(int code, const std::string& msg) {
+  last_error = msg;
+  return code;
+}
+
+#define MTC_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) return fail(e_ == cudaErrorMemoryAllocation ? ST_ENOMEM : ST_ECUDA, \
+                                       std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int Engine::ensure_map(uint64_t want_entries, bool reset) {
+  // load factor <= 3/4 after the worst-case number of inserts of one checkpoint
+  const uint64_t need = next_pow2(std::max<uint64_t>(1024, (want_entries * 4 + 2) / 3));
+  if (reset) {
+    if (slots_.n < need || slots_.n > 4 * need) {
+      slots_.release();
+      MTC_CUDA(slots_.ensure(need, stream_));
+    }
+    map_cap_ = slots_.n;
+    MTC_CUDA(cudaMemsetAsync(slots_.p, 0, sizeof(MapSlot) * map_cap_, stream_));
+    MTC_CUDA(cudaMemsetAsync(map_size_.p, 0, sizeof(uint32_t), stream_));
+    map_size_host_ = 0;
+    return ST_OK;
+  }
+  if (map_cap_ >= need) return ST_OK;
+  DevBuf<MapSlot> fresh;
+  MTC_CUDA(fresh.ensure(need, stream_));
+  MTC_CUDA(cudaMemsetAsync(fresh.p, 0, sizeof(MapSlot) * need, stream_));
+  MTC_CUDA(cudaMemsetAsync(map_size_.p, 0, sizeof(uint32_t), stream_));
+  DigestMap from{slots_.p, map_cap_ - 1, map_size_.p};
+  DigestMap to{fresh.p, need - 1, map_size_.p};
+  MTC_CUDA(launch_map_rehash(from, map_cap_, to, err_.p, stream_));
+  MTC_CUDA(cudaStreamSynchronize(stream_));
+  std::swap(slots_.p, fresh.p);
+  std::swap(slots_.n, fresh.n);
+  map_cap_ = need;
+  return ST_OK;
+}
+
+int Engine::ensure_sort(uint32_t K) {
+  const uint64_t T = (uint64_t)(N_ + 1 + kSortTile - 1) / kSortTile + 1;
+  MTC_CUDA(hist_.ensure(K, stream_));
+  MTC_CUDA(rep_.ensure(K, stream_));
+  MTC_CUDA(sort_mat_.ensure((size_t)K * T, stream_));
+  MTC_CUDA(scan2_.ensure((size_t)K * T / kScanTile + 2, stream_));
+  // staging buffer: pad + header + metadata + data
+  const uint64_t stage = 64 + 32 + 12ull * (N_ + 1) + 8ull * K + (uint64_t)(N_ + 1) * cs_;
+  MTC_CUDA(stage_.ensure(stage, stream_));
+  return ST_OK;
+}
+
+int Engine::ensure_state(uint32_t N, bool fresh) {
+  const uint32_t M = 2 * N - 1;
+  const bool tree = mode_ == MODE_TREE || mode_ == MODE_TREE_LOW_OFFSET || mode_ == MODE_TREE_LOW_OFFSET_REF;
+  if (fresh) {
+    N_ = N;
+    M_ = M;
+    const size_t nd = tree ? M : N;
+    MTC_CUDA(digests_.ensure(nd, stream_));
+    MTC_CUDA(cudaMemsetAsync(digests_.p, 0, sizeof(Digest) * nd, stream_));
+    MTC_CUDA(labels_.ensure(nd, stream_));
+    MTC_CUDA(rflag_.ensure(tree ? M : 1, stream_));
+    MTC_CUDA(chunk_slot_.ensure(N, stream_));
+    MTC_CUDA(map_size_.ensure(1, stream_));
+    MTC_CUDA(err_.ensure(1, stream_));
+    MTC_CUDA(fo_list_.ensure(N + 1, stream_));
+    MTC_CUDA(sh_list_.ensure(N + 1, stream_));
+    MTC_CUDA(fo_val_.ensure(N + 1, stream_));
+    MTC_CUDA(reg_chunk_.ensure(N + 1, stream_));
+    MTC_CUDA(reg_slot_.ensure(N + 1, stream_));
+    MTC_CUDA(reg_len_.ensure(N + 1, stream_));
+    MTC_CUDA(sh_key_.ensure(N + 1, stream_));
+    MTC_CUDA(sh_prev_.ensure(N + 1, stream_));
+    MTC_CUDA(scan_.ensure((size_t)(std::max(M, N + 1) + kScanTile - 1) / kScanTile + 2, stream_));
+    MTC_CUDA(scan_total_.ensure(1, stream_));
+    MTC_CUDA(scan_total2_.ensure(1, stream_));
+    MTC_CUDA(lay_.ensure(1, stream_));
+    if (mode_ != MODE_BASIC) {
+      int rc = ensure_map(tree ? M : N, true);
+      if (rc) return rc;
+    }
+    allocated_ = true;
+  }
+  if (mode_ != MODE_BASIC) {
+    int rc = ensure_map((uint64_t)map_size_host_ + (tree ? M_ : N_), false);
+    if (rc) return rc;
+  }
+  return ensure_sort(current_id + 1);
+}
+
+GatherArgs Engine::gather_args(const uint8_t* data, uint64_t len) {
+  GatherArgs g{};
+  g.approach = mode_ == MODE_LIST ? APPROACH_LIST : mode_ == MODE_BASIC ? APPROACH_BASIC : APPROACH_TREE;
+  g.data = data;
+  g.len = len;
+  g.cs = cs_;
+  g.N = N_;
+  g.M = M_;
+  g.cur = current_id;
+  g.baseline_id = baseline_id;
+  g.digests = digests_.p;
+  g.map = DigestMap{slots_.p, map_cap_ ? map_cap_ - 1 : 0, map_size_.p};
+  g.err = err_.p;
+  g.fo_list = fo_list_.p;
+  g.sh_list = sh_list_.p;
+  g.fo_val = fo_val_.p;
+  g.reg_chunk = reg_chunk_.p;
+  g.reg_slot = reg_slot_.p;
+  g.reg_len = reg_len_.p;
+  g.sh_key = sh_key_.p;
+  g.sh_prev = sh_prev_.p;
+  g.hist = hist_.p;
+  g.rep = rep_.p;
+  g.sort_mat = sort_mat_.p;
+  g.scan_scratch = scan_.p;
+  g.scan_total = scan_total_.p;
+  g.scan_scratch2 = scan2_.p;
+  g.scan_total2 = scan_total2_.p;
+  g.stage = stage_.p;
+  g.stage_cap = stage_.n;
+  g.lay = lay_.p;
+  return g;
+}
+
+int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
+  const uint32_t N = N_, M = M_;
+  DigestMap map{slots_.p, map_cap_ - 1, map_size_.p};
+  LeafArgs la;
+  la.data = data;
+  la.len = len;
+  la.cs = cs_;
+  la.n_chunks = N;
+  la.prev = digests_.p + (N - 1);
+  la.labels = labels_.p + (N - 1);
+  la.chunk_slot = chunk_slot_.p;
+  la.map = map;
+  la.cur = current_id;
+  la.epoch = ++epoch_;
+  la.leaf_base = N - 1;
+  la.err = err_.p;
+  la.hash_kind = hash_kind_;
+  la.epi = EPI_TREE;
+  MTC_CUDA(launch_leaves(la, &tma_, stream_));
+  MTC_CUDA(launch_tree_leaf_finalize(la, stream_));
+
+  ForestArgs fa{digests_.p, labels_.p, rflag_.p, map, current_id, 0, err_.p, hash_kind_};
+  if (N >= 2) {
+    // interior nodes [0, N-2]; depth d holds [2^d - 1, 2^(d+1) - 2]
+    int dmax = 0;
+    while (((2ull << dmax) - 1) <= (uint64_t)(N - 2)) dmax++;
+    for (int d = dmax; d >= 0; d--) {  // first-occurrence forest (src/tree_approach.cpp:378-404)
+      uint32_t beg = (uint32_t)((1ull << d) - 1);
+      uint32_t end = (uint32_t)std::min<uint64_t>((2ull << d) - 2, N - 2);
+      fa.epoch = ++epoch_;
+      MTC_CUDA(launch_fo_level(fa, beg, end, stream_));
+    }
+    for (int d = dmax; d >= 0; d--) {  // duplicate forest (:413-477 / baseline :155-227)
+      uint32_t beg = (uint32_t)((1ull << d) - 1);
+      uint32_t end = (uint32_t)std::min<uint64_t>((2ull << d) - 2, N - 2);
+      MTC_CUDA(launch_dup_level(fa, beg, end, baseline_path ? 1 : 0, stream_));
+      if (baseline_path) {
+        fa.epoch = ++epoch_;
+        MTC_CUDA(launch_insert_level(fa, beg, end, stream_));
+      }
+    }
+  }
+  MTC_CUDA(launch_root_compaction(labels_.p, rflag_.p, N, M, mode_ == MODE_TREE_LOW_OFFSET_REF ? 1 : 0, fo_list_.p,
+                                  sh_list_.p, lay_.p, scan_.p, scan_total_.p, stream_));
+  return ST_OK;
+}
+
+int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
+  LeafArgs la;
+  la.data = data;
+  la.len = len;
+  la.cs = cs_;
+  la.n_chunks = N_;
+  la.prev = digests_.p;
+  la.labels = labels_.p;
+  la.chunk_slot = chunk_slot_.p;
+  la.map = DigestMap{slots_.p, map_cap_ ? map_cap_ - 1 : 0, map_size_.p};
+  la.cur = current_id;
+  la.epoch = ++epoch_;
+  la.leaf_base = 0;
+  la.err = err_.p;
+  la.hash_kind = hash_kind_;
+  la.epi = mode_ == MODE_LIST ? EPI_LIST : EPI_BASIC;
+  la.basic_first = current_id == 0 ? 1 : 0;
+  MTC_CUDA(launch_leaves(la, &tma_, stream_));
+  if (mode_ == MODE_LIST) MTC_CUDA(launch_list_finalize(la, stream_));
+  MTC_CUDA(launch_chunk_compaction(labels_.p, N_, mode_ == MODE_BASIC ? 1 : 0, fo_list_.p, sh_list_.p, lay_.p, scan_.p,
+                                   scan_total_.p, stream_));
+  return ST_OK;
+}
+
+int Engine::checkpoint(const uint8_t* data, uint64_t len, bool make_baseline, HeaderHost* header) {
+  if (!data || len == 0) return fail(ST_EINVAL, "empty buffer");
+  const uint64_t n64 = (len + cs_ - 1) / cs_;
+  if (n64 >= (1ull << 31)) return fail(ST_ENOTSUP, "more than 2^31 chunks");
+  const uint32_t N = (uint32_t)n64;
+  const bool fresh = make_baseline || !allocated_;
+  if (mode_ != MODE_FULL && !fresh && len != data_len)
+    return fail(ST_EINVAL, "buffer length changed without a new baseline");
+  MTC_CUDA(cudaEventRecord(ev_[0], stream_));
+  if (mode_ == MODE_FULL) {
+    // FullDeduplicator: the checkpoint is the raw buffer (src/full_approach.cpp:66-72)
+    MTC_CUDA(stage_.ensure(len + 64, stream_));
+    MTC_CUDA(cudaEventRecord(ev_[1], stream_));
+    MTC_CUDA(cudaEventRecord(ev_[2], stream_));
+    MTC_CUDA(cudaMemcpyAsync(stage_.p, data, len, cudaMemcpyDeviceToDevice, stream_));
+    MTC_CUDA(cudaEventRecord(ev_[3], stream_));
+    MTC_CUDA(cudaEventSynchronize(ev_[3]));
+    allocated_ = true;
+    data_len = len;
+    diff_len_ = len;
+    diff_pad_ = 0;
+    datasizes[0] = len;
+    datasizes[1] = 0;
+    float ms[3];
+    cudaEventElapsedTime(&ms[0], ev_[0], ev_[1]);
+    cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
+    cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
+    timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
+    if (header) std::memset(header, 0, sizeof(*header));
+    return ST_OK;
+  }
+  int rc = ensure_state(N, fresh);
+  if (rc) return rc;
+  data_len = len;
+  if (current_id == 0 || make_baseline) baseline_id = current_id;
+  MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
+  MTC_CUDA(cudaEventRecord(ev_[1], stream_));
+  if (mode_ == MODE_LIST || mode_ == MODE_BASIC) {
+    rc = run_list_basic(data, len);
+  } else {
+    // TreeLowOffsetRef follows include/reference_impl.hpp:16-132, which has
+    // no baseline special case; the tree modes follow dedup_data_baseline for
+    // checkpoint 0 and every requested baseline (src/tree_approach.cpp:1644-1653)
+    const bool baseline_path = mode_ != MODE_TREE_LOW_OFFSET_REF && (current_id == 0 || make_baseline);
+    rc = run_tree(data, len, baseline_path);
+  }
+  if (rc) return rc;
+  MTC_CUDA(cudaEventRecord(ev_[2], stream_));
+  MTC_CUDA(launch_assemble(gather_args(data, len), (uint64_t)N_ + 1, stream_));
+  MTC_CUDA(cudaEventRecord(ev_[3], stream_));
+  return finish(data, len, header);
+}
+
+int Engine::finish(const uint8_t* data, uint64_t len, HeaderHost* header) {
+  (void)data;
+  MTC_CUDA(cudaMemcpyAsync(lay_host_, lay_.p, sizeof(Layout), cudaMemcpyDeviceToHost, stream_));
+  MTC_CUDA(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+  if (map_size_.p) MTC_CUDA(cudaMemcpyAsync(err_host_ + 1, map_size_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+  MTC_CUDA(cudaStreamSynchronize(stream_));
+  const Layout& L = *lay_host_;
+  last_device_error = err_host_[0];
+  if (map_size_.p) map_size_host_ = err_host_[1];
+  float ms[3];
+  cudaEventElapsedTime(&ms[0], ev_[0], ev_[1]);
+  cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
+  cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
+  timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
+  if (last_device_error & DERR_SPIN) return fail(ST_ETIMEOUT, "bounded device wait expired");
+  if (last_device_error & (DERR_MAP_FULL | DERR_CAPACITY)) return fail(ST_ENOMEM, "device table or staging buffer full");
+  if (last_device_error & DERR_MISSING) return fail(ST_EINTERNAL, "root digest missing from the map");
+  if (!L.ok) return fail(ST_EINTERNAL, "diff layout failed");
+  diff_len_ = L.diff_len;
+  diff_pad_ = L.pad;
+  num_first_ocur = L.F;
+  num_shift_dupl = mode_ == MODE_BASIC ? 0 : L.S;
+  num_prior_chkpts = mode_ == MODE_BASIC ? 0 : L.P;
+  datasizes[0] = L.size_data;
+  datasizes[1] = L.size_meta;
+  if (header) {
+    header->ref_id = baseline_id;
+    header->chkpt_id = current_id;
+    header->datalen = len;
+    header->chunk_size = cs_;
+    header->num_first_ocur = num_first_ocur;
+    header->num_prior_chkpts = num_prior_chkpts;
+    header->num_shift_dupl = num_shift_dupl;
+  }
+  return ST_OK;
+}
+
+const uint8_t* Engine::diff_device() const { return stage_.p ? stage_.p + diff_pad_ : nullptr; }
+
+int Engine::copy_diff(void* host, uint64_t cap) {
+  if (!stage_.p) return fail(ST_EINVAL, "no checkpoint staged");
+  if (cap < diff_len_) return fail(ST_EINVAL, "host buffer too small");
+  cudaEvent_t a = ev_[0], b = ev_[1];
+  MTC_CUDA(cudaEventRecord(a, stream_));
+  MTC_CUDA(cudaMemcpyAsync(host, stage_.p + diff_pad_, diff_len_, cudaMemcpyDeviceToHost, stream_));
+  MTC_CUDA(cudaEventRecord(b, stream_));
+  MTC_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  timers[3] = ms * 1e-3;
+  return ST_OK;
+}
+
+}  // namespace mtc

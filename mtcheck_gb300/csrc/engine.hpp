@@ -1,0 +1,112 @@
+// engine.hpp -- the device-side state of one deduplicator and the host code
+// that drives its kernels.  One Engine serves every approach of the
+// reference (full / basic / list / tree, and the tree with the serial
+// reference labelling); the public C++ classes and the C ABI wrap it.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mtc_common.cuh"
+#include "mtc_gather.hpp"
+#include "mtc_internal.hpp"
+
+namespace mtc {
+
+// DedupMode values of the reference (include/utils.hpp:39-49).
+enum : int { MODE_FULL = 1, MODE_BASIC = 2, MODE_LIST = 3, MODE_TREE = 4, MODE_TREE_LOW_OFFSET_REF = 5, MODE_TREE_LOW_OFFSET = 6 };
+
+// Public status codes (mirrored in include/mtcheck.h).
+enum : int { ST_OK = 0, ST_EINVAL = 1, ST_ECORRUPT = 2, ST_ENOMEM = 3, ST_ETIMEOUT = 4, ST_ECUDA = 5, ST_EINTERNAL = 6, ST_ENOTSUP = 7 };
+
+struct HeaderHost {  // header_t, include/utils.hpp:29-37
+  uint32_t ref_id, chkpt_id;
+  uint64_t datalen;
+  uint32_t chunk_size, num_first_ocur, num_prior_chkpts, num_shift_dupl;
+};
+static_assert(sizeof(HeaderHost) == 32, "header_t is 32 bytes");
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;  // elements
+  cudaError_t ensure(size_t want, cudaStream_t s, bool keep = false);
+  void release();
+  ~DevBuf() { release(); }
+};
+
+class Engine {
+ public:
+  Engine(int mode, int hash_kind, uint32_t chunk_size);
+  ~Engine();
+
+  // checkpoint(header_t&, ...) of the reference: the diff is assembled in
+  // device memory; current_id is not advanced.
+  int checkpoint(const uint8_t* dev_data, uint64_t len, bool make_baseline, HeaderHost* header);
+  // Copy the staged diff to host memory (pinned or pageable).
+  int copy_diff(void* host, uint64_t cap);
+  const uint8_t* diff_device() const;
+  uint64_t diff_len() const { return diff_len_; }
+  // restart(View, chain, logname, id): `dev_diffs` are device-resident copies
+  // of the chain (the main one is index `id`).
+  int restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint8_t*>& dev_diffs,
+              const std::vector<uint64_t>& lens, const std::vector<HeaderHost>& headers, uint32_t id);
+
+  int mode() const { return mode_; }
+  int hash_kind() const { return hash_kind_; }
+  uint32_t chunk_size() const { return cs_; }
+  uint32_t current_id = 0;
+  uint32_t baseline_id = 0;
+  uint64_t data_len = 0;
+  uint32_t num_first_ocur = 0, num_shift_dupl = 0, num_prior_chkpts = 0;
+  uint64_t datasizes[2] = {0, 0};
+  double timers[4] = {0, 0, 0, 0};          // setup, compare, gather, copy-to-host (seconds)
+  double restart_timers[2] = {0, 0};        // copy, total
+  uint32_t last_device_error = 0;
+  std::string last_error;
+
+  cudaStream_t stream() const { return stream_; }
+  void set_stream(cudaStream_t s) { stream_ = s; }
+  uint32_t launches() const { return launches_; }
+
+ private:
+  int fail(int code, const std::string& msg);
+  int ensure_state(uint32_t N, bool fresh);
+  int ensure_map(uint64_t want_entries, bool reset);
+  int ensure_sort(uint32_t K);
+  int run_tree(const uint8_t* data, uint64_t len, bool baseline_path);
+  int run_list_basic(const uint8_t* data, uint64_t len);
+  int finish(const uint8_t* data, uint64_t len, HeaderHost* header);
+  GatherArgs gather_args(const uint8_t* data, uint64_t len);
+
+  int mode_, hash_kind_;
+  uint32_t cs_;
+  cudaStream_t stream_ = nullptr;
+  bool allocated_ = false;
+  uint32_t N_ = 0, M_ = 0;
+  uint32_t epoch_ = 0;
+  uint64_t map_cap_ = 0;
+  uint32_t map_size_host_ = 0;
+  uint32_t launches_ = 0;
+
+  DevBuf<Digest> digests_;     // tree heap (M) or hash list (N)
+  DevBuf<uint8_t> labels_, rflag_;
+  DevBuf<uint32_t> chunk_slot_;
+  DevBuf<MapSlot> slots_;
+  DevBuf<uint32_t> map_size_, err_;
+  DevBuf<uint32_t> fo_list_, sh_list_, reg_chunk_, reg_slot_, reg_len_, sh_key_, sh_prev_, hist_, rep_;
+  DevBuf<uint64_t> fo_val_, sort_mat_, scan_, scan_total_, scan2_, scan_total2_;
+  DevBuf<uint8_t> stage_;
+  DevBuf<Layout> lay_;
+  Layout* lay_host_ = nullptr;      // pinned
+  uint32_t* err_host_ = nullptr;    // pinned [err, map size]
+  uint64_t diff_len_ = 0, diff_pad_ = 0;
+  TmaCache tma_;
+  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+
+  friend class RestartRunner;
+};
+
+}  // namespace mtc

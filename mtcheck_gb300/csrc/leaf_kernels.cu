@@ -1,0 +1,404 @@
+// leaf_kernels.cu -- chunk hashing and per-chunk classification.
+//
+// One thread owns one chunk (Murmur3 and MD5 are serial over a chunk).  On the
+// fast path the chunk bytes reach shared memory through TMA tiled loads: the
+// buffer is viewed as a 2-D tensor [n_full rows x cs bytes]; each stage moves a
+// box of 256 rows x W bytes (W = 128, 64, 32 or 16) with the matching TMA
+// swizzle so that the 256 consumer threads read their rows without bank
+// conflicts.  A dedicated producer warp keeps STAGES boxes in flight; full/empty
+// mbarriers hand stages between producer and consumers.  Odd chunk sizes,
+// unaligned buffers and the partial last chunk use a thread-per-chunk kernel
+// that reads global memory directly.  Both end in the same epilogue, which
+// restates the leaf loops of the reference:
+//   tree  -- src/tree_approach.cpp:57-94 (baseline) and :309-351
+//   list  -- src/list_approach.cpp:38-61
+//   basic -- src/basic_approach.cpp:25-46
+#include <cstdio>
+#include <atomic>
+#include <mutex>
+
+#include "mtc_common.cuh"
+#include "mtc_internal.hpp"
+#include "mtc_tma.cuh"
+
+namespace mtc {
+
+namespace {
+constexpr int kRows = 256;    // consumer threads = chunks per tile = TMA box rows
+constexpr int kStages = 3;    // boxes in flight per CTA
+constexpr int kThreads = kRows + 32;
+
+template <int W>
+__device__ __forceinline__ uint32_t swz(uint32_t logical) {
+  constexpr uint32_t mask = W == 128 ? 7u : W == 64 ? 3u : W == 32 ? 1u : 0u;
+  return logical ^ (((logical >> 7) & mask) << 4);
+}
+
+template <int EPI>
+__device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, uint32_t c, const Digest& dg, const Digest& old) {
+  if (EPI == EPI_HASH) {
+    st_digest(a.out + c, dg);
+    return;
+  }
+  if (EPI == EPI_BASIC) {
+    uint8_t changed = 1;
+    if (!a.basic_first && digest_eq(dg, old)) changed = 0;
+    if (changed) st_digest(a.prev + c, dg);
+    a.labels[c] = changed;
+    return;
+  }
+  if (EPI == EPI_TREE) {
+    const uint32_t node = a.leaf_base + c;
+    uint8_t label;
+    if (digest_eq(dg, old)) {
+      // FIXED_DUPL.  The reference also calls insert() here; that insert always
+      // finds the digest (every earlier leaf digest was inserted) and changes
+      // nothing, so it is skipped.
+      label = FIXED_DUPL;
+    } else {
+      uint64_t slot = 0;
+      int r = map_insert(a.map, dg, node, a.cur, a.epoch, &slot, a.err);
+      label = SHIFT_DUPL;
+      if (r == INS_NEW) {
+        label = FIRST_OCUR;
+        a.chunk_slot[c] = (uint32_t)slot;
+      } else if (r == INS_EXISTING) {
+        MapSlot* s = &a.map.slots[slot];
+        if (__ldcg(&s->tree) == a.cur) {
+          atomicMin(&s->node, node);  // lowest offset wins
+          label = FIRST_OCUR;
+          a.chunk_slot[c] = (uint32_t)slot;
+        }
+      }
+      st_digest(a.prev + c, dg);
+    }
+    a.labels[c] = label;
+    return;
+  }
+  if (EPI == EPI_LIST) {
+    uint8_t label = DONE;  // unchanged chunk
+    if (!digest_eq(dg, old)) {
+      uint64_t slot = 0;
+      int r = map_insert(a.map, dg, c, a.cur, a.epoch, &slot, a.err);
+      label = SHIFT_DUPL;
+      if (r == INS_NEW) {
+        label = FIRST_OCUR;
+      } else if (r == INS_EXISTING) {
+        MapSlot* s = &a.map.slots[slot];
+        // a serial backend gives the digest to the lowest changed chunk of this pass
+        if (__ldcg(&s->epoch) == a.epoch) { atomicMin(&s->node, c); label = FIRST_OCUR; }
+      }
+      a.chunk_slot[c] = (uint32_t)slot;
+      st_digest(a.prev + c, dg);
+    }
+    a.labels[c] = label;
+  }
+}
+
+template <int EPI>
+__device__ __forceinline__ bool needs_old(const LeafArgs& a) {
+  return EPI != EPI_HASH && !(EPI == EPI_BASIC && a.basic_first);
+}
+
+// ---------------------------------------------------------------------------
+// TMA pipeline kernel.
+// ---------------------------------------------------------------------------
+template <int HK, int EPI, int W>
+__global__ void __launch_bounds__(kThreads) leaf_tma_kernel(const __grid_constant__ CUtensorMap tmap, LeafArgs a,
+                                                            uint32_t n_full) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t kStageBytes = kRows * W;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  const int tid = threadIdx.x;
+  const uint32_t xsteps = a.cs / W;
+  const uint32_t ntiles = (n_full + kRows - 1) / kRows;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kRows / 32);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  if (tid >= kRows) {
+    // producer warp: one elected lane issues every box in consumption order
+    if (tid == kRows) {
+      tma_prefetch_desc(&tmap);
+      uint32_t it = 0;
+      bool ok = true;
+      for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (uint32_t xs = 0; xs < xsteps; xs++, it++) {
+          const uint32_t s = it % kStages, ph = (it / kStages) & 1;
+          if (!mbar_wait(&empty[s], ph ^ 1)) { atomicOr(a.err, DERR_SPIN); ok = false; break; }
+          mbar_arrive_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(smem + s * kStageBytes, &tmap, (int32_t)(xs * W), (int32_t)(tile * kRows), &full[s]);
+        }
+      }
+      // drain: every issued box must land before the CTA may exit
+      uint32_t first = it > (uint32_t)kStages ? it - kStages : 0;
+      for (uint32_t j = first; j < it; j++) mbar_wait(&full[j % kStages], (j / kStages) & 1);
+    }
+    return;
+  }
+
+  const uint32_t lane = tid & 31;
+  uint32_t it = 0;
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t c = tile * kRows + tid;
+    const bool valid = c < n_full;
+    Digest old{{0, 0, 0, 0}};
+    if (valid && needs_old<EPI>(a)) old = ld_digest(a.prev + c);
+    Murmur3State mm;
+    Md5State md;
+    if (HK == HASH_MD5) md.init(); else mm.init();
+    uint32_t X[16];
+    for (uint32_t xs = 0; xs < xsteps; xs++, it++) {
+      const uint32_t s = it % kStages, ph = (it / kStages) & 1;
+      if (!mbar_wait(&full[s], ph)) { atomicOr(a.err, DERR_SPIN); return; }
+      const uint8_t* stage = smem + s * kStageBytes;
+      const uint32_t rowbase = (uint32_t)tid * W;
+      if (HK == HASH_MD5) {
+        if (W >= 64) {
+#pragma unroll
+          for (int blk = 0; blk < W / 64; blk++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              uint4 v = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + blk * 64 + q * 16));
+              X[4 * q] = v.x; X[4 * q + 1] = v.y; X[4 * q + 2] = v.z; X[4 * q + 3] = v.w;
+            }
+            md.block(X);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; i++) X[i] = 0;
+#pragma unroll
+          for (int q = 0; q < W / 16; q++) {
+            uint4 v = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + q * 16));
+            X[4 * q] = v.x; X[4 * q + 1] = v.y; X[4 * q + 2] = v.z; X[4 * q + 3] = v.w;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < W / 16; q++) {
+          uint4 v = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + q * 16));
+          mm.block(v.x, v.y, v.z, v.w);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+    }
+    if (valid) {
+      Digest dg;
+      if (HK == HASH_MD5) {
+        if (W >= 64) {
+#pragma unroll
+          for (int i = 0; i < 16; i++) X[i] = 0;
+          dg = md.finish(X, 0, a.cs);
+        } else {
+          dg = md.finish(X, a.cs, a.cs);
+        }
+      } else {
+        dg = mm.finish(a.cs);
+      }
+      leaf_epilogue<EPI>(a, c, dg, old);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Thread-per-chunk kernel reading global memory directly, for chunks
+// [c0, c1).
+// ---------------------------------------------------------------------------
+template <int EPI>
+__global__ void leaf_direct_kernel(LeafArgs a, uint32_t c0, uint32_t c1) {
+  for (uint64_t c = c0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < c1; c += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t off = c * (uint64_t)a.cs;
+    uint64_t nb = a.cs;
+    if (c == a.n_chunks - 1) nb = a.len - off;
+    Digest old{{0, 0, 0, 0}};
+    if (needs_old<EPI>(a)) old = ld_digest(a.prev + c);
+    Digest dg = hash_bytes(a.hash_kind, a.data + off, nb);
+    leaf_epilogue<EPI>(a, (uint32_t)c, dg, old);
+  }
+}
+
+__global__ void tree_leaf_finalize_kernel(LeafArgs a) {
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n_chunks; c += (uint64_t)gridDim.x * blockDim.x) {
+    if (a.labels[c] == FIRST_OCUR) {
+      const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
+      if (s->tree == a.cur && s->node != a.leaf_base + (uint32_t)c) a.labels[c] = SHIFT_DUPL;
+    }
+  }
+}
+
+__global__ void list_finalize_kernel(LeafArgs a) {
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n_chunks; c += (uint64_t)gridDim.x * blockDim.x) {
+    if (a.labels[c] == FIRST_OCUR) {
+      const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
+      if (s->node != (uint32_t)c) a.labels[c] = SHIFT_DUPL;
+    }
+  }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+int tma_width(uint32_t cs) {
+  if (cs % 128 == 0) return 128;
+  if (cs == 64 || cs == 32 || cs == 16) return (int)cs;
+  return 0;
+}
+
+bool make_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, int W, uint32_t n_full) {
+  if (c->ptr == data && c->len == len && c->cs == cs && c->width == W) return true;
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {cs, n_full};
+  cuuint64_t strides[1] = {cs};
+  cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)kRows};
+  cuuint32_t estr[2] = {1, 1};
+  CUtensorMapSwizzle sw = W == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                        : W == 64  ? CU_TENSOR_MAP_SWIZZLE_64B
+                        : W == 32  ? CU_TENSOR_MAP_SWIZZLE_32B
+                                   : CU_TENSOR_MAP_SWIZZLE_NONE;
+  CUresult r = fn(&c->map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(data), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) { c->ptr = nullptr; return false; }
+  c->ptr = data; c->len = len; c->cs = cs; c->width = W;
+  return true;
+}
+
+template <int HK, int EPI, int W>
+cudaError_t launch_tma_t(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, cudaStream_t s) {
+  auto k = leaf_tma_kernel<HK, EPI, W>;
+  const size_t smem = 1024 + (size_t)kStages * kRows * W + 2 * kStages * sizeof(uint64_t);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const uint32_t ntiles = (n_full + kRows - 1) / kRows;
+  int per_sm = W >= 128 ? 2 : 3;
+  uint32_t grid = (uint32_t)(num_sms() * per_sm);
+  if (grid > ntiles) grid = ntiles;
+  k<<<grid, kThreads, smem, s>>>(m, a, n_full);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <int HK, int EPI>
+cudaError_t launch_tma_w(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, cudaStream_t s) {
+  switch (W) {
+    case 128: return launch_tma_t<HK, EPI, 128>(a, m, n_full, s);
+    case 64: return launch_tma_t<HK, EPI, 64>(a, m, n_full, s);
+    case 32: return launch_tma_t<HK, EPI, 32>(a, m, n_full, s);
+    default: return launch_tma_t<HK, EPI, 16>(a, m, n_full, s);
+  }
+}
+
+template <int EPI>
+cudaError_t launch_tma_e(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, cudaStream_t s) {
+  if (a.hash_kind == HASH_MD5) return launch_tma_w<HASH_MD5, EPI>(a, m, n_full, W, s);
+  return launch_tma_w<HASH_MURMUR3, EPI>(a, m, n_full, W, s);
+}
+
+template <int EPI>
+cudaError_t launch_direct(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStream_t s) {
+  if (c1 <= c0) return cudaSuccess;
+  uint64_t n = c1 - c0;
+  uint32_t grid = (uint32_t)((n + 127) / 128);
+  uint32_t cap = (uint32_t)num_sms() * 16;
+  if (grid > cap) grid = cap;
+  leaf_direct_kernel<EPI><<<grid, 128, 0, s>>>(a, c0, c1);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t dispatch_direct(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStream_t s) {
+  switch (a.epi) {
+    case EPI_TREE: return launch_direct<EPI_TREE>(a, c0, c1, s);
+    case EPI_LIST: return launch_direct<EPI_LIST>(a, c0, c1, s);
+    case EPI_BASIC: return launch_direct<EPI_BASIC>(a, c0, c1, s);
+    default: return launch_direct<EPI_HASH>(a, c0, c1, s);
+  }
+}
+cudaError_t dispatch_tma(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, cudaStream_t s) {
+  switch (a.epi) {
+    case EPI_TREE: return launch_tma_e<EPI_TREE>(a, m, n_full, W, s);
+    case EPI_LIST: return launch_tma_e<EPI_LIST>(a, m, n_full, W, s);
+    case EPI_BASIC: return launch_tma_e<EPI_BASIC>(a, m, n_full, W, s);
+    default: return launch_tma_e<EPI_HASH>(a, m, n_full, W, s);
+  }
+}
+}  // namespace
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s) {
+  if (a.n_chunks == 0) return cudaSuccess;
+  const uint32_t n_full = (uint32_t)(a.len / a.cs);
+  const int W = tma_width(a.cs);
+  const bool aligned = (reinterpret_cast<uintptr_t>(a.data) & 15) == 0;
+  uint32_t done = 0;
+  if (W && aligned && n_full > 0 && cache && make_tmap(cache, a.data, a.len, a.cs, W, n_full)) {
+    cudaError_t e = dispatch_tma(a, cache->map, n_full, W, s);
+    if (e != cudaSuccess) return e;
+    done = n_full;
+  }
+  return dispatch_direct(a, done, a.n_chunks, s);
+}
+
+cudaError_t launch_tree_leaf_finalize(const LeafArgs& a, cudaStream_t s) {
+  uint32_t grid = (uint32_t)((a.n_chunks + 255) / 256);
+  uint32_t cap = (uint32_t)num_sms() * 8;
+  if (grid > cap) grid = cap;
+  if (grid == 0) return cudaSuccess;
+  tree_leaf_finalize_kernel<<<grid, 256, 0, s>>>(a);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_list_finalize(const LeafArgs& a, cudaStream_t s) {
+  uint32_t grid = (uint32_t)((a.n_chunks + 255) / 256);
+  uint32_t cap = (uint32_t)num_sms() * 8;
+  if (grid > cap) grid = cap;
+  if (grid == 0) return cudaSuccess;
+  list_finalize_kernel<<<grid, 256, 0, s>>>(a);
+  note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace mtc

@@ -1,0 +1,351 @@
+// mtc_common.cuh -- device-side building blocks shared by every kernel of the
+// deduplicator: the two digest functions, the digest -> NodeID open-addressing
+// map, the Merkle-tree index arithmetic and the device error word.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mtc {
+
+// Label values of the reference (include/utils.hpp:51-57).
+enum : uint8_t { FIRST_OCUR = 0, FIXED_DUPL = 1, SHIFT_DUPL = 2, FIRST_DUPL = 3, DONE = 4 };
+// Root flags written by the forest passes.
+enum : uint8_t { ROOT_NONE = 0, ROOT_FO = 1, ROOT_SHIFT = 2 };
+enum : int { HASH_MURMUR3 = 0, HASH_MD5 = 1 };
+
+// Bits of the per-handle device error word.
+enum : uint32_t {
+  DERR_MAP_FULL = 1u << 0,      // probe sequence wrapped: table full
+  DERR_SPIN = 1u << 1,          // bounded wait on a slot being published ran out
+  DERR_FO_MISMATCH = 1u << 2,   // a first-occurrence root is not its digest's owner
+  DERR_CAPACITY = 1u << 3,      // diff larger than the device staging buffer
+  DERR_MISSING = 1u << 4,       // a root digest is absent from the map
+  DERR_RANGE = 1u << 5,         // restart metadata out of range
+};
+
+struct __align__(16) Digest { uint32_t w[4]; };
+
+__device__ __forceinline__ bool digest_eq(const Digest& a, const Digest& b) {
+  return ((a.w[0] ^ b.w[0]) | (a.w[1] ^ b.w[1]) | (a.w[2] ^ b.w[2]) | (a.w[3] ^ b.w[3])) == 0;
+}
+__device__ __forceinline__ Digest ld_digest(const Digest* p) {
+  uint4 v = *reinterpret_cast<const uint4*>(p);
+  return Digest{{v.x, v.y, v.z, v.w}};
+}
+__device__ __forceinline__ void st_digest(Digest* p, const Digest& d) {
+  *reinterpret_cast<uint4*>(p) = make_uint4(d.w[0], d.w[1], d.w[2], d.w[3]);
+}
+
+// ---------------------------------------------------------------------------
+// Murmur3 variant of the reference (include/kokkos_murmur3.hpp:213-292):
+// MurmurHash3_x64_128 with seed 0 in which rotl64 returns uint32_t, so each
+// rotated value is truncated to its low 32 bits before further use.
+// ---------------------------------------------------------------------------
+#define MTC_HD __host__ __device__ __forceinline__
+struct Murmur3State {
+  uint64_t h1, h2;
+  MTC_HD void init() { h1 = 0; h2 = 0; }
+  MTC_HD static uint32_t rotl_lo(uint64_t x, int r) {
+    // low 32 bits of the 64-bit rotation
+    return (uint32_t)((x << r) | (x >> (64 - r)));
+  }
+  // one 16-byte body block given as four little-endian words
+  MTC_HD void block(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
+    const uint64_t c1 = 0x87c37b91114253d5ull, c2 = 0x4cf5ad432745937full;
+    uint64_t k1 = ((uint64_t)w1 << 32) | w0;
+    uint64_t k2 = ((uint64_t)w3 << 32) | w2;
+    k1 *= c1; k1 = rotl_lo(k1, 31); k1 *= c2; h1 ^= k1;
+    h1 = rotl_lo(h1, 27); h1 += h2; h1 = h1 * 5 + 0x52dce729;
+    k2 *= c2; k2 = rotl_lo(k2, 33); k2 *= c1; h2 ^= k2;
+    h2 = rotl_lo(h2, 31); h2 += h1; h2 = h2 * 5 + 0x38495ab5;
+  }
+  // tail of `rem` (1..15) bytes packed little-endian in t0 (bytes 0..7) and t1 (8..15)
+  MTC_HD void tail(uint64_t t0, uint64_t t1, unsigned rem) {
+    const uint64_t c1 = 0x87c37b91114253d5ull, c2 = 0x4cf5ad432745937full;
+    if (rem > 8) {
+      uint64_t k2 = t1; k2 *= c2; k2 = rotl_lo(k2, 33); k2 *= c1; h2 ^= k2;
+    }
+    if (rem > 0) {
+      uint64_t k1 = t0; k1 *= c1; k1 = rotl_lo(k1, 31); k1 *= c2; h1 ^= k1;
+    }
+  }
+  MTC_HD static uint64_t fmix64(uint64_t k) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33; return k;
+  }
+  MTC_HD Digest finish(uint64_t len) {
+    uint64_t a = h1 ^ len, b = h2 ^ len;
+    a += b; b += a;
+    a = fmix64(a); b = fmix64(b);
+    a += b; b += a;
+    return Digest{{(uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32)}};
+  }
+};
+
+// ---------------------------------------------------------------------------
+// MD5 (RFC 1321) as computed by the reference for inputs of at most INT_MAX
+// bytes (include/kokkos_md5.hpp:61-265).  Round constants are the RFC's
+// floor(abs(sin(i+1)) * 2^32) table.
+// ---------------------------------------------------------------------------
+struct Md5State {
+  uint32_t a, b, c, d;
+  MTC_HD void init() { a = 0x67452301u; b = 0xefcdab89u; c = 0x98badcfeu; d = 0x10325476u; }
+  MTC_HD static uint32_t rol(uint32_t x, int n) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(x, x, n);
+#else
+    return (x << n) | (x >> (32 - n));
+#endif
+  }
+#define MTC_MD5_STEP(F, A, B, C, D, X, S, T) A = B + rol(A + (F) + (X) + (T), S)
+  MTC_HD void block(const uint32_t* X) {
+    uint32_t A = a, B = b, C = c, D = d;
+#define F1(x, y, z) ((z) ^ ((x) & ((y) ^ (z))))
+#define F2(x, y, z) ((y) ^ ((z) & ((x) ^ (y))))
+#define F3(x, y, z) ((x) ^ (y) ^ (z))
+#define F4(x, y, z) ((y) ^ ((x) | ~(z)))
+    MTC_MD5_STEP(F1(B,C,D), A, B, C, D, X[0], 7, 0xd76aa478u);  MTC_MD5_STEP(F1(A,B,C), D, A, B, C, X[1], 12, 0xe8c7b756u);
+    MTC_MD5_STEP(F1(D,A,B), C, D, A, B, X[2], 17, 0x242070dbu); MTC_MD5_STEP(F1(C,D,A), B, C, D, A, X[3], 22, 0xc1bdceeeu);
+    MTC_MD5_STEP(F1(B,C,D), A, B, C, D, X[4], 7, 0xf57c0fafu);  MTC_MD5_STEP(F1(A,B,C), D, A, B, C, X[5], 12, 0x4787c62au);
+    MTC_MD5_STEP(F1(D,A,B), C, D, A, B, X[6], 17, 0xa8304613u); MTC_MD5_STEP(F1(C,D,A), B, C, D, A, X[7], 22, 0xfd469501u);
+    MTC_MD5_STEP(F1(B,C,D), A, B, C, D, X[8], 7, 0x698098d8u);  MTC_MD5_STEP(F1(A,B,C), D, A, B, C, X[9], 12, 0x8b44f7afu);
+    MTC_MD5_STEP(F1(D,A,B), C, D, A, B, X[10], 17, 0xffff5bb1u); MTC_MD5_STEP(F1(C,D,A), B, C, D, A, X[11], 22, 0x895cd7beu);
+    MTC_MD5_STEP(F1(B,C,D), A, B, C, D, X[12], 7, 0x6b901122u); MTC_MD5_STEP(F1(A,B,C), D, A, B, C, X[13], 12, 0xfd987193u);
+    MTC_MD5_STEP(F1(D,A,B), C, D, A, B, X[14], 17, 0xa679438eu); MTC_MD5_STEP(F1(C,D,A), B, C, D, A, X[15], 22, 0x49b40821u);
+
+    MTC_MD5_STEP(F2(B,C,D), A, B, C, D, X[1], 5, 0xf61e2562u);  MTC_MD5_STEP(F2(A,B,C), D, A, B, C, X[6], 9, 0xc040b340u);
+    MTC_MD5_STEP(F2(D,A,B), C, D, A, B, X[11], 14, 0x265e5a51u); MTC_MD5_STEP(F2(C,D,A), B, C, D, A, X[0], 20, 0xe9b6c7aau);
+    MTC_MD5_STEP(F2(B,C,D), A, B, C, D, X[5], 5, 0xd62f105du);  MTC_MD5_STEP(F2(A,B,C), D, A, B, C, X[10], 9, 0x02441453u);
+    MTC_MD5_STEP(F2(D,A,B), C, D, A, B, X[15], 14, 0xd8a1e681u); MTC_MD5_STEP(F2(C,D,A), B, C, D, A, X[4], 20, 0xe7d3fbc8u);
+    MTC_MD5_STEP(F2(B,C,D), A, B, C, D, X[9], 5, 0x21e1cde6u);  MTC_MD5_STEP(F2(A,B,C), D, A, B, C, X[14], 9, 0xc33707d6u);
+    MTC_MD5_STEP(F2(D,A,B), C, D, A, B, X[3], 14, 0xf4d50d87u); MTC_MD5_STEP(F2(C,D,A), B, C, D, A, X[8], 20, 0x455a14edu);
+    MTC_MD5_STEP(F2(B,C,D), A, B, C, D, X[13], 5, 0xa9e3e905u); MTC_MD5_STEP(F2(A,B,C), D, A, B, C, X[2], 9, 0xfcefa3f8u);
+    MTC_MD5_STEP(F2(D,A,B), C, D, A, B, X[7], 14, 0x676f02d9u); MTC_MD5_STEP(F2(C,D,A), B, C, D, A, X[12], 20, 0x8d2a4c8au);
+
+    MTC_MD5_STEP(F3(B,C,D), A, B, C, D, X[5], 4, 0xfffa3942u);  MTC_MD5_STEP(F3(A,B,C), D, A, B, C, X[8], 11, 0x8771f681u);
+    MTC_MD5_STEP(F3(D,A,B), C, D, A, B, X[11], 16, 0x6d9d6122u); MTC_MD5_STEP(F3(C,D,A), B, C, D, A, X[14], 23, 0xfde5380cu);
+    MTC_MD5_STEP(F3(B,C,D), A, B, C, D, X[1], 4, 0xa4beea44u);  MTC_MD5_STEP(F3(A,B,C), D, A, B, C, X[4], 11, 0x4bdecfa9u);
+    MTC_MD5_STEP(F3(D,A,B), C, D, A, B, X[7], 16, 0xf6bb4b60u); MTC_MD5_STEP(F3(C,D,A), B, C, D, A, X[10], 23, 0xbebfbc70u);
+    MTC_MD5_STEP(F3(B,C,D), A, B, C, D, X[13], 4, 0x289b7ec6u); MTC_MD5_STEP(F3(A,B,C), D, A, B, C, X[0], 11, 0xeaa127fau);
+    MTC_MD5_STEP(F3(D,A,B), C, D, A, B, X[3], 16, 0xd4ef3085u); MTC_MD5_STEP(F3(C,D,A), B, C, D, A, X[6], 23, 0x04881d05u);
+    MTC_MD5_STEP(F3(B,C,D), A, B, C, D, X[9], 4, 0xd9d4d039u);  MTC_MD5_STEP(F3(A,B,C), D, A, B, C, X[12], 11, 0xe6db99e5u);
+    MTC_MD5_STEP(F3(D,A,B), C, D, A, B, X[15], 16, 0x1fa27cf8u); MTC_MD5_STEP(F3(C,D,A), B, C, D, A, X[2], 23, 0xc4ac5665u);
+
+    MTC_MD5_STEP(F4(B,C,D), A, B, C, D, X[0], 6, 0xf4292244u);  MTC_MD5_STEP(F4(A,B,C), D, A, B, C, X[7], 10, 0x432aff97u);
+    MTC_MD5_STEP(F4(D,A,B), C, D, A, B, X[14], 15, 0xab9423a7u); MTC_MD5_STEP(F4(C,D,A), B, C, D, A, X[5], 21, 0xfc93a039u);
+    MTC_MD5_STEP(F4(B,C,D), A, B, C, D, X[12], 6, 0x655b59c3u); MTC_MD5_STEP(F4(A,B,C), D, A, B, C, X[3], 10, 0x8f0ccc92u);
+    MTC_MD5_STEP(F4(D,A,B), C, D, A, B, X[10], 15, 0xffeff47du); MTC_MD5_STEP(F4(C,D,A), B, C, D, A, X[1], 21, 0x85845dd1u);
+    MTC_MD5_STEP(F4(B,C,D), A, B, C, D, X[8], 6, 0x6fa87e4fu);  MTC_MD5_STEP(F4(A,B,C), D, A, B, C, X[15], 10, 0xfe2ce6e0u);
+    MTC_MD5_STEP(F4(D,A,B), C, D, A, B, X[6], 15, 0xa3014314u); MTC_MD5_STEP(F4(C,D,A), B, C, D, A, X[13], 21, 0x4e0811a1u);
+    MTC_MD5_STEP(F4(B,C,D), A, B, C, D, X[4], 6, 0xf7537e82u);  MTC_MD5_STEP(F4(A,B,C), D, A, B, C, X[11], 10, 0xbd3af235u);
+    MTC_MD5_STEP(F4(D,A,B), C, D, A, B, X[2], 15, 0x2ad7d2bbu); MTC_MD5_STEP(F4(C,D,A), B, C, D, A, X[9], 21, 0xeb86d391u);
+#undef F1
+#undef F2
+#undef F3
+#undef F4
+    a += A; b += B; c += C; d += D;
+  }
+#undef MTC_MD5_STEP
+  // Final padding for a message of `len` bytes whose last `rem` (< 64) bytes
+  // are in words tw[0..15] (zero beyond rem, little-endian).
+  MTC_HD Digest finish(uint32_t* tw, uint32_t rem, uint64_t len) {
+    // append 0x80 at byte `rem`
+    tw[rem >> 2] |= 0x80u << (8 * (rem & 3));
+    if (rem >= 56) {
+      block(tw);
+#pragma unroll
+      for (int i = 0; i < 16; i++) tw[i] = 0;
+    }
+    uint64_t bits = len << 3;
+    tw[14] = (uint32_t)bits; tw[15] = (uint32_t)(bits >> 32);
+    block(tw);
+    return Digest{{a, b, c, d}};
+  }
+};
+
+// Digest of one 32-byte interior node: hash(left || right)
+// (src/tree_approach.cpp:131, :221, :389, :459).
+__device__ __forceinline__ Digest hash_pair(int kind, const Digest& l, const Digest& r) {
+  if (kind == HASH_MD5) {
+    Md5State s; s.init();
+    uint32_t X[16] = {l.w[0], l.w[1], l.w[2], l.w[3], r.w[0], r.w[1], r.w[2], r.w[3], 0, 0, 0, 0, 0, 0, 0, 0};
+    return s.finish(X, 32, 32);
+  }
+  Murmur3State s; s.init();
+  s.block(l.w[0], l.w[1], l.w[2], l.w[3]);
+  s.block(r.w[0], r.w[1], r.w[2], r.w[3]);
+  return s.finish(32);
+}
+
+// Digest of `len` bytes at an arbitrary global address, one thread (any
+// alignment; used for short, odd-sized and tail chunks).
+__device__ __forceinline__ uint32_t ld_word_any(const uint8_t* p, uint64_t off, uint64_t len) {
+  uint32_t w = 0;
+#pragma unroll
+  for (int b = 0; b < 4; b++) if (off + b < len) w |= (uint32_t)__ldg(p + off + b) << (8 * b);
+  return w;
+}
+__device__ inline Digest hash_bytes(int kind, const uint8_t* p, uint64_t len) {
+  const bool al4 = ((reinterpret_cast<uintptr_t>(p) & 3) == 0);
+  auto word = [&](uint64_t off) -> uint32_t {
+    if (al4 && off + 4 <= len) return __ldg(reinterpret_cast<const uint32_t*>(p + off));
+    return ld_word_any(p, off, len);
+  };
+  if (kind == HASH_MD5) {
+    Md5State s; s.init();
+    uint32_t X[16];
+    uint64_t off = 0;
+    for (; off + 64 <= len; off += 64) {
+#pragma unroll
+      for (int i = 0; i < 16; i++) X[i] = word(off + 4 * i);
+      s.block(X);
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) X[i] = word(off + 4 * i);
+    return s.finish(X, (uint32_t)(len - off), len);
+  }
+  Murmur3State s; s.init();
+  uint64_t off = 0;
+  for (; off + 16 <= len; off += 16) s.block(word(off), word(off + 4), word(off + 8), word(off + 12));
+  unsigned rem = (unsigned)(len - off);
+  uint64_t t0 = ((uint64_t)word(off + 4) << 32) | word(off);
+  uint64_t t1 = ((uint64_t)word(off + 12) << 32) | word(off + 8);
+  s.tail(t0, t1, rem);
+  return s.finish(len);
+}
+
+// ---------------------------------------------------------------------------
+// Merkle heap index arithmetic, include/kokkos_merkle_tree.hpp:102-142
+// (exact only for a power-of-two leaf count; restated as written).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ void leaf_range(uint32_t node, uint32_t num_nodes, uint32_t& lo, uint32_t& hi) {
+  uint32_t l = 2 * node + 1, r = 2 * node + 2;
+  while (l < num_nodes) { l = 2 * l + 1; r = 2 * r + 2; }
+  l = (l - 1) / 2; r = (r - 2) / 2;
+  if (r > num_nodes) r = num_nodes - 1;
+  lo = l; hi = r;
+}
+__host__ __device__ __forceinline__ uint32_t num_leaf_descendents(uint32_t node, uint32_t num_nodes) {
+  uint32_t l, r; leaf_range(node, num_nodes, l, r); return r - l + 1;
+}
+__host__ __device__ __forceinline__ uint32_t leftmost_leaf(uint32_t node, uint32_t num_nodes) {
+  uint32_t l, r; leaf_range(node, num_nodes, l, r); return l;
+}
+
+// ---------------------------------------------------------------------------
+// Digest -> NodeID map (the reference's DigestNodeIDDeviceMap,
+// include/map_helpers.hpp:105-110, with Kokkos::UnorderedMap's
+// insert-if-absent semantics).  Open addressing, linear probing, 32-byte
+// slots.  A slot is claimed by CAS on `state` (0 empty, 1 being written,
+// 2 published); waits on state 1 are bounded and raise DERR_SPIN.
+// `epoch` identifies the launch that inserted the entry, which gives the
+// serial "first insert wins" order between launches and "lowest node wins"
+// among the inserts of one launch.
+// ---------------------------------------------------------------------------
+struct __align__(32) MapSlot {
+  uint32_t key[4];
+  uint32_t node, tree, epoch, state;
+};
+struct DigestMap {
+  MapSlot* slots;
+  uint64_t mask;       // capacity - 1 (capacity a power of two)
+  uint32_t* size;      // number of published entries
+};
+
+enum : int { INS_FAILED = 0, INS_NEW = 1, INS_EXISTING = 2 };
+constexpr int kSpinLimit = 1 << 20;
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t slot_of(const Digest& k, uint64_t mask) {
+  uint64_t a = ((uint64_t)k.w[1] << 32) | k.w[0];
+  a ^= a >> 29; a *= 0xbf58476d1ce4e5b9ull; a ^= a >> 32;
+  return a & mask;
+}
+__device__ __forceinline__ bool slot_key_eq(const MapSlot* s, const Digest& k) {
+  uint4 v = __ldcg(reinterpret_cast<const uint4*>(s->key));
+  return ((v.x ^ k.w[0]) | (v.y ^ k.w[1]) | (v.z ^ k.w[2]) | (v.w ^ k.w[3])) == 0;
+}
+// Wait until slot state leaves 1; returns the state or 0xffffffff on timeout.
+__device__ __forceinline__ uint32_t wait_published(MapSlot* s, uint32_t st, uint32_t* err) {
+  int spins = 0;
+  while (st == 1) {
+    if (++spins > kSpinLimit) { atomicOr(err, DERR_SPIN); return 0xffffffffu; }
+    __nanosleep(32);
+    st = ld_acquire_u32(&s->state);
+  }
+  return st;
+}
+
+// Insert (key -> node, tree, epoch) if absent.  Returns INS_NEW / INS_EXISTING
+// with *slot set, or INS_FAILED (error word set).
+__device__ inline int map_insert(const DigestMap& m, const Digest& k, uint32_t node, uint32_t tree, uint32_t epoch,
+                                 uint64_t* slot, uint32_t* err) {
+  uint64_t i = slot_of(k, m.mask);
+  for (uint64_t probe = 0; probe <= m.mask; probe++) {
+    MapSlot* s = &m.slots[i];
+    uint32_t st = ld_acquire_u32(&s->state);
+    if (st == 0) {
+      uint32_t old = atomicCAS(&s->state, 0u, 1u);
+      if (old == 0) {
+        *reinterpret_cast<uint4*>(s->key) = make_uint4(k.w[0], k.w[1], k.w[2], k.w[3]);
+        s->node = node; s->tree = tree; s->epoch = epoch;
+        st_release_u32(&s->state, 2u);
+        atomicAdd(m.size, 1u);
+        *slot = i;
+        return INS_NEW;
+      }
+      st = old;
+    }
+    st = wait_published(s, st, err);
+    if (st == 0xffffffffu) return INS_FAILED;
+    if (slot_key_eq(s, k)) { *slot = i; return INS_EXISTING; }
+    i = (i + 1) & m.mask;
+  }
+  atomicOr(err, DERR_MAP_FULL);
+  return INS_FAILED;
+}
+
+// Slot index of key, or -1.
+__device__ inline int64_t map_find(const DigestMap& m, const Digest& k, uint32_t* err) {
+  uint64_t i = slot_of(k, m.mask);
+  for (uint64_t probe = 0; probe <= m.mask; probe++) {
+    MapSlot* s = &m.slots[i];
+    uint32_t st = ld_acquire_u32(&s->state);
+    if (st == 0) return -1;
+    st = wait_published(s, st, err);
+    if (st == 0xffffffffu) return -1;
+    if (slot_key_eq(s, k)) return (int64_t)i;
+    i = (i + 1) & m.mask;
+  }
+  return -1;
+}
+
+// Insert with the serial order of one reference launch: an entry created by an
+// earlier launch is kept; among inserts of this launch the lowest node wins.
+__device__ inline void map_insert_first(const DigestMap& m, const Digest& k, uint32_t node, uint32_t tree,
+                                        uint32_t epoch, uint32_t* err) {
+  uint64_t slot;
+  int r = map_insert(m, k, node, tree, epoch, &slot, err);
+  if (r == INS_EXISTING) {
+    MapSlot* s = &m.slots[slot];
+    if (__ldcg(&s->epoch) == epoch) atomicMin(&s->node, node);
+  }
+}
+
+// Plain read of a slot's value after the launch that wrote it has finished.
+struct NodeIdDev { uint32_t node, tree; };
+__device__ __forceinline__ NodeIdDev slot_value(const DigestMap& m, int64_t slot) {
+  if (slot < 0) return NodeIdDev{0xffffffffu, 0xffffffffu};
+  const MapSlot* s = &m.slots[slot];
+  return NodeIdDev{s->node, s->tree};
+}
+
+}  // namespace mtc

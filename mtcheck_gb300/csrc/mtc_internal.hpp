@@ -1,0 +1,64 @@
+// mtc_internal.hpp -- host-side declarations shared by the translation units
+// of the library (kernel launchers and their argument blocks).  Not part of
+// the public interface (see include/mtcheck.h and include/mtcheck/*.hpp).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda.h>
+
+#include "mtc_common.cuh"
+
+namespace mtc {
+
+// Per-chunk epilogue of the leaf kernel.
+enum LeafEpi : int {
+  EPI_HASH = 0,   // write the digest only
+  EPI_TREE = 1,   // TreeDeduplicator leaves (src/tree_approach.cpp:57-94, :309-351)
+  EPI_LIST = 2,   // ListDeduplicator::dedup_data (src/list_approach.cpp:38-61)
+  EPI_BASIC = 3,  // BasicDeduplicator::dedup_data (src/basic_approach.cpp:25-46)
+};
+
+struct LeafArgs {
+  const uint8_t* data = nullptr;  // device buffer being checkpointed
+  uint64_t len = 0;               // bytes
+  uint32_t cs = 0;                // chunk size
+  uint32_t n_chunks = 0;          // ceil(len / cs)
+  Digest* prev = nullptr;         // per-chunk digest of the previous checkpoint (tree leaves or hash list)
+  uint8_t* labels = nullptr;      // per-chunk label / changed flag out
+  uint32_t* chunk_slot = nullptr; // per-chunk map slot of a changed chunk
+  Digest* out = nullptr;          // EPI_HASH output
+  DigestMap map{};
+  uint32_t cur = 0;               // current checkpoint id
+  uint32_t epoch = 0;             // launch epoch for the map's first-insert order
+  uint32_t leaf_base = 0;         // node id of chunk 0 (N-1 for the tree, 0 for the list)
+  uint32_t* err = nullptr;        // device error word
+  int hash_kind = HASH_MURMUR3;
+  int epi = EPI_HASH;
+  int basic_first = 0;            // basic approach with current_id == 0: every chunk changed
+};
+
+// Cached TMA descriptor for one (buffer, length, chunk size).
+struct TmaCache {
+  const void* ptr = nullptr;
+  uint64_t len = 0;
+  uint32_t cs = 0;
+  int width = 0;
+  CUtensorMap map;
+};
+
+// Launch the leaf hashing kernel(s) over every chunk.  Uses the TMA pipeline
+// for chunk sizes that are a multiple of 128 bytes (or 16/32/64) on 16-byte
+// aligned buffers, and a thread-per-chunk kernel otherwise and for the tail.
+cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s);
+// Tree: demote FIRST_OCUR leaves that do not own their digest (src/tree_approach.cpp:356-369).
+cudaError_t launch_tree_leaf_finalize(const LeafArgs& a, cudaStream_t s);
+// List: a changed chunk is a first occurrence only if it owns its digest.
+cudaError_t launch_list_finalize(const LeafArgs& a, cudaStream_t s);
+
+int num_sms();
+// Running count of kernel launches issued by the library (all handles).
+void note_launch(uint32_t n = 1);
+uint64_t launch_count();
+
+}  // namespace mtc

@@ -1,0 +1,115 @@
+"""ctypes binding of the C oracle (``oracle/mtc_oracle.c``).
+
+Test infrastructure: imported only by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py``.  The product library never loads it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FULL, BASIC, LIST, TREE, TREE_LOW_OFFSET_REF, TREE_LOW_OFFSET = 1, 2, 3, 4, 5, 6
+MURMUR3, MD5 = 0, 1
+APPROACH_NAMES = {FULL: "full", BASIC: "basic", LIST: "list", TREE: "tree",
+                  TREE_LOW_OFFSET_REF: "tree-low-offset-ref", TREE_LOW_OFFSET: "tree-low-offset"}
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = ctypes.CDLL(path)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint32]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_checkpoint.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
+        L.orc_free.argtypes = [ctypes.c_void_p]
+        L.orc_restart.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64),
+                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64]
+        L.orc_hash.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+        for f in ("orc_num_first_ocur", "orc_num_shift_dupl", "orc_current_id"):
+            getattr(L, f).restype = ctypes.c_uint32
+            getattr(L, f).argtypes = [ctypes.c_void_p]
+        L.orc_datasizes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+        L.orc_labels.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own hash headers compiled on this host, or None."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None:
+            return None
+        _ref = ctypes.CDLL(path)
+        for f in (_ref.ref_murmur3_hash, _ref.ref_md5_hash):
+            f.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+    return _ref
+
+
+def _buf(data):
+    a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray)) else data,
+                             dtype=np.uint8)
+    return a
+
+
+def digest(data, kind=MURMUR3):
+    a = _buf(data)
+    out = (ctypes.c_uint8 * 16)()
+    lib().orc_hash(kind, a.ctypes.data if a.size else None, a.size, out)
+    return bytes(out)
+
+
+class Deduplicator:
+    """Serial restatement of one reference deduplicator (tree/list/basic/full)."""
+
+    def __init__(self, approach, chunk_size, hash_kind=MURMUR3):
+        self.approach = approach
+        self.h = lib().orc_create(approach, hash_kind, chunk_size)
+        if not self.h:
+            raise ValueError("bad oracle arguments")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def checkpoint(self, data, make_baseline, increment=True):
+        a = _buf(data)
+        p = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        rc = lib().orc_checkpoint(self.h, a.ctypes.data, a.size, int(make_baseline), int(increment),
+                                  ctypes.byref(p), ctypes.byref(n))
+        if rc != 0:
+            raise RuntimeError(f"oracle checkpoint failed: {rc}")
+        out = ctypes.string_at(p.value, n.value)
+        lib().orc_free(p)
+        return out
+
+    def num_first_ocur(self):
+        return lib().orc_num_first_ocur(self.h)
+
+    def num_shift_dupl(self):
+        return lib().orc_num_shift_dupl(self.h)
+
+    def datasizes(self):
+        v = (ctypes.c_uint64 * 2)()
+        lib().orc_datasizes(self.h, v)
+        return int(v[0]), int(v[1])
+
+
+def restart(approach, diffs, chkpt_id, out):
+    """Restart checkpoint ``chkpt_id`` of ``diffs`` into the uint8 array ``out`` (in place)."""
+    bufs = [np.frombuffer(d, dtype=np.uint8) for d in diffs]
+    ptrs = (ctypes.c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+    lens = (ctypes.c_uint64 * len(bufs))(*[b.size for b in bufs])
+    rc = lib().orc_restart(approach, ptrs, lens, len(bufs), chkpt_id, out.ctypes.data, out.size)
+    return rc

@@ -1,0 +1,76 @@
+"""Regenerate the golden fixtures in this folder from the reference itself.
+
+* ``tree_kat.json``: the ten known-answer tests of the reference
+  (test/test_case_01.cpp .. test_case_10.cpp): the two 8-byte checkpoints
+  (chunk size 1), and the expected number of first-occurrence and
+  shifted-duplicate regions after the second checkpoint.  Parsed from the
+  test sources as text.
+* ``hash_vectors.json``: digests of seeded byte strings of many lengths,
+  computed by the reference's own hash headers (include/kokkos_murmur3.hpp,
+  include/kokkos_md5.hpp) compiled by ``oracle/build.py`` into oracle/_ref.
+
+Run from the repository root, where /root/reference is mounted:
+    python tests/golden/make_golden.py
+"""
+import ctypes
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+REF = "/root/reference"
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+# lengths: every tail length, block boundaries, and the chunk sizes in use
+HASH_LENGTHS = sorted(set(list(range(0, 130)) + [255, 256, 257, 511, 512, 513, 1000, 4095, 4096, 4097]))
+HASH_SEED = 20260101
+
+
+def kat_cases():
+    cases = []
+    for i in range(1, 11):
+        path = os.path.join(REF, "test", "test_case_%02d.cpp" % i)
+        src = open(path).read()
+        steps = {0: {}, 1: {}}
+        for step, idx, ch in re.findall(r"step([01])_h\((\d)\)\s*=\s*static_cast<uint8_t>\('(.)'\)", src):
+            steps[int(step)][int(idx)] = ch
+        chunk = int(re.search(r"TreeDeduplicator deduplicator\((\d+)\)", src).group(1))
+        m = re.search(r"num_first_ocur\(\) != (\d+) \|\| deduplicator.num_shift_dupl\(\) != (\d+)", src)
+        cases.append({
+            "name": "test_case_%02d" % i,
+            "source": "test/test_case_%02d.cpp" % i,
+            "chunk_size": chunk,
+            "step0": "".join(steps[0][k] for k in range(8)),
+            "step1": "".join(steps[1][k] for k in range(8)),
+            "num_first_ocur": int(m.group(1)),
+            "num_shift_dupl": int(m.group(2)),
+        })
+    return cases
+
+
+def hash_vectors():
+    from oracle import build
+    lib = ctypes.CDLL(build.build_ref(force=True))
+    rng = np.random.default_rng(HASH_SEED)
+    vecs = []
+    for n in HASH_LENGTHS:
+        data = rng.integers(0, 256, n, dtype=np.uint8)
+        ent = {"len": n, "data": data.tobytes().hex()}
+        for name, fn in (("murmur3", lib.ref_murmur3_hash), ("md5", lib.ref_md5_hash)):
+            out = (ctypes.c_uint8 * 16)()
+            fn(ctypes.c_void_p(data.ctypes.data), ctypes.c_uint64(n), out)
+            ent[name] = bytes(out).hex()
+        vecs.append(ent)
+    return vecs
+
+
+if __name__ == "__main__":
+    with open(os.path.join(OUT, "tree_kat.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": kat_cases()}, f, indent=1)
+    with open(os.path.join(OUT, "hash_vectors.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": HASH_SEED, "vectors": hash_vectors()}, f)
+    print("wrote", os.listdir(OUT))

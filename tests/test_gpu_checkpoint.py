@@ -1,0 +1,101 @@
+"""Incremental checkpoints from the GPU path are byte-identical to the oracle's
+(header, metadata in serial push order, data) for every approach, both
+digests, both update patterns, power-of-two and ragged sizes."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from mtcheck_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+APPROACHES = {"full": 1, "basic": 2, "list": 3, "tree": 4, "tree-ref": 5}
+KAT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "tree_kat.json")))["cases"]
+
+
+def series(pattern, nbytes, cs, steps, seed):
+    if pattern == 1:
+        return [s.copy() for s in workloads.pattern1(nbytes, cs, steps, seed=seed)]
+    z = (nbytes // 4, nbytes // 4 + nbytes // 8)
+    return [s.copy() for s in workloads.pattern2(nbytes, cs, steps, seed=seed, zero_range=z)]
+
+
+def run_both(cuda, mtc, oracle, approach, kind, seq, cs):
+    ref = oracle.Deduplicator(approach, cs, kind)
+    gpu = mtc.Deduplicator(cs, kind, approach=approach)
+    for i, s in enumerate(seq):
+        want = ref.checkpoint(s, i == 0)
+        got = gpu.checkpoint(cuda.from_numpy(s).cuda(), i == 0)
+        assert len(got) == len(want), (i, len(got), len(want))
+        if got != want:
+            diff = np.nonzero(np.frombuffer(got, np.uint8) != np.frombuffer(want, np.uint8))[0]
+            raise AssertionError("checkpoint %d differs at %d bytes, first %d" % (i, diff.size, diff[0]))
+        if approach != 1:
+            assert (gpu.num_first_ocur(), gpu.num_shift_dupl()) == (ref.num_first_ocur(), ref.num_shift_dupl())
+            assert gpu.info().data_size == ref.datasizes()[0] and gpu.info().metadata_size == ref.datasizes()[1]
+    return gpu
+
+
+@pytest.mark.parametrize("approach", list(APPROACHES.values()), ids=list(APPROACHES))
+@pytest.mark.parametrize("kind", [0, 1], ids=["murmur3", "md5"])
+@pytest.mark.parametrize("pattern,nbytes,cs", [
+    (1, 1 << 20, 128),          # 64 MiB / 128 B series, scaled down
+    (2, 1 << 21, 512),          # 4 GiB / 512 B series, scaled down
+    (2, (1 << 20) + 77, 256),   # ragged last chunk, non-power-of-two leaves
+    (1, 3 * 64 * 1000, 64),
+])
+def test_series_matches_oracle(cuda, mtc, oracle, approach, kind, pattern, nbytes, cs):
+    seq = series(pattern, nbytes, cs, 5, seed=nbytes % 1000 + pattern)
+    run_both(cuda, mtc, oracle, approach, kind, seq, cs)
+
+
+@pytest.mark.parametrize("cs", [1, 3, 24, 4096])
+def test_odd_chunk_sizes(cuda, mtc, oracle, cs):
+    seq = series(2, 64 * 1024 + 5, cs, 4, seed=cs)
+    for approach in (2, 3, 4, 5):
+        run_both(cuda, mtc, oracle, approach, 0, seq, cs)
+
+
+@pytest.mark.parametrize("case", KAT, ids=[c["name"] for c in KAT])
+def test_known_answer(cuda, mtc, case):
+    gpu = mtc.TreeDeduplicator(case["chunk_size"])
+    s0 = np.frombuffer(case["step0"].encode(), np.uint8).copy()
+    s1 = np.frombuffer(case["step1"].encode(), np.uint8).copy()
+    gpu.checkpoint(cuda.from_numpy(s0).cuda(), True)
+    gpu.checkpoint(cuda.from_numpy(s1).cuda(), False)
+    assert (gpu.num_first_ocur(), gpu.num_shift_dupl()) == (case["num_first_ocur"], case["num_shift_dupl"])
+
+
+def test_heavy_duplication_and_zero_region(cuda, mtc, oracle):
+    # many equal digests hit one map slot (the zero-filled range of the 4 GiB series)
+    rng = np.random.default_rng(1)
+    base = rng.integers(0, 256, 1 << 20, dtype=np.uint8)
+    base[1 << 18: 3 << 18] = 0
+    seq = [base.copy()]
+    nxt = base.copy()
+    nxt[:4096] = nxt[8192:12288]
+    nxt[5 << 16:(5 << 16) + 2048] = 0
+    seq.append(nxt)
+    for approach in (3, 4, 5):
+        run_both(cuda, mtc, oracle, approach, 0, seq, 128)
+
+
+def test_same_id_header_overload(cuda, mtc, oracle):
+    # checkpoint(header_t&, ...) does not advance current_id
+    seq = series(1, 1 << 18, 128, 3, seed=2)
+    ref = oracle.Deduplicator(4, 128)
+    gpu = mtc.TreeDeduplicator(128)
+    for i, s in enumerate(seq):
+        want = ref.checkpoint(s, i == 0, increment=False)
+        got = gpu.checkpoint(cuda.from_numpy(s).cuda(), i == 0, advance=False)
+        assert got == want
+
+
+def test_length_change_requires_baseline(cuda, mtc):
+    gpu = mtc.TreeDeduplicator(128)
+    gpu.checkpoint(cuda.zeros(1 << 16, dtype=cuda.uint8, device="cuda"), True)
+    with pytest.raises(mtc.MtcError) as e:
+        gpu.checkpoint(cuda.zeros(1 << 15, dtype=cuda.uint8, device="cuda"), False)
+    assert e.value.code == 1
