@@ -659,6 +659,8 @@ static int basic_run(orc_t* h, const uint8_t* data, uint64_t len, uint8_t** out,
     else { h->changed[i] = 1; h->list[i] = dg; }
   }
   for (uint32_t i = 0; i < N; i++) F += h->changed[i];
+  h->fo_len = F;  /* reported as num_first_ocur (header field) */
+  h->sh_len = 0;
   uint64_t size = 32 + (uint64_t)F * (4 + (uint64_t)cs);
   uint8_t* buf = (uint8_t*)calloc(size, 1);
   if (!buf) return ORC_ENOMEM;
