@@ -69,6 +69,8 @@ typedef struct mtc_info {
   uint64_t metadata_size;  /* datasizes.second */
   double timers[4];        /* setup, compare, gather, copy to host (s) */
   double restart_timers[2];/* copy, total (s) */
+  double phase_times[3];   /* device time of the last checkpoint: leaf hashing kernel,
+                              forest passes and root compaction, diff assembly (s) */
   uint32_t device_error;   /* last device error bits (0 = none) */
   uint32_t reserved;
 } mtc_info_t;

@@ -45,6 +45,7 @@ class Info(ctypes.Structure):
                 ("num_prior_chkpts", ctypes.c_uint32), ("data_len", ctypes.c_uint64),
                 ("diff_len", ctypes.c_uint64), ("data_size", ctypes.c_uint64), ("metadata_size", ctypes.c_uint64),
                 ("timers", ctypes.c_double * 4), ("restart_timers", ctypes.c_double * 2),
+                ("phase_times", ctypes.c_double * 3),
                 ("device_error", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 

@@ -222,6 +222,7 @@ int mtc_get_info(const mtc_dedup_t* h, mtc_info_t* o) {
   for (int i = 0; i < 4; i++) o->timers[i] = e.timers[i];
   o->restart_timers[0] = e.restart_timers[0];
   o->restart_timers[1] = e.restart_timers[1];
+  for (int i = 0; i < 3; i++) o->phase_times[i] = e.phase_times[i];
   o->device_error = e.last_device_error;
   return MTC_OK;
 }

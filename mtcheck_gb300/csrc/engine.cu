@@ -12,28 +12,6 @@
 
 namespace mtc {
 
-template <class T>
-cudaError_t DevBuf<T>::ensure(size_t want, cudaStream_t s, bool keep) {
-  if (want <= n && p) return cudaSuccess;
-  T* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, sizeof(T) * std::max<size_t>(want, 1));
-  if (e != cudaSuccess) return e;
-  if (keep && p && n) cudaMemcpyAsync(q, p, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
-  if (p) {
-    cudaStreamSynchronize(s);
-    cudaFree(p);
-  }
-  p = q;
-  n = want;
-  return cudaSuccess;
-}
-template <class T>
-void DevBuf<T>::release() {
-  if (p) cudaFree(p);
-  p = nullptr;
-  n = 0;
-}
-
 static uint64_t next_pow2(uint64_t v) {
   uint64_t c = 1;
   while (c < v) c <<= 1;
@@ -52,6 +30,7 @@ Engine::~Engine() {
   for (auto& e : ev_) if (e) cudaEventDestroy(e);
   if (lay_host_) cudaFreeHost(lay_host_);
   if (err_host_) cudaFreeHost(err_host_);
+  destroy_restart_scratch(rs_);
 }
 
 int Engine::fail(int code, const std::string& msg) {
@@ -199,6 +178,7 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.hash_kind = hash_kind_;
   la.epi = EPI_TREE;
   MTC_CUDA(launch_leaves(la, &tma_, stream_));
+  MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   MTC_CUDA(launch_tree_leaf_finalize(la, stream_));
 
   ForestArgs fa{digests_.p, labels_.p, rflag_.p, map, current_id, 0, err_.p, hash_kind_};
@@ -245,6 +225,7 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.epi = mode_ == MODE_LIST ? EPI_LIST : EPI_BASIC;
   la.basic_first = current_id == 0 ? 1 : 0;
   MTC_CUDA(launch_leaves(la, &tma_, stream_));
+  MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   if (mode_ == MODE_LIST) MTC_CUDA(launch_list_finalize(la, stream_));
   MTC_CUDA(launch_chunk_compaction(labels_.p, N_, mode_ == MODE_BASIC ? 1 : 0, fo_list_.p, sh_list_.p, lay_.p, scan_.p,
                                    scan_total_.p, stream_));
@@ -318,6 +299,10 @@ int Engine::finish(const uint8_t* data, uint64_t len, HeaderHost* header) {
   cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
   cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
   timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
+  float leaf = 0, rest = 0;
+  cudaEventElapsedTime(&leaf, ev_[1], ev_[4]);
+  cudaEventElapsedTime(&rest, ev_[4], ev_[2]);
+  phase_times[0] = leaf * 1e-3; phase_times[1] = rest * 1e-3; phase_times[2] = ms[2] * 1e-3;
   if (last_device_error & DERR_SPIN) return fail(ST_ETIMEOUT, "bounded device wait expired");
   if (last_device_error & (DERR_MAP_FULL | DERR_CAPACITY)) return fail(ST_ENOMEM, "device table or staging buffer full");
   if (last_device_error & DERR_MISSING) return fail(ST_EINTERNAL, "root digest missing from the map");

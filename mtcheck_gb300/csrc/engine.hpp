@@ -15,6 +15,18 @@
 
 namespace mtc {
 
+// Return a status from an Engine member when a CUDA call fails.
+#define MTC_CUDA_R(call)                                                                                   \
+  do {                                                                                                     \
+    cudaError_t e_ = (call);                                                                               \
+    if (e_ != cudaSuccess)                                                                                 \
+      return fail(e_ == cudaErrorMemoryAllocation ? ST_ENOMEM : ST_ECUDA,                                  \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                                      \
+  } while (0)
+
+struct RestartScratch;
+void destroy_restart_scratch(RestartScratch* r);
+
 // DedupMode values of the reference (include/utils.hpp:39-49).
 enum : int { MODE_FULL = 1, MODE_BASIC = 2, MODE_LIST = 3, MODE_TREE = 4, MODE_TREE_LOW_OFFSET_REF = 5, MODE_TREE_LOW_OFFSET = 6 };
 
@@ -28,12 +40,30 @@ struct HeaderHost {  // header_t, include/utils.hpp:29-37
 };
 static_assert(sizeof(HeaderHost) == 32, "header_t is 32 bytes");
 
+// Grow-only device array.
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;  // elements
-  cudaError_t ensure(size_t want, cudaStream_t s, bool keep = false);
-  void release();
+  cudaError_t ensure(size_t want, cudaStream_t s, bool keep = false) {
+    if (want <= n && p) return cudaSuccess;
+    T* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (want ? want : 1));
+    if (e != cudaSuccess) return e;
+    if (keep && p && n) cudaMemcpyAsync(q, p, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+    if (p) {
+      cudaStreamSynchronize(s);
+      cudaFree(p);
+    }
+    p = q;
+    n = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
   ~DevBuf() { release(); }
 };
 
@@ -64,6 +94,7 @@ class Engine {
   uint64_t datasizes[2] = {0, 0};
   double timers[4] = {0, 0, 0, 0};          // setup, compare, gather, copy-to-host (seconds)
   double restart_timers[2] = {0, 0};        // copy, total
+  double phase_times[3] = {0, 0, 0};        // leaf hashing kernel, forest + roots, diff assembly (s)
   uint32_t last_device_error = 0;
   std::string last_error;
 
@@ -104,9 +135,8 @@ class Engine {
   uint32_t* err_host_ = nullptr;    // pinned [err, map size]
   uint64_t diff_len_ = 0, diff_pad_ = 0;
   TmaCache tma_;
-  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
-
-  friend class RestartRunner;
+  cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  RestartScratch* rs_ = nullptr;  // restart buffers, created on first use
 };
 
 }  // namespace mtc

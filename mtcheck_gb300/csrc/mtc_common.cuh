@@ -21,6 +21,7 @@ enum : uint32_t {
   DERR_CAPACITY = 1u << 3,      // diff larger than the device staging buffer
   DERR_MISSING = 1u << 4,       // a root digest is absent from the map
   DERR_RANGE = 1u << 5,         // restart metadata out of range
+  DERR_INTERIOR = 1u << 6,      // restart provenance names an interior node
 };
 
 struct __align__(16) Digest { uint32_t w[4]; };

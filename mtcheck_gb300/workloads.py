@@ -59,6 +59,23 @@ def _ops(seed, device):
     return _NpOps(seed) if device is None else _TorchOps(seed, device)
 
 
+def _rows(buf, cs, nbytes):
+    """2-D view [full chunks, cs] of the buffer."""
+    full = nbytes // cs
+    return buf[:full * cs].reshape(full, cs) if hasattr(buf, "reshape") else buf[:full * cs].view(full, cs)
+
+
+def _is_torch(buf):
+    return type(buf).__module__.split(".")[0] == "torch"
+
+
+def _index(buf, idx):
+    if _is_torch(buf):
+        import torch
+        return torch.from_numpy(np.ascontiguousarray(idx)).to(buf.device)
+    return idx
+
+
 def _copy_chunks(buf, cs, dst, src, nbytes, prev=None):
     """buf[chunk d] = (prev or buf)[chunk s] for whole chunks (partial last chunk skipped)."""
     full = nbytes // cs
@@ -68,30 +85,25 @@ def _copy_chunks(buf, cs, dst, src, nbytes, prev=None):
     dst, src = dst[keep], src[keep]
     if dst.size == 0:
         return
-    off = np.arange(cs, dtype=np.int64)
-    di = (dst[:, None] * cs + off[None, :]).reshape(-1)
-    si = (src[:, None] * cs + off[None, :]).reshape(-1)
-    source = buf if prev is None else prev
-    if hasattr(buf, "index_copy_"):
-        import torch
-        di_t = torch.from_numpy(di).to(buf.device)
-        si_t = torch.from_numpy(si).to(buf.device)
-        buf[di_t] = source[si_t].clone()
-    else:
-        buf[di] = source[si].copy()
+    rows = _rows(buf, cs, nbytes)
+    srows = rows if prev is None else _rows(prev, cs, nbytes)
+    vals = srows[_index(buf, src)]
+    rows[_index(buf, dst)] = vals
 
 
 def _fill_random(ops, buf, cs, chunks, nbytes):
+    """Fresh random bytes in the given chunks."""
     chunks = np.unique(np.asarray(chunks, dtype=np.int64))
     if chunks.size == 0:
         return
-    # group contiguous chunk runs to fill them with one call each
-    breaks = np.nonzero(np.diff(chunks) != 1)[0] + 1
-    for run in np.split(chunks, breaks):
-        a = int(run[0]) * cs
-        b = min(int(run[-1] + 1) * cs, nbytes)
-        if b > a:
-            buf[a:b] = ops.random_bytes(b - a)
+    full = nbytes // cs
+    body = chunks[chunks < full]
+    if body.size:
+        rows = _rows(buf, cs, nbytes)
+        rnd = ops.random_bytes(int(body.size) * cs)
+        rows[_index(buf, body)] = rnd.reshape(int(body.size), cs)
+    if full * cs < nbytes and chunks[-1] >= full:
+        buf[full * cs:nbytes] = ops.random_bytes(nbytes - full * cs)
 
 
 def pattern1(nbytes, cs, steps, seed=1, device=None, dup_frac=0.2, rate=0.01, run_max=32):
