@@ -75,9 +75,13 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
 }
 
 int Engine::ensure_sort(uint32_t K) {
+  // capacities grow in powers of two so that a growing checkpoint id does not
+  // reallocate on every call
+  K = (uint32_t)next_pow2(std::max<uint32_t>(K, 64));
   const uint64_t T = (uint64_t)(N_ + 1 + kSortTile - 1) / kSortTile + 1;
   MTC_CUDA(hist_.ensure(K, stream_));
   MTC_CUDA(rep_.ensure(K, stream_));
+  MTC_CUDA(rank_.ensure(K, stream_));
   MTC_CUDA(sort_mat_.ensure((size_t)K * T, stream_));
   MTC_CUDA(scan2_.ensure((size_t)K * T / kScanTile + 2, stream_));
   // staging buffer: pad + header + metadata + data
@@ -98,6 +102,8 @@ int Engine::ensure_state(uint32_t N, bool fresh) {
     MTC_CUDA(labels_.ensure(nd, stream_));
     MTC_CUDA(rflag_.ensure(tree ? M : 1, stream_));
     MTC_CUDA(chunk_slot_.ensure(N, stream_));
+    MTC_CUDA(changed_list_.ensure(N, stream_));
+    MTC_CUDA(changed_count_.ensure(1, stream_));
     MTC_CUDA(map_size_.ensure(1, stream_));
     MTC_CUDA(err_.ensure(1, stream_));
     MTC_CUDA(fo_list_.ensure(N + 1, stream_));
@@ -148,6 +154,7 @@ GatherArgs Engine::gather_args(const uint8_t* data, uint64_t len) {
   g.sh_prev = sh_prev_.p;
   g.hist = hist_.p;
   g.rep = rep_.p;
+  g.rank = rank_.p;
   g.sort_mat = sort_mat_.p;
   g.scan_scratch = scan_.p;
   g.scan_total = scan_total_.p;
@@ -177,33 +184,30 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.err = err_.p;
   la.hash_kind = hash_kind_;
   la.epi = EPI_TREE;
+  la.changed_list = changed_list_.p;
+  la.changed_count = changed_count_.p;
+  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_));
   MTC_CUDA(cudaEventRecord(ev_[4], stream_));
-  MTC_CUDA(launch_tree_leaf_finalize(la, stream_));
+  MTC_CUDA(launch_leaf_inserts(la, stream_));
 
-  ForestArgs fa{digests_.p, labels_.p, rflag_.p, map, current_id, 0, err_.p, hash_kind_};
-  if (N >= 2) {
-    // interior nodes [0, N-2]; depth d holds [2^d - 1, 2^(d+1) - 2]
-    int dmax = 0;
-    while (((2ull << dmax) - 1) <= (uint64_t)(N - 2)) dmax++;
-    for (int d = dmax; d >= 0; d--) {  // first-occurrence forest (src/tree_approach.cpp:378-404)
-      uint32_t beg = (uint32_t)((1ull << d) - 1);
-      uint32_t end = (uint32_t)std::min<uint64_t>((2ull << d) - 2, N - 2);
-      fa.epoch = ++epoch_;
-      MTC_CUDA(launch_fo_level(fa, beg, end, stream_));
-    }
-    for (int d = dmax; d >= 0; d--) {  // duplicate forest (:413-477 / baseline :155-227)
-      uint32_t beg = (uint32_t)((1ull << d) - 1);
-      uint32_t end = (uint32_t)std::min<uint64_t>((2ull << d) - 2, N - 2);
-      MTC_CUDA(launch_dup_level(fa, beg, end, baseline_path ? 1 : 0, stream_));
-      if (baseline_path) {
-        fa.epoch = ++epoch_;
-        MTC_CUDA(launch_insert_level(fa, beg, end, stream_));
-      }
-    }
-  }
-  MTC_CUDA(launch_root_compaction(labels_.p, rflag_.p, N, M, mode_ == MODE_TREE_LOW_OFFSET_REF ? 1 : 0, fo_list_.p,
-                                  sh_list_.p, lay_.p, scan_.p, scan_total_.p, stream_));
+  ForestArgs fa{};
+  fa.tree = digests_.p;
+  fa.labels = labels_.p;
+  fa.rflag = rflag_.p;
+  fa.map = map;
+  fa.cur = current_id;
+  fa.err = err_.p;
+  fa.hash_kind = hash_kind_;
+  fa.ascending = mode_ == MODE_TREE_LOW_OFFSET_REF ? 1 : 0;
+  fa.D = 0;
+  while (((2ull << fa.D) - 1) <= (uint64_t)(M - 1)) fa.D++;  // depth of node M-1
+  fa.sizeD = (uint64_t)M - ((1ull << fa.D) - 1);
+  fa.epoch = ++epoch_;
+  MTC_CUDA(launch_forest(fa, 0, 0, N, 0, stream_));  // first-occurrence forest
+  const uint32_t e2 = ++epoch_;
+  MTC_CUDA(launch_forest(fa, 1, baseline_path ? 1 : 0, N, e2, stream_));  // duplicate forest
+  MTC_CUDA(launch_root_compaction(fa, N, M, fo_list_.p, sh_list_.p, lay_.p, scan_.p, scan_total_.p, stream_));
   return ST_OK;
 }
 
@@ -224,9 +228,12 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.hash_kind = hash_kind_;
   la.epi = mode_ == MODE_LIST ? EPI_LIST : EPI_BASIC;
   la.basic_first = current_id == 0 ? 1 : 0;
+  la.changed_list = changed_list_.p;
+  la.changed_count = changed_count_.p;
+  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_));
   MTC_CUDA(cudaEventRecord(ev_[4], stream_));
-  if (mode_ == MODE_LIST) MTC_CUDA(launch_list_finalize(la, stream_));
+  if (mode_ == MODE_LIST) MTC_CUDA(launch_leaf_inserts(la, stream_));
   MTC_CUDA(launch_chunk_compaction(labels_.p, N_, mode_ == MODE_BASIC ? 1 : 0, fo_list_.p, sh_list_.p, lay_.p, scan_.p,
                                    scan_total_.p, stream_));
   return ST_OK;
@@ -306,6 +313,7 @@ int Engine::finish(const uint8_t* data, uint64_t len, HeaderHost* header) {
   if (last_device_error & DERR_SPIN) return fail(ST_ETIMEOUT, "bounded device wait expired");
   if (last_device_error & (DERR_MAP_FULL | DERR_CAPACITY)) return fail(ST_ENOMEM, "device table or staging buffer full");
   if (last_device_error & DERR_MISSING) return fail(ST_EINTERNAL, "root digest missing from the map");
+  if (last_device_error & DERR_SORTKEYS) return fail(ST_ENOTSUP, "more than 1024 distinct source checkpoints in one diff");
   if (!L.ok) return fail(ST_EINTERNAL, "diff layout failed");
   diff_len_ = L.diff_len;
   diff_pad_ = L.pad;

@@ -124,10 +124,10 @@ class Engine {
 
   DevBuf<Digest> digests_;     // tree heap (M) or hash list (N)
   DevBuf<uint8_t> labels_, rflag_;
-  DevBuf<uint32_t> chunk_slot_;
+  DevBuf<uint32_t> chunk_slot_, changed_list_, changed_count_;
   DevBuf<MapSlot> slots_;
   DevBuf<uint32_t> map_size_, err_;
-  DevBuf<uint32_t> fo_list_, sh_list_, reg_chunk_, reg_slot_, reg_len_, sh_key_, sh_prev_, hist_, rep_;
+  DevBuf<uint32_t> fo_list_, sh_list_, reg_chunk_, reg_slot_, reg_len_, sh_key_, sh_prev_, hist_, rep_, rank_;
   DevBuf<uint64_t> fo_val_, sort_mat_, scan_, scan_total_, scan2_, scan_total2_;
   DevBuf<uint8_t> stage_;
   DevBuf<Layout> lay_;

@@ -8,6 +8,7 @@
 //     shifted duplicates by source checkpoint, metadata and the chunk gather
 //     (src/tree_approach.cpp:512-710, src/list_approach.cpp:79-247,
 //     src/basic_approach.cpp:52-143).
+#include <algorithm>
 #include <cstdio>
 
 #include "mtc_common.cuh"
@@ -17,6 +18,8 @@
 namespace mtc {
 
 namespace {
+
+constexpr uint32_t kSortFastKeys = 1024;  // distinct source checkpoints per diff
 
 inline uint32_t grid_for(uint64_t n, int threads, int per_sm = 8) {
   uint64_t g = (n + threads - 1) / threads;
@@ -29,109 +32,163 @@ inline uint32_t grid_for(uint64_t n, int threads, int per_sm = 8) {
 // ---------------------------------------------------------------------------
 // Forest passes
 // ---------------------------------------------------------------------------
-__global__ void fo_level_kernel(ForestArgs a, uint32_t beg, uint32_t end) {
-  for (uint64_t n = beg + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; n <= end; n += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t l = 2 * (uint32_t)n + 1, r = l + 1;
-    if (a.labels[l] == FIRST_OCUR && a.labels[r] == FIRST_OCUR) {
-      a.labels[n] = FIRST_OCUR;
-      Digest d = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + r));
-      st_digest(a.tree + n, d);
-      map_insert_first(a.map, d, (uint32_t)n, a.cur, a.epoch, a.err);
-    } else {
-      a.labels[n] = DONE;
-    }
-  }
-}
-
 __device__ __forceinline__ uint8_t child_flag(uint8_t lab) {
   return (lab == FIXED_DUPL || lab == DONE) ? ROOT_NONE : (lab == SHIFT_DUPL ? ROOT_SHIFT : ROOT_FO);
 }
 
-// baseline != 0: the shift test reads the node's digest before it is hashed
-// (src/tree_approach.cpp:202 vs :221).
-__global__ void dup_level_kernel(ForestArgs a, uint32_t beg, uint32_t end, int baseline) {
-  for (uint64_t n = beg + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; n <= end; n += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t l = 2 * (uint32_t)n + 1, r = l + 1;
-    const uint8_t ll = a.labels[l], lr = a.labels[r];
-    uint8_t fl = ROOT_NONE, fr = ROOT_NONE;
-    if (ll != lr) {
-      a.labels[n] = DONE;
-      fl = child_flag(ll);
-      fr = child_flag(lr);
-    } else if (ll == FIXED_DUPL) {
-      a.labels[n] = FIXED_DUPL;
-    } else if (ll == SHIFT_DUPL) {
-      Digest d;
-      if (baseline) {
-        d = ld_digest(a.tree + n);
-      } else {
-        d = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + r));
-        st_digest(a.tree + n, d);
-      }
-      if (map_find(a.map, d, a.err) >= 0) {
-        a.labels[n] = SHIFT_DUPL;
-      } else {
-        a.labels[n] = DONE;
-        fl = ROOT_SHIFT;
-        fr = ROOT_SHIFT;
-      }
+// Several levels per launch: CTA b owns the subtree of interior node
+// r = 2^d_top - 1 + b and computes its interior nodes from depth d_bot up to
+// d_top.  The labels of one level stay in shared memory for the next; only
+// the bottom children, leaves met on the way, digests and the results touch
+// global memory.  pass 0: first-occurrence forest (src/tree_approach.cpp
+// :378-404); pass 1: duplicate forest (:413-477), with baseline != 0 the
+// baseline variant that tests the not-yet-hashed digest and then hashes and
+// inserts every interior node (:155-227).
+constexpr uint32_t kSpanLevels = 9;  // 256 nodes on the bottom level of a span
+__global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass, int baseline, uint32_t N,
+                                                          uint32_t d_top, uint32_t d_bot, uint32_t epoch2) {
+  __shared__ uint8_t lab[2][2 << (kSpanLevels - 1)];
+  const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
+  const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
+  if (r > last_interior) return;
+  const uint32_t wb = 1u << (d_bot - d_top);
+  uint8_t* child = lab[0];
+  uint8_t* cur = lab[1];
+  {
+    const uint64_t cfirst = (r + 1) * (2ull * wb) - 1;  // subtree nodes at depth d_bot + 1
+    for (uint32_t i = threadIdx.x; i < 2 * wb; i += blockDim.x) {
+      const uint64_t n = cfirst + i;
+      child[i] = n < M ? a.labels[n] : DONE;
     }
-    a.rflag[l] = fl;
-    a.rflag[r] = fr;
   }
-}
-
-// baseline only: hash and insert every interior node of the level (:218-224)
-__global__ void insert_level_kernel(ForestArgs a, uint32_t beg, uint32_t end) {
-  for (uint64_t n = beg + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; n <= end; n += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t l = 2 * (uint32_t)n + 1, r = l + 1;
-    Digest d = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + r));
-    st_digest(a.tree + n, d);
-    map_insert_first(a.map, d, (uint32_t)n, a.cur, a.epoch, a.err);
+  __syncthreads();
+  for (int d = (int)d_bot; d >= (int)d_top; d--) {
+    const uint32_t width = 1u << (d - d_top);
+    const uint64_t first = (r + 1) * width - 1;
+    for (uint32_t i = threadIdx.x; i < width; i += blockDim.x) {
+      const uint64_t n = first + i;
+      if (n > last_interior) {  // a leaf (or past the end): its label is final
+        cur[i] = n < M ? a.labels[n] : DONE;
+        continue;
+      }
+      const uint32_t l = 2 * (uint32_t)n + 1, rr = l + 1;
+      const uint8_t ll = child[2 * i], lr = child[2 * i + 1];
+      uint8_t lab_n;
+      if (pass == 0) {
+        if (ll == FIRST_OCUR && lr == FIRST_OCUR) {
+          lab_n = FIRST_OCUR;
+          Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
+          st_digest(a.tree + n, dg);
+          map_insert_serial(a.map, dg, (uint32_t)n, a.cur, a.epoch, a.err);
+        } else {
+          lab_n = DONE;
+        }
+      } else {
+        uint8_t fl = ROOT_NONE, fr = ROOT_NONE;
+        if (ll != lr) {
+          lab_n = DONE;
+          fl = child_flag(ll);
+          fr = child_flag(lr);
+        } else if (ll == FIXED_DUPL) {
+          lab_n = FIXED_DUPL;
+        } else if (ll == SHIFT_DUPL) {
+          Digest dg;
+          if (baseline) {
+            dg = ld_digest(a.tree + n);
+          } else {
+            dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
+            st_digest(a.tree + n, dg);
+          }
+          if (map_find(a.map, dg, a.err) >= 0) {
+            lab_n = SHIFT_DUPL;
+          } else {
+            lab_n = DONE;
+            fl = ROOT_SHIFT;
+            fr = ROOT_SHIFT;
+          }
+        } else {
+          lab_n = ll == FIRST_OCUR ? FIRST_OCUR : DONE;  // both first occurrences, or both done
+        }
+        a.rflag[canon_pos(a, l)] = fl;
+        a.rflag[canon_pos(a, rr)] = fr;
+        if (baseline) {
+          Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
+          st_digest(a.tree + n, dg);
+          map_insert_serial(a.map, dg, (uint32_t)n, a.cur, epoch2, a.err);
+        }
+      }
+      cur[i] = lab_n;
+      a.labels[n] = lab_n;
+    }
+    __syncthreads();
+    uint8_t* t = child;
+    child = cur;
+    cur = t;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Root compaction in serial push order.
+// Root compaction in serial push order.  rflag holds the flags at canonical
+// positions, so the lists are a stable compaction of one byte array.
 // ---------------------------------------------------------------------------
-struct LevelTable {
-  uint32_t nlev;
-  uint32_t first_node[33];  // first node of each level in output order
-  uint64_t first_pos[34];   // position of that level's first node
-};
+__device__ __forceinline__ uint32_t node_at(const ForestArgs& a, uint64_t p) {
+  if (a.ascending) return (uint32_t)p + 1;
+  if (p < a.sizeD) return (uint32_t)(((1ull << a.D) - 1) + p);
+  uint64_t q = p - a.sizeD;  // within levels D-1, D-2, ... of sizes 2^(D-1), 2^(D-2), ...
+  int d = (int)a.D - 1;
+  while (d > 0 && q >= (1ull << d)) { q -= 1ull << d; d--; }
+  return (uint32_t)(((1ull << d) - 1) + q);
+}
 
-// canonical position -> node
-struct PosToNode {
-  LevelTable t;
-  int ascending;  // 1: plain ascending node order (std::set of roots)
-  __device__ __forceinline__ uint32_t operator()(uint64_t p) const {
-    if (ascending) return (uint32_t)p + 1;
-    uint32_t k = 0;
-    while (k + 1 < t.nlev && p >= t.first_pos[k + 1]) k++;
-    return t.first_node[k] + (uint32_t)(p - t.first_pos[k]);
+// 8 flags per thread, 4096 per tile; counts packed as (shift << 32) | fo
+__device__ __forceinline__ uint64_t flags8(const uint8_t* f, uint64_t p, uint64_t n, uint8_t out[8]) {
+  uint64_t c = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    uint8_t v = (p + k < n) ? f[p + k] : 0;
+    out[k] = v;
+    c += (v == ROOT_FO) ? 1ull : (v == ROOT_SHIFT ? (1ull << 32) : 0ull);
   }
-};
+  return c;
+}
 
-struct RootVal {
-  PosToNode map;
-  const uint8_t* rflag;
-  __device__ __forceinline__ uint64_t operator()(uint64_t p) const {
-    uint8_t f = rflag[map(p)];
-    return (f == ROOT_FO ? 1ull : 0ull) | (f == ROOT_SHIFT ? (1ull << 32) : 0ull);
+__global__ void __launch_bounds__(kScanThreads) root_count_kernel(const uint8_t* rflag, uint64_t n, uint64_t* tile_sums) {
+  __shared__ uint64_t sh[33];
+  const uint64_t p = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanPerThread;
+  uint8_t v[8];
+  uint64_t c = 0;
+  if (p + 8 <= n && ((p & 7) == 0)) {
+    uint64_t w = *reinterpret_cast<const uint64_t*>(rflag + p);
+    if (w) c = flags8(rflag, p, n, v);
+  } else if (p < n) {
+    c = flags8(rflag, p, n, v);
   }
-};
-struct RootEmit {
-  PosToNode map;
-  uint32_t* fo_list;
-  uint32_t* sh_list;
-  const Layout* lay;
-  __device__ __forceinline__ void operator()(uint64_t p, uint64_t ex, uint64_t v) const {
-    if (!v) return;
-    uint32_t node = map(p);
-    if (v & 1ull) fo_list[lay->root_fo + (uint32_t)ex] = node;
-    if (v >> 32) sh_list[(uint32_t)(ex >> 32)] = node;
+  uint64_t total;
+  block_excl_scan(c, sh, &total);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, uint64_t n, const uint64_t* tile_off,
+                                                                 uint32_t* fo_list, uint32_t* sh_list, const Layout* lay) {
+  __shared__ uint64_t sh[33];
+  const uint64_t p = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanPerThread;
+  uint8_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint64_t c = 0;
+  if (p < n) {
+    if (p + 8 <= n && ((p & 7) == 0)) {
+      if (*reinterpret_cast<const uint64_t*>(a.rflag + p)) c = flags8(a.rflag, p, n, v);
+    } else {
+      c = flags8(a.rflag, p, n, v);
+    }
   }
-};
+  uint64_t ex = block_excl_scan(c, sh, nullptr) + tile_off[blockIdx.x];
+  if (!c) return;
+  const uint32_t root = lay->root_fo;
+  for (int k = 0; k < 8; k++) {
+    if (v[k] == ROOT_FO) { fo_list[root + (uint32_t)ex] = node_at(a, p + k); ex += 1; }
+    else if (v[k] == ROOT_SHIFT) { sh_list[(uint32_t)(ex >> 32)] = node_at(a, p + k); ex += 1ull << 32; }
+  }
+}
 
 __global__ void root_prologue_kernel(const uint8_t* labels, uint32_t N, int ascending, uint32_t* fo_list, Layout* lay) {
   // the incremental/baseline passes push the root only for N >= 2
@@ -209,7 +266,11 @@ __global__ void layout_kernel(GatherArgs g) {
   const uint32_t F = lay->F, S = lay->S, nd = lay->num_distinct;
   // P = number of source checkpoints that occur; max_key = largest of them
   __shared__ uint32_t smax;
-  if (threadIdx.x == 0) smax = 0;
+  if (threadIdx.x == 0) {
+    smax = 0;
+    lay->nkeys = 0;  // set below once the keys are known
+    lay->sort_n = 0;
+  }
   __syncthreads();
   uint32_t P = 0;
   for (uint32_t b = 0; b < K; b += blockDim.x) {
@@ -299,6 +360,30 @@ __global__ void layout_kernel(GatherArgs g) {
     uint32_t rep = k;
     while (rep > 0 && (int)(mul * (double)(rep - 1)) == bk) rep--;
     g.rep[k] = rep;
+    g.rank[k] = 0;
+  }
+  __syncthreads();
+  // dense index of each representative that some present key maps to
+  for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+    if (g.hist[k] > 0) g.rank[g.rep[k]] = 1;
+  __syncthreads();
+  uint32_t run = 0;
+  for (uint32_t b0 = 0; b0 < K; b0 += blockDim.x) {
+    uint32_t k = b0 + threadIdx.x;
+    uint64_t v = k < K ? g.rank[k] : 0;
+    uint64_t t;
+    uint64_t ex = block_excl_scan(v, sh, &t);
+    if (k < K) g.rank[k] = run + (uint32_t)ex;
+    run += (uint32_t)t;
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+    if (g.hist[k] > 0) g.rep[k] = g.rank[g.rep[k]];
+  if (threadIdx.x == 0) {
+    lay->nkeys = run;
+    const uint32_t T = (uint32_t)((g.N + 1 + kSortTile - 1) / kSortTile) + 1;
+    lay->sort_n = run * T;
+    if (run > kSortFastKeys) atomicOr(g.err, DERR_SORTKEYS);
   }
 }
 
@@ -306,7 +391,8 @@ __global__ void layout_kernel(GatherArgs g) {
 // Tile t counts its keys; matrix[key * T + t] (key-major).
 __global__ void sort_count_kernel(GatherArgs g, uint32_t T) {
   extern __shared__ uint32_t cnt[];
-  const uint32_t K = g.cur + 1, S = g.lay->S;
+  const uint32_t K = g.lay->nkeys, S = g.lay->S;
+  if (K > kSortFastKeys) return;
   for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
@@ -325,38 +411,59 @@ struct MatEmit {
   uint64_t* m;
   __device__ __forceinline__ void operator()(uint64_t i, uint64_t ex, uint64_t) const { m[i] = ex; }
 };
-// one warp per tile; entries are placed in tile order, 32 at a time
-__global__ void sort_scatter_kernel(GatherArgs g, uint32_t T) {
-  extern __shared__ uint32_t cur[];
-  const uint32_t K = g.cur + 1, S = g.lay->S;
-  const uint32_t lane = threadIdx.x;
-  if (!g.lay->ok) return;
+// Stable placement of the shift entries of one 4096-entry tile: 8 warps each
+// rank a contiguous 512-entry slice in order (per-warp key counters in shared
+// memory), then the per-key counts of earlier warps and the tile's global
+// base (key-major scan of sort_mat) give each entry its position.
+constexpr int kSortWarps = 8;
+__global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g, uint32_t T) {
+  __shared__ uint32_t keys[kSortTile];
+  __shared__ uint32_t lrank[kSortTile];
+  extern __shared__ uint32_t cnt[];  // [kSortWarps][K]
+  const uint32_t K = g.lay->nkeys, S = g.lay->S;
+  if (!g.lay->ok || K > kSortFastKeys) return;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr uint32_t kSlice = kSortTile / kSortWarps;
   uint8_t* pairs = g.stage + g.lay->pad + g.lay->pairs_off;
   for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
     const uint64_t b = (uint64_t)t * kSortTile;
     if (b >= S) break;
-    for (uint32_t k = lane; k < K; k += 32) cur[k] = (uint32_t)g.sort_mat[(uint64_t)k * T + t];
-    __syncwarp();
-    for (uint64_t i0 = b; i0 < b + kSortTile && i0 < S; i0 += 32) {
-      const uint64_t i = i0 + lane;
-      const bool v = i < S && i < b + kSortTile;
-      const uint32_t key = v ? g.rep[g.sh_key[i]] : 0xffffffffu;
+    const uint32_t n = (uint32_t)(S - b < kSortTile ? S - b : kSortTile);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) keys[i] = g.rep[g.sh_key[b + i]];
+    for (uint32_t k = threadIdx.x; k < kSortWarps * K; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    uint32_t* wc = cnt + warp * K;
+    for (uint32_t i0 = warp * kSlice; i0 < (warp + 1) * kSlice && i0 < n; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const bool v = i < n && i < (warp + 1) * kSlice;
+      const uint32_t key = v ? keys[i] : 0xffffffffu;
       const uint32_t peers = __match_any_sync(0xffffffffu, key);
       const uint32_t rank = __popc(peers & ((1u << lane) - 1));
-      const uint32_t leader = __ffs(peers) - 1;
-      uint32_t base = 0;
-      if (v) base = cur[key];
+      uint32_t base = v ? wc[key] : 0;
       __syncwarp();
       if (v) {
-        const uint32_t pos = base + rank;
-        uint32_t* e = reinterpret_cast<uint32_t*>(pairs + 8ull * pos);
-        e[0] = g.sh_list[i];
-        e[1] = g.sh_prev[i];
-        if (lane == leader) cur[key] = base + __popc(peers);
+        lrank[i] = base + rank;
+        if (lane == (uint32_t)(__ffs(peers) - 1)) wc[key] = base + __popc(peers);
       }
       __syncwarp();
     }
-    __syncwarp();
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+      uint32_t run = (uint32_t)g.sort_mat[(uint64_t)k * T + t];
+      for (int w = 0; w < kSortWarps; w++) {
+        uint32_t c = cnt[w * K + k];
+        cnt[w * K + k] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const uint32_t pos = cnt[(i / kSlice) * K + keys[i]] + lrank[i];
+      uint32_t* e = reinterpret_cast<uint32_t*>(pairs + 8ull * pos);
+      e[0] = g.sh_list[b + i];
+      e[1] = g.sh_prev[b + i];
+    }
+    __syncthreads();
   }
 }
 
@@ -473,52 +580,34 @@ cudaError_t launch_map_rehash(const DigestMap& from, uint64_t from_cap, const Di
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_fo_level(const ForestArgs& a, uint32_t beg, uint32_t end, cudaStream_t s) {
-  fo_level_kernel<<<grid_for(end - beg + 1, 256), 256, 0, s>>>(a, beg, end);
-  note_launch();
-  return cudaGetLastError();
-}
-cudaError_t launch_dup_level(const ForestArgs& a, uint32_t beg, uint32_t end, int baseline, cudaStream_t s) {
-  dup_level_kernel<<<grid_for(end - beg + 1, 256), 256, 0, s>>>(a, beg, end, baseline);
-  note_launch();
-  return cudaGetLastError();
-}
-cudaError_t launch_insert_level(const ForestArgs& a, uint32_t beg, uint32_t end, cudaStream_t s) {
-  insert_level_kernel<<<grid_for(end - beg + 1, 256), 256, 0, s>>>(a, beg, end);
-  note_launch();
+cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, uint32_t epoch2, cudaStream_t s) {
+  if (N < 2) return cudaSuccess;
+  // deepest interior depth: that of node N-2
+  uint32_t dmax = 0;
+  while (((2ull << dmax) - 1) <= (uint64_t)(N - 2)) dmax++;
+  for (int bot = (int)dmax; bot >= 0; bot -= kSpanLevels) {
+    const uint32_t top = bot >= (int)kSpanLevels - 1 ? (uint32_t)bot - (kSpanLevels - 1) : 0;
+    const uint64_t first = (1ull << top) - 1;
+    const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
+    forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot, epoch2);
+    note_launch();
+    if (top == 0) break;
+  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_root_compaction(const uint8_t* labels, const uint8_t* rflag, uint32_t N, uint32_t M, int ascending,
-                                   uint32_t* fo_list, uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch,
-                                   uint64_t* scan_total, cudaStream_t s) {
-  PosToNode map{};
-  map.ascending = ascending;
-  if (!ascending) {
-    // levels by depth, deepest first; depth d holds nodes [2^d - 1, 2^(d+1) - 2]
-    uint32_t D = 0;
-    while (((2ull << D) - 1) < M) D++;  // depth of node M-1
-    uint32_t k = 0;
-    uint64_t pos = 0;
-    for (int d = (int)D; d >= 1; d--) {
-      uint64_t lo = (1ull << d) - 1, hi = (2ull << d) - 2;
-      if (hi > M - 1) hi = M - 1;
-      if (lo > hi) continue;
-      map.t.first_node[k] = (uint32_t)lo;
-      map.t.first_pos[k] = pos;
-      pos += hi - lo + 1;
-      k++;
-    }
-    map.t.nlev = k;
-    map.t.first_pos[k] = pos;
-  }
-  root_prologue_kernel<<<1, 1, 0, s>>>(labels, N, ascending, fo_list, lay);
-  note_launch();
-  cudaError_t e = grid_scan(RootVal{map, rflag}, RootEmit{map, fo_list, sh_list, lay}, nullptr, (uint64_t)M - 1,
-                            scan_scratch, scan_total, s);
-  if (e != cudaSuccess) return e;
+cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M, uint32_t* fo_list,
+                                   uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch, uint64_t* scan_total,
+                                   cudaStream_t s) {
+  const uint64_t n = (uint64_t)M - 1;  // every node but the root
+  uint32_t ntiles = (uint32_t)((n + kScanTile - 1) / kScanTile);
+  if (ntiles == 0) ntiles = 1;
+  root_prologue_kernel<<<1, 1, 0, s>>>(fa.labels, N, fa.ascending, fo_list, lay);
+  root_count_kernel<<<ntiles, kScanThreads, 0, s>>>(fa.rflag, n, scan_scratch);
+  scan_tile_offsets_kernel<<<1, 1024, 0, s>>>(scan_scratch, ntiles, scan_total);
+  root_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
   root_epilogue_kernel<<<1, 1, 0, s>>>(scan_total, lay);
-  note_launch();
+  note_launch(5);
   return cudaGetLastError();
 }
 
@@ -554,23 +643,20 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   note_launch(7);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (g.approach != APPROACH_BASIC) {
-    const uint32_t K = g.cur + 1;
+    const uint32_t K = std::min<uint32_t>(g.cur + 1, kSortFastKeys);  // bound on the distinct keys
     const uint32_t T = (uint32_t)((max_entries + kSortTile - 1) / kSortTile) + 1;
-    const size_t smem = sizeof(uint32_t) * (size_t)K;
-    if (smem > 200 * 1024) return cudaErrorNotSupported;
-    static size_t attr_cnt = 0, attr_sc = 0;
-    if (smem > 48 * 1024 && smem > attr_cnt) {
-      cudaFuncSetAttribute(sort_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr_cnt = smem;
+    const size_t smem_cnt = sizeof(uint32_t) * (size_t)K;
+    const size_t smem_sc = sizeof(uint32_t) * (size_t)K * kSortWarps;
+    static size_t attr_sc = 0;
+    if (smem_sc > 16 * 1024 && smem_sc > attr_sc) {
+      cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sc);
+      attr_sc = smem_sc;
     }
-    if (smem > 48 * 1024 && smem > attr_sc) {
-      cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr_sc = smem;
-    }
-    sort_count_kernel<<<grid_for(T, 1, 16), 256, smem, s>>>(g, T);
-    e = grid_scan(MatVal{g.sort_mat}, MatEmit{g.sort_mat}, nullptr, (uint64_t)K * T, g.scan_scratch2, g.scan_total2, s);
+    sort_count_kernel<<<grid_for(T, 1, 16), 256, smem_cnt, s>>>(g, T);
+    e = grid_scan(MatVal{g.sort_mat}, MatEmit{g.sort_mat}, &g.lay->sort_n, (uint64_t)K * T, g.scan_scratch2,
+                  g.scan_total2, s);
     if (e != cudaSuccess) return e;
-    sort_scatter_kernel<<<grid_for(T, 1, 16), 32, smem, s>>>(g, T);
+    sort_scatter_kernel<<<grid_for(T, 1, 16), 256, smem_sc, s>>>(g, T);
     note_launch(2);
   }
   const bool vec = (g.cs % 16 == 0) && ((reinterpret_cast<uintptr_t>(g.data) & 15) == 0);

@@ -34,53 +34,74 @@ __device__ __forceinline__ uint32_t swz(uint32_t logical) {
   return logical ^ (((logical >> 7) & mask) << 4);
 }
 
+constexpr uint8_t PENDING = 0xFE;  // changed chunk, classified by the insert pass
+
+// Append chunk c to the changed list (one atomic per warp).
+__device__ __forceinline__ void append_changed(bool changed, uint32_t c, uint32_t* list, uint32_t* count) {
+  const unsigned act = __activemask();
+  const unsigned b = __ballot_sync(act, changed);
+  if (!b) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(b) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(b));
+  base = __shfl_sync(act, base, leader);
+  if (changed) list[base + __popc(b & ((1u << lane) - 1))] = c;
+}
+
+// Streaming part of the per-chunk work: compare with the previous digest,
+// store the new one.  Map inserts happen in leaf_insert_kernel so that the
+// hashing pipeline never waits on random memory accesses.
 template <int EPI>
-__device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, uint32_t c, const Digest& dg, const Digest& old) {
+__device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uint32_t c, const Digest& dg,
+                                              const Digest& old) {
   if (EPI == EPI_HASH) {
-    st_digest(a.out + c, dg);
+    if (valid) st_digest(a.out + c, dg);
     return;
   }
   if (EPI == EPI_BASIC) {
+    if (!valid) return;
     uint8_t changed = 1;
     if (!a.basic_first && digest_eq(dg, old)) changed = 0;
     if (changed) st_digest(a.prev + c, dg);
     a.labels[c] = changed;
     return;
   }
-  if (EPI == EPI_TREE) {
-    const uint32_t node = a.leaf_base + c;
-    uint8_t label;
-    if (digest_eq(dg, old)) {
-      // FIXED_DUPL.  The reference also calls insert() here; that insert always
-      // finds the digest (every earlier leaf digest was inserted) and changes
-      // nothing, so it is skipped.
-      label = FIXED_DUPL;
-    } else {
-      uint64_t slot = 0;
+  // tree (src/tree_approach.cpp:326-349) and list (src/list_approach.cpp:50-59)
+  bool changed = false;
+  if (valid) {
+    changed = !digest_eq(dg, old);
+    if (changed) st_digest(a.prev + c, dg);
+    a.labels[c] = changed ? PENDING : (EPI == EPI_TREE ? FIXED_DUPL : DONE);
+    // A FIXED_DUPL leaf's insert() always finds its digest (every earlier
+    // leaf digest was inserted) and changes nothing, so it is not repeated.
+  }
+  append_changed(changed, c, a.changed_list, a.changed_count);
+}
+
+// Map insert of one changed chunk.
+template <int EPI>
+__global__ void leaf_insert_kernel(LeafArgs a) {
+  const uint32_t n = *a.changed_count;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = a.changed_list[k];
+    const Digest dg = ld_digest(a.prev + c);
+    uint64_t slot = 0;
+    uint8_t label = SHIFT_DUPL;
+    if (EPI == EPI_TREE) {
+      const uint32_t node = a.leaf_base + c;
       int r = map_insert(a.map, dg, node, a.cur, a.epoch, &slot, a.err);
-      label = SHIFT_DUPL;
       if (r == INS_NEW) {
         label = FIRST_OCUR;
-        a.chunk_slot[c] = (uint32_t)slot;
       } else if (r == INS_EXISTING) {
         MapSlot* s = &a.map.slots[slot];
         if (__ldcg(&s->tree) == a.cur) {
           atomicMin(&s->node, node);  // lowest offset wins
           label = FIRST_OCUR;
-          a.chunk_slot[c] = (uint32_t)slot;
         }
       }
-      st_digest(a.prev + c, dg);
-    }
-    a.labels[c] = label;
-    return;
-  }
-  if (EPI == EPI_LIST) {
-    uint8_t label = DONE;  // unchanged chunk
-    if (!digest_eq(dg, old)) {
-      uint64_t slot = 0;
+    } else {
       int r = map_insert(a.map, dg, c, a.cur, a.epoch, &slot, a.err);
-      label = SHIFT_DUPL;
       if (r == INS_NEW) {
         label = FIRST_OCUR;
       } else if (r == INS_EXISTING) {
@@ -88,10 +109,22 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, uint32_t c, con
         // a serial backend gives the digest to the lowest changed chunk of this pass
         if (__ldcg(&s->epoch) == a.epoch) { atomicMin(&s->node, c); label = FIRST_OCUR; }
       }
-      a.chunk_slot[c] = (uint32_t)slot;
-      st_digest(a.prev + c, dg);
     }
+    a.chunk_slot[c] = (uint32_t)slot;
     a.labels[c] = label;
+  }
+}
+
+// Second pass (src/tree_approach.cpp:356-369): a first occurrence that does
+// not own its digest becomes a shifted duplicate.
+__global__ void leaf_demote_kernel(LeafArgs a) {
+  const uint32_t n = *a.changed_count;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = a.changed_list[k];
+    if (a.labels[c] != FIRST_OCUR) continue;
+    const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
+    const uint32_t node = a.leaf_base + c;
+    if (a.epi == EPI_TREE ? (s->tree == a.cur && s->node != node) : (s->node != node)) a.labels[c] = SHIFT_DUPL;
   }
 }
 
@@ -191,21 +224,19 @@ __global__ void __launch_bounds__(kThreads) leaf_tma_kernel(const __grid_constan
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
-    if (valid) {
-      Digest dg;
-      if (HK == HASH_MD5) {
-        if (W >= 64) {
+    Digest dg;
+    if (HK == HASH_MD5) {
+      if (W >= 64) {
 #pragma unroll
-          for (int i = 0; i < 16; i++) X[i] = 0;
-          dg = md.finish(X, 0, a.cs);
-        } else {
-          dg = md.finish(X, a.cs, a.cs);
-        }
+        for (int i = 0; i < 16; i++) X[i] = 0;
+        dg = md.finish(X, 0, a.cs);
       } else {
-        dg = mm.finish(a.cs);
+        dg = md.finish(X, a.cs, a.cs);
       }
-      leaf_epilogue<EPI>(a, c, dg, old);
+    } else {
+      dg = mm.finish(a.cs);
     }
+    leaf_epilogue<EPI>(a, valid, c, dg, old);
   }
 }
 
@@ -222,25 +253,7 @@ __global__ void leaf_direct_kernel(LeafArgs a, uint32_t c0, uint32_t c1) {
     Digest old{{0, 0, 0, 0}};
     if (needs_old<EPI>(a)) old = ld_digest(a.prev + c);
     Digest dg = hash_bytes(a.hash_kind, a.data + off, nb);
-    leaf_epilogue<EPI>(a, (uint32_t)c, dg, old);
-  }
-}
-
-__global__ void tree_leaf_finalize_kernel(LeafArgs a) {
-  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n_chunks; c += (uint64_t)gridDim.x * blockDim.x) {
-    if (a.labels[c] == FIRST_OCUR) {
-      const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
-      if (s->tree == a.cur && s->node != a.leaf_base + (uint32_t)c) a.labels[c] = SHIFT_DUPL;
-    }
-  }
-}
-
-__global__ void list_finalize_kernel(LeafArgs a) {
-  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n_chunks; c += (uint64_t)gridDim.x * blockDim.x) {
-    if (a.labels[c] == FIRST_OCUR) {
-      const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
-      if (s->node != (uint32_t)c) a.labels[c] = SHIFT_DUPL;
-    }
+    leaf_epilogue<EPI>(a, true, (uint32_t)c, dg, old);
   }
 }
 
@@ -381,23 +394,12 @@ cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s) {
   return dispatch_direct(a, done, a.n_chunks, s);
 }
 
-cudaError_t launch_tree_leaf_finalize(const LeafArgs& a, cudaStream_t s) {
-  uint32_t grid = (uint32_t)((a.n_chunks + 255) / 256);
-  uint32_t cap = (uint32_t)num_sms() * 8;
-  if (grid > cap) grid = cap;
-  if (grid == 0) return cudaSuccess;
-  tree_leaf_finalize_kernel<<<grid, 256, 0, s>>>(a);
-  note_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_list_finalize(const LeafArgs& a, cudaStream_t s) {
-  uint32_t grid = (uint32_t)((a.n_chunks + 255) / 256);
-  uint32_t cap = (uint32_t)num_sms() * 8;
-  if (grid > cap) grid = cap;
-  if (grid == 0) return cudaSuccess;
-  list_finalize_kernel<<<grid, 256, 0, s>>>(a);
-  note_launch();
+cudaError_t launch_leaf_inserts(const LeafArgs& a, cudaStream_t s) {
+  const uint32_t grid = (uint32_t)num_sms() * 8;
+  if (a.epi == EPI_TREE) leaf_insert_kernel<EPI_TREE><<<grid, 256, 0, s>>>(a);
+  else leaf_insert_kernel<EPI_LIST><<<grid, 256, 0, s>>>(a);
+  leaf_demote_kernel<<<grid, 256, 0, s>>>(a);
+  note_launch(2);
   return cudaGetLastError();
 }
 

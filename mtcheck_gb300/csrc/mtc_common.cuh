@@ -22,6 +22,7 @@ enum : uint32_t {
   DERR_MISSING = 1u << 4,       // a root digest is absent from the map
   DERR_RANGE = 1u << 5,         // restart metadata out of range
   DERR_INTERIOR = 1u << 6,      // restart provenance names an interior node
+  DERR_SORTKEYS = 1u << 7,      // more distinct source checkpoints than the sort supports
 };
 
 struct __align__(16) Digest { uint32_t w[4]; };
@@ -338,6 +339,29 @@ __device__ inline void map_insert_first(const DigestMap& m, const Digest& k, uin
   if (r == INS_EXISTING) {
     MapSlot* s = &m.slots[slot];
     if (__ldcg(&s->epoch) == epoch) atomicMin(&s->node, node);
+  }
+}
+
+// Serial insertion order inside one forest pass: deeper levels first, then
+// ascending node id.  Smaller key = inserted earlier = keeps the entry.
+__device__ __forceinline__ uint64_t serial_prio(uint32_t node) {
+  const uint32_t depth = 31 - __clz(node + 1);
+  return ((uint64_t)(63 - depth) << 32) | node;
+}
+// Insert for a pass that spans several levels in one launch: an entry from an
+// earlier launch is kept; among inserts of this pass the serially first wins.
+__device__ inline void map_insert_serial(const DigestMap& m, const Digest& k, uint32_t node, uint32_t tree,
+                                         uint32_t epoch, uint32_t* err) {
+  uint64_t slot;
+  int r = map_insert(m, k, node, tree, epoch, &slot, err);
+  if (r != INS_EXISTING) return;
+  MapSlot* s = &m.slots[slot];
+  if (__ldcg(&s->epoch) != epoch) return;
+  uint32_t cur = __ldcg(&s->node);
+  for (int i = 0; i < 64 && serial_prio(node) < serial_prio(cur); i++) {
+    uint32_t old = atomicCAS(&s->node, cur, node);
+    if (old == cur) return;
+    cur = old;
   }
 }
 

@@ -21,18 +21,35 @@ struct Layout {
   uint64_t chunk_counter;          // chunk slots in the data section
   uint64_t pad, data_off, table_off, pairs_off, diff_len;
   uint64_t size_data, size_meta;   // the reference's datasizes pair
-  uint32_t root_fo, max_key, ok, reserved;
+  uint32_t root_fo, max_key, ok, nkeys;  // nkeys: distinct sort keys of the shift entries
+  uint32_t sort_n, reserved2;             // nkeys * sort tiles
 };
 
 struct ForestArgs {
   Digest* tree;
   uint8_t* labels;
-  uint8_t* rflag;
+  uint8_t* rflag;  // root flags at canonical positions (M-1 bytes)
   DigestMap map;
   uint32_t cur, epoch;
   uint32_t* err;
   int hash_kind;
+  int ascending;   // canonical order: 0 = deeper levels first (serial push order), 1 = ascending node id
+  uint32_t D;      // depth of node M-1
+  uint64_t sizeD;  // nodes on depth D
 };
+
+// Position of node x (>= 1) in the canonical root order.
+__host__ __device__ __forceinline__ uint64_t canon_pos(const ForestArgs& a, uint32_t x) {
+  if (a.ascending) return (uint64_t)x - 1;
+#ifdef __CUDA_ARCH__
+  const uint32_t d = 31 - __clz(x + 1);
+#else
+  uint32_t d = 0;
+  while (((2ull << d) - 1) <= (uint64_t)x) d++;
+#endif
+  const uint64_t fp = d == a.D ? 0 : a.sizeD + ((1ull << a.D) - (2ull << d));
+  return fp + (x - ((1ull << d) - 1));
+}
 
 struct GatherArgs {
   int approach;
@@ -47,7 +64,7 @@ struct GatherArgs {
   uint64_t* fo_val;
   uint32_t *reg_chunk, *reg_slot, *reg_len;
   uint32_t *sh_key, *sh_prev;
-  uint32_t *hist, *rep;
+  uint32_t *hist, *rep, *rank;
   uint64_t* sort_mat;
   uint64_t *scan_scratch, *scan_total, *scan_scratch2, *scan_total2;
   uint8_t* stage;
@@ -55,12 +72,13 @@ struct GatherArgs {
   Layout* lay;
 };
 
-cudaError_t launch_fo_level(const ForestArgs& a, uint32_t beg, uint32_t end, cudaStream_t s);
-cudaError_t launch_dup_level(const ForestArgs& a, uint32_t beg, uint32_t end, int baseline, cudaStream_t s);
-cudaError_t launch_insert_level(const ForestArgs& a, uint32_t beg, uint32_t end, cudaStream_t s);
-cudaError_t launch_root_compaction(const uint8_t* labels, const uint8_t* rflag, uint32_t N, uint32_t M, int ascending,
-                                   uint32_t* fo_list, uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch,
-                                   uint64_t* scan_total, cudaStream_t s);
+// All levels of one forest pass in a few launches (9 levels each).
+// pass 0 = first-occurrence forest, 1 = duplicate forest; epoch2 is the epoch
+// of the baseline's insert-every-node pass.
+cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, uint32_t epoch2, cudaStream_t s);
+cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M, uint32_t* fo_list,
+                                   uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch, uint64_t* scan_total,
+                                   cudaStream_t s);
 cudaError_t launch_chunk_compaction(const uint8_t* labels, uint32_t n_chunks, int basic, uint32_t* fo_list,
                                     uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch, uint64_t* scan_total,
                                     cudaStream_t s);

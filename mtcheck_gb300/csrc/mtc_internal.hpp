@@ -33,6 +33,8 @@ struct LeafArgs {
   uint32_t epoch = 0;             // launch epoch for the map's first-insert order
   uint32_t leaf_base = 0;         // node id of chunk 0 (N-1 for the tree, 0 for the list)
   uint32_t* err = nullptr;        // device error word
+  uint32_t* changed_list = nullptr;  // chunks whose digest changed (tree, list)
+  uint32_t* changed_count = nullptr;
   int hash_kind = HASH_MURMUR3;
   int epi = EPI_HASH;
   int basic_first = 0;            // basic approach with current_id == 0: every chunk changed
@@ -51,10 +53,10 @@ struct TmaCache {
 // for chunk sizes that are a multiple of 128 bytes (or 16/32/64) on 16-byte
 // aligned buffers, and a thread-per-chunk kernel otherwise and for the tail.
 cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s);
-// Tree: demote FIRST_OCUR leaves that do not own their digest (src/tree_approach.cpp:356-369).
-cudaError_t launch_tree_leaf_finalize(const LeafArgs& a, cudaStream_t s);
-// List: a changed chunk is a first occurrence only if it owns its digest.
-cudaError_t launch_list_finalize(const LeafArgs& a, cudaStream_t s);
+// Tree / list: map inserts of the changed chunks collected by launch_leaves,
+// then the lowest-offset demotion (src/tree_approach.cpp:356-369; for the
+// list a changed chunk is a first occurrence only if it owns its digest).
+cudaError_t launch_leaf_inserts(const LeafArgs& a, cudaStream_t s);
 
 int num_sms();
 // Running count of kernel launches issued by the library (all handles).
