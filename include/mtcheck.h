@@ -93,6 +93,9 @@ int mtc_checkpoint_header(mtc_dedup_t* h, mtc_header_t* header, const void* dev_
                           int make_baseline, uint64_t* diff_len);
 /* checkpoint(uint8_t*, size_t, HostMirror&, bool), :93-96 (advances current_id) */
 int mtc_checkpoint(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_baseline, uint64_t* diff_len);
+/* current_id += 1: what the reference's convenience overloads do after
+ * checkpoint(header_t&, ...) (src/tree_approach.cpp:1723, :1747, :1775) */
+int mtc_advance(mtc_dedup_t* h);
 /* the device->host copy of the diff, src/tree_approach.cpp:1677-1688 */
 int mtc_diff_copy(mtc_dedup_t* h, void* host_dst, uint64_t capacity);
 /* the diff of the last checkpoint in device memory (valid until the next call) */

@@ -57,6 +57,7 @@ SIGNATURES = {
     "mtc_set_stream": (_I, [_VP, _VP]),
     "mtc_checkpoint_header": (_I, [_VP, ctypes.POINTER(Header), _VP, _U64, _I, ctypes.POINTER(_U64)]),
     "mtc_checkpoint": (_I, [_VP, _VP, _U64, _I, ctypes.POINTER(_U64)]),
+    "mtc_advance": (_I, [_VP]),
     "mtc_diff_copy": (_I, [_VP, _VP, _U64]),
     "mtc_diff_device": (_I, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(_U64)]),
     "mtc_checkpoint_alloc": (_I, [_VP, _VP, _U64, _I, ctypes.POINTER(_VP), ctypes.POINTER(_U64)]),

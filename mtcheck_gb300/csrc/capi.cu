@@ -27,6 +27,7 @@ int ret_eng(int rc, mtc::Engine* e) { return ret(rc, e ? e->last_error : std::st
 bool valid_mode(int a) { return a >= MTC_FULL && a <= MTC_TREE_LOW_OFFSET; }
 }  // namespace
 
+
 extern "C" {
 
 int mtc_create(int approach, int hash, uint32_t chunk_size, mtc_dedup_t** out) {
@@ -73,6 +74,12 @@ int mtc_checkpoint(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_
   int rc = mtc_checkpoint_header(h, nullptr, dev_data, len, make_baseline, diff_len);
   if (rc == MTC_OK) h->eng->current_id += 1;
   return rc;
+}
+
+int mtc_advance(mtc_dedup_t* h) {
+  if (!h) return ret(MTC_EINVAL, "NULL handle");
+  h->eng->current_id += 1;
+  return MTC_OK;
 }
 
 int mtc_diff_copy(mtc_dedup_t* h, void* host_dst, uint64_t capacity) {
