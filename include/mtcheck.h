@@ -143,6 +143,28 @@ int mtc_digest_host(int hash, const void* host_data, uint64_t len, uint8_t out[1
 /* its printable form: "XXXXXXXX XXXXXXXX XXXXXXXX XXXXXXXX " (37 bytes incl. NUL) */
 int mtc_digest_hex(const uint8_t digest[16], char out[37]);
 
+/* Checkpoint for callers that cannot allocate memory -- code running inside an
+ * allocator or an out-of-memory handler, a signal or crash handler that saves
+ * state on the way down, or a runtime whose pool owns all GPU memory.  No
+ * counterpart in the reference; it produces the same bytes as the basic
+ * approach (MTC_BASIC) without a handle and without allocating anything:
+ *   dev_digests  caller-owned, 16 bytes per chunk; the previous checkpoint's
+ *                chunk digests on entry (zeros before the first), the current
+ *                ones on return
+ *   first        nonzero for the first checkpoint (every chunk is saved)
+ *   dev_diff     caller-owned device buffer, 4-byte aligned, capacity at least
+ *                32 + chunks * (4 + chunk_size); receives the .basic checkpoint
+ *                (header with ref_id/chkpt_id as given, changed chunk ids in
+ *                ascending order, their data)
+ * At most 4194304 chunks (MTC_ENOTSUP beyond).  Its scratch is a fixed 4 MiB
+ * device array that every GPU loading the library holds until exit; the first
+ * call on a device looks up that array's address, so make that first call
+ * before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
+int mtc_basic_checkpoint_noalloc(int hash, const void* dev_data, uint64_t len, uint32_t chunk_size,
+                                 void* dev_digests, uint32_t ref_id, uint32_t chkpt_id, int first, void* dev_diff,
+                                 uint64_t diff_capacity, uint64_t* diff_len, void* cuda_stream);
+
 /* kernels launched by the library so far (all handles) */
 uint64_t mtc_launch_count(void);
 /* message for the last failing call on this thread */

@@ -72,6 +72,8 @@ SIGNATURES = {
     "mtc_hash_chunks": (_I, [_I, _VP, _U64, _U32, _VP, _VP]),
     "mtc_digest_host": (_I, [_I, _VP, _U64, _VP]),
     "mtc_digest_hex": (_I, [_VP, ctypes.c_char_p]),
+    "mtc_basic_checkpoint_noalloc": (_I, [_I, _VP, _U64, _U32, _VP, _U32, _U32, _I, _VP, _U64,
+                                         ctypes.POINTER(_U64), _VP]),
     "mtc_launch_count": (_U64, []),
     "mtc_last_error": (ctypes.c_char_p, []),
 }

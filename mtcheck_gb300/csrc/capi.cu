@@ -27,6 +27,7 @@ int ret_eng(int rc, mtc::Engine* e) { return ret(rc, e ? e->last_error : std::st
 bool valid_mode(int a) { return a >= MTC_FULL && a <= MTC_TREE_LOW_OFFSET; }
 }  // namespace
 
+void mtc::set_last_error(const char* msg) { t_err = msg ? msg : ""; }
 
 extern "C" {
 

@@ -62,5 +62,7 @@ int num_sms();
 // Running count of kernel launches issued by the library (all handles).
 void note_launch(uint32_t n = 1);
 uint64_t launch_count();
+// Message returned by mtc_last_error() on this thread.
+void set_last_error(const char* msg);
 
 }  // namespace mtc
