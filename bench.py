@@ -42,6 +42,10 @@ def parse():
     p.add_argument("--chunk", type=int, default=512)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-restart", action="store_true")
+    p.add_argument("--restart-gib", type=float, default=1.0)
+    p.add_argument("--restart-chunk", type=int, default=256)
+    p.add_argument("--restart-chain", type=int, default=31)
     return p.parse_args()
 
 
@@ -132,6 +136,66 @@ def make_states(torch, nbytes, cs, count, seed, device):
     for s in workloads.pattern2(nbytes, cs, count, seed=seed, device=device, zero_range=z):
         states.append(s.clone())
     return states
+
+
+def restart_bench(torch, mc, dev, a, kind):
+    """Restart of the last checkpoint of a chain (1 GiB, 256 B chunks, 30
+    incrementals after a baseline, 4 GiB update pattern), tree approach."""
+    from mtcheck_gb300 import workloads
+    nbytes = int(a.restart_gib * GIB) // a.restart_chunk * a.restart_chunk
+    z = (nbytes // 4, nbytes // 4 + nbytes // 8)
+    d = mc.TreeDeduplicator(a.restart_chunk, kind)
+    chain_dev, chain_host, last = [], [], None
+    for i, s in enumerate(workloads.pattern2(nbytes, a.restart_chunk, a.restart_chain, seed=303, device=dev,
+                                             zero_range=z)):
+        n = d.checkpoint_device(s, i == 0)
+        keep = torch.empty(n, dtype=torch.uint8, device=dev)
+        host = torch.empty(n, dtype=torch.uint8).pin_memory()
+        d.copy_diff(host.numpy())
+        keep.copy_(host)
+        chain_dev.append(keep)
+        chain_host.append(host)
+        last = s.clone()
+    torch.cuda.synchronize()
+    out = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    ptrs = [(t.data_ptr(), t.numel()) for t in chain_dev]
+    rid = len(chain_dev) - 1
+    r = mc.TreeDeduplicator(a.restart_chunk, kind)
+    r.restart_device(out, ptrs, rid)  # warm-up
+    ok = bool(torch.equal(out, last))
+    reps = 5
+    times, dev_times = [], []
+    for _ in range(reps):
+        out.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.restart_device(out, ptrs, rid)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        dev_times.append(r.info().restart_timers[1])
+        ok = ok and bool(torch.equal(out, last))
+    dev_t = statistics.median(dev_times)
+    call_t = statistics.median(times)
+    chain_bytes = sum(t.numel() for t in chain_dev)
+    # chain in pinned host memory: H2D inside the call (mtc_restart)
+    host_list = [h.numpy().tobytes() for h in chain_host]
+    e2e_t = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.restart(out, host_list, rid)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+        ok = ok and bool(torch.equal(out, last))
+    return {"workload": "restart of checkpoint %d of a tree chain, %.3g GiB buffer, %d B chunks, 4 GiB update "
+                        "pattern" % (rid, a.restart_gib, a.restart_chunk),
+            "value": round(nbytes / dev_t / 1e9, 3), "unit": "GB/s", "ms": round(dev_t * 1e3, 3),
+            "call_ms": round(call_t * 1e3, 3),
+            "chain_bytes": int(chain_bytes), "verified_byte_identical": ok,
+            "host_chain_value": round(nbytes / statistics.median(e2e_t) / 1e9, 3),
+            "host_chain_ms": round(statistics.median(e2e_t) * 1e3, 3),
+            "note": "value: device time with the chain resident in HBM; call_ms adds the host side of the call; "
+                    "host_chain_value: chain in pageable host memory, copied to HBM inside the call"}
 
 
 def cpu_sample(kind, cs, seconds_hint=20.0):
@@ -303,6 +367,12 @@ def main():
                "d2h_bytes_per_step": int(d2h / K)}
         del host, pinned_out, outs
 
+    rst = None
+    if not a.no_restart and rank == 0:
+        del states
+        torch.cuda.empty_cache()
+        rst = restart_bench(torch, mc, dev, a, kind)
+
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu:
         v, nsteps = cpu_sample(1 if a.hash == "md5" else 0, cs)
@@ -331,6 +401,7 @@ def main():
                          else "fallback 6.8 TB/s"},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "restart": rst,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }

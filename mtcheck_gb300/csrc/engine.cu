@@ -22,7 +22,9 @@ Engine::Engine(int mode, int hash_kind, uint32_t chunk_size) : mode_(mode), hash
   for (auto& e : ev_) cudaEventCreate(&e);
   cudaMallocHost(&lay_host_, sizeof(Layout));
   cudaMallocHost(&err_host_, 2 * sizeof(uint32_t));
+  cudaMallocHost(&sp_host_, sizeof(StepParams));
   std::memset(lay_host_, 0, sizeof(Layout));
+  std::memset(sp_host_, 0, sizeof(StepParams));
 }
 
 Engine::~Engine() {
@@ -30,6 +32,7 @@ Engine::~Engine() {
   for (auto& e : ev_) if (e) cudaEventDestroy(e);
   if (lay_host_) cudaFreeHost(lay_host_);
   if (err_host_) cudaFreeHost(err_host_);
+  if (sp_host_) cudaFreeHost(sp_host_);
   destroy_restart_scratch(rs_);
 }
 
@@ -118,6 +121,7 @@ int Engine::ensure_state(uint32_t N, bool fresh) {
     MTC_CUDA(scan_total_.ensure(1, stream_));
     MTC_CUDA(scan_total2_.ensure(1, stream_));
     MTC_CUDA(lay_.ensure(1, stream_));
+    MTC_CUDA(sp_.ensure(1, stream_));
     if (mode_ != MODE_BASIC) {
       int rc = ensure_map(tree ? M : N, true);
       if (rc) return rc;
@@ -139,8 +143,8 @@ GatherArgs Engine::gather_args(const uint8_t* data, uint64_t len) {
   g.cs = cs_;
   g.N = N_;
   g.M = M_;
-  g.cur = current_id;
-  g.baseline_id = baseline_id;
+  g.sp = sp_.p;
+  g.k_cap = (uint32_t)hist_.n;
   g.digests = digests_.p;
   g.map = DigestMap{slots_.p, map_cap_ ? map_cap_ - 1 : 0, map_size_.p};
   g.err = err_.p;
@@ -178,8 +182,7 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.labels = labels_.p + (N - 1);
   la.chunk_slot = chunk_slot_.p;
   la.map = map;
-  la.cur = current_id;
-  la.epoch = ++epoch_;
+  la.sp = sp_.p;
   la.leaf_base = N - 1;
   la.err = err_.p;
   la.hash_kind = hash_kind_;
@@ -196,17 +199,15 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   fa.labels = labels_.p;
   fa.rflag = rflag_.p;
   fa.map = map;
-  fa.cur = current_id;
+  fa.sp = sp_.p;
   fa.err = err_.p;
   fa.hash_kind = hash_kind_;
   fa.ascending = mode_ == MODE_TREE_LOW_OFFSET_REF ? 1 : 0;
   fa.D = 0;
   while (((2ull << fa.D) - 1) <= (uint64_t)(M - 1)) fa.D++;  // depth of node M-1
   fa.sizeD = (uint64_t)M - ((1ull << fa.D) - 1);
-  fa.epoch = ++epoch_;
-  MTC_CUDA(launch_forest(fa, 0, 0, N, 0, stream_));  // first-occurrence forest
-  const uint32_t e2 = ++epoch_;
-  MTC_CUDA(launch_forest(fa, 1, baseline_path ? 1 : 0, N, e2, stream_));  // duplicate forest
+  MTC_CUDA(launch_forest(fa, 0, 0, N, stream_));                         // first-occurrence forest
+  MTC_CUDA(launch_forest(fa, 1, baseline_path ? 1 : 0, N, stream_));  // duplicate forest
   MTC_CUDA(launch_root_compaction(fa, N, M, fo_list_.p, sh_list_.p, lay_.p, scan_.p, scan_total_.p, stream_));
   return ST_OK;
 }
@@ -221,8 +222,7 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.labels = labels_.p;
   la.chunk_slot = chunk_slot_.p;
   la.map = DigestMap{slots_.p, map_cap_ ? map_cap_ - 1 : 0, map_size_.p};
-  la.cur = current_id;
-  la.epoch = ++epoch_;
+  la.sp = sp_.p;
   la.leaf_base = 0;
   la.err = err_.p;
   la.hash_kind = hash_kind_;
@@ -274,6 +274,12 @@ int Engine::checkpoint(const uint8_t* data, uint64_t len, bool make_baseline, He
   if (rc) return rc;
   data_len = len;
   if (current_id == 0 || make_baseline) baseline_id = current_id;
+  // the previous call synchronised the stream, so the pinned block is free
+  sp_host_->cur = current_id;
+  sp_host_->baseline_id = baseline_id;
+  sp_host_->epoch = epoch_ + 1;
+  epoch_ += kEpochsPerCheckpoint;
+  MTC_CUDA(cudaMemcpyAsync(sp_.p, sp_host_, sizeof(StepParams), cudaMemcpyHostToDevice, stream_));
   MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
   MTC_CUDA(cudaEventRecord(ev_[1], stream_));
   if (mode_ == MODE_LIST || mode_ == MODE_BASIC) {

@@ -131,6 +131,8 @@ class Engine {
   DevBuf<uint64_t> fo_val_, sort_mat_, scan_, scan_total_, scan2_, scan_total2_;
   DevBuf<uint8_t> stage_;
   DevBuf<Layout> lay_;
+  DevBuf<StepParams> sp_;
+  StepParams* sp_host_ = nullptr;   // pinned
   Layout* lay_host_ = nullptr;      // pinned
   uint32_t* err_host_ = nullptr;    // pinned [err, map size]
   uint64_t diff_len_ = 0, diff_pad_ = 0;

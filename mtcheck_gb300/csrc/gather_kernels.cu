@@ -46,8 +46,9 @@ __device__ __forceinline__ uint8_t child_flag(uint8_t lab) {
 // inserts every interior node (:155-227).
 constexpr uint32_t kSpanLevels = 9;  // 256 nodes on the bottom level of a span
 __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass, int baseline, uint32_t N,
-                                                          uint32_t d_top, uint32_t d_bot, uint32_t epoch2) {
+                                                          uint32_t d_top, uint32_t d_bot) {
   __shared__ uint8_t lab[2][2 << (kSpanLevels - 1)];
+  const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1, epoch_all = a.sp->epoch + 2;
   const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
   const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
   if (r > last_interior) return;
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass
           lab_n = FIRST_OCUR;
           Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
           st_digest(a.tree + n, dg);
-          map_insert_serial(a.map, dg, (uint32_t)n, a.cur, a.epoch, a.err);
+          map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_fo, a.err);
         } else {
           lab_n = DONE;
         }
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass
         if (baseline) {
           Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
           st_digest(a.tree + n, dg);
-          map_insert_serial(a.map, dg, (uint32_t)n, a.cur, epoch2, a.err);
+          map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_all, a.err);
         }
       }
       cur[i] = lab_n;
@@ -209,12 +210,13 @@ __global__ void root_epilogue_kernel(const uint64_t* total, Layout* lay) {
 // First-occurrence roots: region size if the root owns its digest.
 __global__ void fo_prep_kernel(GatherArgs g) {
   const uint32_t F = g.lay->F;
+  const uint32_t cur = g.sp->cur;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F; i += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t node = g.fo_list[i];
     uint64_t v = 0;
     if (g.approach == APPROACH_TREE) {
       NodeIdDev prev = slot_value(g.map, map_find(g.map, ld_digest(g.digests + node), g.err));
-      if (prev.node == node && prev.tree == g.cur) v = (1ull << 32) | num_leaf_descendents(node, g.M);
+      if (prev.node == node && prev.tree == cur) v = (1ull << 32) | num_leaf_descendents(node, g.M);
     } else {
       v = (1ull << 32) | 1ull;  // list / basic: one chunk per entry
     }
@@ -246,11 +248,12 @@ __global__ void fo_totals_kernel(const uint64_t* total, Layout* lay) {
 // Shifted duplicates: (source checkpoint, source node) of each root.
 __global__ void shift_prep_kernel(GatherArgs g) {
   const uint32_t S = g.lay->S;
+  const uint32_t cur = g.sp->cur;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t node = g.sh_list[i];
     int64_t slot = map_find(g.map, ld_digest(g.digests + node), g.err);
     NodeIdDev prev = slot_value(g.map, slot);
-    if (slot < 0 || prev.tree > g.cur) { atomicOr(g.err, DERR_MISSING); prev.tree = 0; prev.node = 0; }
+    if (slot < 0 || prev.tree > cur) { atomicOr(g.err, DERR_MISSING); prev.tree = 0; prev.node = 0; }
     g.sh_key[i] = prev.tree;
     g.sh_prev[i] = prev.node;
     atomicAdd(&g.hist[prev.tree], 1u);
@@ -262,7 +265,8 @@ __global__ void shift_prep_kernel(GatherArgs g) {
 __global__ void layout_kernel(GatherArgs g) {
   __shared__ uint64_t sh[33];
   Layout* lay = g.lay;
-  const uint32_t K = g.cur + 1;
+  const uint32_t cur = g.sp->cur;
+  const uint32_t K = cur + 1;
   const uint32_t F = lay->F, S = lay->S, nd = lay->num_distinct;
   // P = number of source checkpoints that occur; max_key = largest of them
   __shared__ uint32_t smax;
@@ -324,8 +328,8 @@ __global__ void layout_kernel(GatherArgs g) {
   if (threadIdx.x == 0) {
     // header_t, include/utils.hpp:29-37
     uint32_t* h32 = reinterpret_cast<uint32_t*>(diff);
-    h32[0] = g.baseline_id;
-    h32[1] = g.cur;
+    h32[0] = g.sp->baseline_id;
+    h32[1] = cur;
     h32[2] = (uint32_t)g.len;
     h32[3] = (uint32_t)(g.len >> 32);
     h32[4] = g.cs;
@@ -352,8 +356,8 @@ __global__ void layout_kernel(GatherArgs g) {
   }
   // sort representative of each key: stable sort by BinOp1D bin equals stable
   // sort by the smallest key sharing the bin
-  const uint32_t nbins = g.approach == APPROACH_TREE ? g.cur : S;
-  const double range = (double)(g.approach == APPROACH_TREE ? g.cur : max_key);
+  const uint32_t nbins = g.approach == APPROACH_TREE ? cur : S;
+  const double range = (double)(g.approach == APPROACH_TREE ? cur : max_key);
   const double mul = (range <= (double)nbins) ? 1.0 : (double)nbins / range;
   for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
     int bk = (int)(mul * (double)k);
@@ -580,7 +584,7 @@ cudaError_t launch_map_rehash(const DigestMap& from, uint64_t from_cap, const Di
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, uint32_t epoch2, cudaStream_t s) {
+cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, cudaStream_t s) {
   if (N < 2) return cudaSuccess;
   // deepest interior depth: that of node N-2
   uint32_t dmax = 0;
@@ -589,7 +593,7 @@ cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t 
     const uint32_t top = bot >= (int)kSpanLevels - 1 ? (uint32_t)bot - (kSpanLevels - 1) : 0;
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
-    forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot, epoch2);
+    forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot);
     note_launch();
     if (top == 0) break;
   }
@@ -628,7 +632,7 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   // pad depends on F, P, S; P needs the histogram.  Order: shift prep
   // (histogram), FO prep + scan (region sizes), layout (pad, table, header),
   // FO emit (metadata + regions), sort, copy.
-  cudaMemsetAsync(g.hist, 0, sizeof(uint32_t) * ((size_t)g.cur + 1), s);
+  cudaMemsetAsync(g.hist, 0, sizeof(uint32_t) * (size_t)g.k_cap, s);
   const uint32_t gs = grid_for(max_entries, 256);
   shift_prep_kernel<<<gs, 256, 0, s>>>(g);
   fo_prep_kernel<<<gs, 256, 0, s>>>(g);
@@ -643,7 +647,9 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   note_launch(7);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (g.approach != APPROACH_BASIC) {
-    const uint32_t K = std::min<uint32_t>(g.cur + 1, kSortFastKeys);  // bound on the distinct keys
+    // bound on the distinct keys (source checkpoints): at most k_cap, which
+    // covers every checkpoint id that this launch sequence can see
+    const uint32_t K = std::min<uint32_t>(g.k_cap, kSortFastKeys);
     const uint32_t T = (uint32_t)((max_entries + kSortTile - 1) / kSortTile) + 1;
     const size_t smem_cnt = sizeof(uint32_t) * (size_t)K;
     const size_t smem_sc = sizeof(uint32_t) * (size_t)K * kSortWarps;

@@ -83,6 +83,7 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uin
 template <int EPI>
 __global__ void leaf_insert_kernel(LeafArgs a) {
   const uint32_t n = *a.changed_count;
+  const uint32_t cur = a.sp->cur, epoch = a.sp->epoch;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = a.changed_list[k];
     const Digest dg = ld_digest(a.prev + c);
@@ -90,24 +91,24 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
     uint8_t label = SHIFT_DUPL;
     if (EPI == EPI_TREE) {
       const uint32_t node = a.leaf_base + c;
-      int r = map_insert(a.map, dg, node, a.cur, a.epoch, &slot, a.err);
+      int r = map_insert(a.map, dg, node, cur, epoch, &slot, a.err);
       if (r == INS_NEW) {
         label = FIRST_OCUR;
       } else if (r == INS_EXISTING) {
         MapSlot* s = &a.map.slots[slot];
-        if (__ldcg(&s->tree) == a.cur) {
+        if (__ldcg(&s->tree) == cur) {
           atomicMin(&s->node, node);  // lowest offset wins
           label = FIRST_OCUR;
         }
       }
     } else {
-      int r = map_insert(a.map, dg, c, a.cur, a.epoch, &slot, a.err);
+      int r = map_insert(a.map, dg, c, cur, epoch, &slot, a.err);
       if (r == INS_NEW) {
         label = FIRST_OCUR;
       } else if (r == INS_EXISTING) {
         MapSlot* s = &a.map.slots[slot];
         // a serial backend gives the digest to the lowest changed chunk of this pass
-        if (__ldcg(&s->epoch) == a.epoch) { atomicMin(&s->node, c); label = FIRST_OCUR; }
+        if (__ldcg(&s->epoch) == epoch) { atomicMin(&s->node, c); label = FIRST_OCUR; }
       }
     }
     a.chunk_slot[c] = (uint32_t)slot;
@@ -119,12 +120,13 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
 // not own its digest becomes a shifted duplicate.
 __global__ void leaf_demote_kernel(LeafArgs a) {
   const uint32_t n = *a.changed_count;
+  const uint32_t cur = a.sp->cur;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = a.changed_list[k];
     if (a.labels[c] != FIRST_OCUR) continue;
     const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
     const uint32_t node = a.leaf_base + c;
-    if (a.epi == EPI_TREE ? (s->tree == a.cur && s->node != node) : (s->node != node)) a.labels[c] = SHIFT_DUPL;
+    if (a.epi == EPI_TREE ? (s->tree == cur && s->node != node) : (s->node != node)) a.labels[c] = SHIFT_DUPL;
   }
 }
 

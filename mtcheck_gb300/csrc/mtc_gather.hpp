@@ -30,7 +30,7 @@ struct ForestArgs {
   uint8_t* labels;
   uint8_t* rflag;  // root flags at canonical positions (M-1 bytes)
   DigestMap map;
-  uint32_t cur, epoch;
+  const StepParams* sp;  // cur, epochs (device)
   uint32_t* err;
   int hash_kind;
   int ascending;   // canonical order: 0 = deeper levels first (serial push order), 1 = ascending node id
@@ -55,7 +55,9 @@ struct GatherArgs {
   int approach;
   const uint8_t* data;
   uint64_t len;
-  uint32_t cs, N, M, cur, baseline_id;
+  uint32_t cs, N, M;
+  const StepParams* sp;   // cur, baseline_id (device)
+  uint32_t k_cap;         // capacity of hist / rep / rank (checkpoint ids + 1)
   const Digest* digests;  // tree heap (by node) or hash list (by chunk)
   DigestMap map;
   uint32_t* err;
@@ -73,9 +75,8 @@ struct GatherArgs {
 };
 
 // All levels of one forest pass in a few launches (9 levels each).
-// pass 0 = first-occurrence forest, 1 = duplicate forest; epoch2 is the epoch
-// of the baseline's insert-every-node pass.
-cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, uint32_t epoch2, cudaStream_t s);
+// pass 0 = first-occurrence forest, 1 = duplicate forest.
+cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, cudaStream_t s);
 cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M, uint32_t* fo_list,
                                    uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch, uint64_t* scan_total,
                                    cudaStream_t s);

@@ -19,6 +19,18 @@ enum LeafEpi : int {
   EPI_BASIC = 3,  // BasicDeduplicator::dedup_data (src/basic_approach.cpp:25-46)
 };
 
+// Per-checkpoint values that kernels read from device memory, so that one
+// launch sequence (or a captured graph) serves every checkpoint of a chain.
+// Epochs used in one checkpoint: epoch (leaf inserts), epoch + 1 (first-
+// occurrence forest), epoch + 2 (the baseline's insert-every-node pass).
+struct StepParams {
+  uint32_t cur;          // current_id
+  uint32_t baseline_id;  // reference checkpoint written into the header
+  uint32_t epoch;
+  uint32_t pad;
+};
+constexpr uint32_t kEpochsPerCheckpoint = 3;
+
 struct LeafArgs {
   const uint8_t* data = nullptr;  // device buffer being checkpointed
   uint64_t len = 0;               // bytes
@@ -29,8 +41,7 @@ struct LeafArgs {
   uint32_t* chunk_slot = nullptr; // per-chunk map slot of a changed chunk
   Digest* out = nullptr;          // EPI_HASH output
   DigestMap map{};
-  uint32_t cur = 0;               // current checkpoint id
-  uint32_t epoch = 0;             // launch epoch for the map's first-insert order
+  const StepParams* sp = nullptr; // current checkpoint id and launch epoch (device)
   uint32_t leaf_base = 0;         // node id of chunk 0 (N-1 for the tree, 0 for the list)
   uint32_t* err = nullptr;        // device error word
   uint32_t* changed_list = nullptr;  // chunks whose digest changed (tree, list)

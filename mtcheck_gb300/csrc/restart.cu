@@ -238,32 +238,70 @@ __device__ __forceinline__ uint32_t upper_entry(const uint64_t* excl, uint32_t n
   return lo;
 }
 
+// Items numbered by an exclusive prefix over entries are processed in tiles of
+// kExpandTile per block: the entries overlapping a tile (each entry has at
+// least one item) are staged in shared memory once, and every item finds its
+// entry by a binary search there instead of in global memory.
+constexpr uint32_t kExpandTile = 2048;
+struct ExpandTile {
+  uint64_t ex[kExpandTile + 1];
+  uint32_t e0, cnt;
+};
+__device__ __forceinline__ void expand_stage(ExpandTile& T, const uint64_t* excl, uint32_t n, uint64_t t0,
+                                             uint64_t t1) {
+  if (threadIdx.x == 0) {
+    const uint32_t e0 = upper_entry(excl, n, t0), e1 = upper_entry(excl, n, t1 - 1);
+    T.e0 = e0;
+    T.cnt = e1 - e0 + 1;
+  }
+  __syncthreads();
+  const uint32_t cnt = T.cnt <= kExpandTile + 1 ? T.cnt : 0;
+  for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) T.ex[i] = excl[T.e0 + i];
+  __syncthreads();
+}
+__device__ __forceinline__ uint32_t expand_entry(const ExpandTile& T, const uint64_t* excl, uint32_t n,
+                                                 uint64_t item) {
+  if (T.cnt > kExpandTile + 1) return upper_entry(excl, n, item);
+  uint32_t lo = 0, hi = T.cnt - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi + 1) >> 1;
+    if (T.ex[mid] <= item) lo = mid; else hi = mid - 1;
+  }
+  return T.e0 + lo;
+}
+
 // main scatter: which entry writes node_list / copies each chunk last
 // (src/tree_approach.cpp:825-925; ranks: FO entries 1+i, shift entries 2^32+i)
-__global__ void main_cover_kernel(RArgs a) {
+// which = 0: FO regions (prefix fo_excl, total tot[2]); 1: shift regions
+// (prefix sh_excl, total tot[3])
+__global__ void __launch_bounds__(256) main_cover_kernel(RArgs a, int which) {
+  __shared__ ExpandTile T;
   const DiffInfo& d = a.di[0];
-  const uint64_t nfo_items = a.tot[2], nsh_items = a.tot[3];
-  const uint64_t total = nfo_items + nsh_items;
+  const uint64_t total = a.tot[2 + which];
+  const uint64_t* excl = which ? a.sh_excl : a.fo_excl;
+  const uint32_t n = which ? d.S : d.F;
   const bool tree = a.approach == APPROACH_TREE;
-  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
-    if (t < nfo_items) {
-      uint32_t i = upper_entry(a.fo_excl, d.F, t);
-      uint32_t j = (uint32_t)(t - a.fo_excl[i]);
-      uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.fo_node[i], a.M) - (a.N - 1) + j) : a.fo_node[i];
-      if (c >= a.N) continue;
-      const unsigned long long r = 1ull + i;
-      atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
-      atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
-    } else {
-      uint64_t tt = t - nfo_items;
-      uint32_t i = upper_entry(a.sh_excl, d.S, tt);
-      uint32_t j = (uint32_t)(tt - a.sh_excl[i]);
-      uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1) + j) : a.sh_node[i];
-      if (c >= a.N) continue;
-      const unsigned long long r = (1ull << 32) + i;
-      atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
-      if (a.sh_tree[i] == d.id) atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
+  for (uint64_t t0 = (uint64_t)blockIdx.x * kExpandTile; t0 < total; t0 += (uint64_t)gridDim.x * kExpandTile) {
+    const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
+    expand_stage(T, excl, n, t0, t1);
+    for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+      const uint32_t i = expand_entry(T, excl, n, t);
+      const uint32_t j = (uint32_t)(t - excl[i]);
+      if (which == 0) {
+        uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.fo_node[i], a.M) - (a.N - 1) + j) : a.fo_node[i];
+        if (c >= a.N) continue;
+        const unsigned long long r = 1ull + i;
+        atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
+        atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
+      } else {
+        uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1) + j) : a.sh_node[i];
+        if (c >= a.N) continue;
+        const unsigned long long r = (1ull << 32) + i;
+        atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
+        if (a.sh_tree[i] == d.id) atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -365,67 +403,71 @@ struct ChainRmCount {
 __device__ __forceinline__ uint32_t key_of_leaf(const RArgs& a, uint32_t x) { return x - (a.N - 1); }
 
 // pass 0: set the initial value of every covered table cell and its mask bit;
-// pass 1: lowest rank wins
-__global__ void chain_tables_kernel(RArgs a, int pass) {
+// pass 1: lowest rank wins.  which = 0: distinct-map keys of the FO entries,
+// 1: repeat-map keys of the shift entries.
+__global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a, int pass, int which) {
+  __shared__ ExpandTile T;
   if (a.nsteps == 0) return;
-  const uint64_t ndm = a.tot[0], nrm = a.tot[1];
-  const uint32_t nfo_chain = a.nfo - a.di[1].fo_begin, nsh_chain = a.nsh - a.di[1].sh_begin;
+  const uint64_t total = a.tot[which];
+  const uint32_t n = which ? a.nsh - a.di[1].sh_begin : a.nfo - a.di[1].fo_begin;
+  const uint64_t* excl = which ? a.rm_excl : a.dm_excl;
   const bool tree = a.approach == APPROACH_TREE;
-  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ndm + nrm; t += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t key, rank, s;
-    bool dm = t < ndm;
-    if (dm) {
-      const uint32_t k = upper_entry(a.dm_excl, nfo_chain, t);
-      const uint64_t g = a.di[1].fo_begin + k;
-      s = a.fo_seg[g] - 1;
-      rank = (uint32_t)g - a.di[1 + s].fo_begin;
-      uint64_t j = t - a.dm_excl[k];
-      if (tree) {
-        uint32_t lo[2], hi[2];
-        int n = fo_leaf_ranges(a.fo_node[g], a.N, a.M, lo, hi);
-        uint32_t x = 0;
-        for (int r = 0; r < n; r++) {
-          uint64_t sz = hi[r] - lo[r] + 1;
-          if (j < sz) { x = lo[r] + (uint32_t)j; break; }
-          j -= sz;
-        }
-        key = key_of_leaf(a, x);
-      } else {
-        key = a.fo_node[g];
-        if (key >= a.N) continue;
-      }
-    } else {
-      const uint64_t tt = t - ndm;
-      const uint32_t k = upper_entry(a.rm_excl, nsh_chain, tt);
-      const uint64_t h = a.di[1].sh_begin + k;
-      s = a.sh_seg[h] - 1;
-      const uint32_t i = (uint32_t)h - a.di[1 + s].sh_begin;
-      const uint64_t j = tt - a.rm_excl[k];
-      if (tree) {
-        const uint32_t node = a.sh_node[h];
-        const uint32_t len = num_leaf_descendents(node, a.M);
-        if (j < len) {
-          const uint32_t x = leftmost_leaf(node, a.M) + (uint32_t)j;
-          if (x < a.N - 1 || x > a.M) continue;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * kExpandTile; t0 < total; t0 += (uint64_t)gridDim.x * kExpandTile) {
+    const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
+    expand_stage(T, excl, n, t0, t1);
+    for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+      const uint32_t k = expand_entry(T, excl, n, t);
+      uint64_t j = t - excl[k];
+      uint32_t key, rank, s;
+      if (which == 0) {
+        const uint64_t g = a.di[1].fo_begin + k;  // chain entries follow the main ones
+        s = a.fo_seg[g] - 1;
+        rank = (uint32_t)g - a.di[1 + s].fo_begin;
+        if (tree) {
+          uint32_t lo[2], hi[2];
+          const int nr = fo_leaf_ranges(a.fo_node[g], a.N, a.M, lo, hi);
+          uint32_t x = 0;
+          for (int r = 0; r < nr; r++) {
+            const uint64_t sz = hi[r] - lo[r] + 1;
+            if (j < sz) { x = lo[r] + (uint32_t)j; break; }
+            j -= sz;
+          }
           key = key_of_leaf(a, x);
-          rank = 2 * i + 1;
         } else {
-          key = key_of_leaf(a, node);
+          key = a.fo_node[g];
+          if (key >= a.N) continue;
+        }
+      } else {
+        const uint64_t h = a.di[1].sh_begin + k;
+        s = a.sh_seg[h] - 1;
+        const uint32_t i = (uint32_t)h - a.di[1 + s].sh_begin;
+        if (tree) {
+          const uint32_t node = a.sh_node[h];
+          const uint32_t len = num_leaf_descendents(node, a.M);
+          if (j < len) {
+            const uint32_t x = leftmost_leaf(node, a.M) + (uint32_t)j;
+            if (x < a.N - 1 || x > a.M) continue;
+            key = key_of_leaf(a, x);
+            rank = 2 * i + 1;
+          } else {
+            key = key_of_leaf(a, node);
+            rank = 2 * i;
+          }
+        } else {
+          key = a.sh_node[h];
+          if (key >= a.N) continue;
           rank = 2 * i;
         }
+      }
+      uint32_t* tab = (which ? a.rm_tab : a.dm_tab) + (uint64_t)s * a.K + key;
+      if (pass == 0) {
+        *tab = 0xffffffffu;
+        atomicOr((which ? a.rm_mask : a.dm_mask) + (uint64_t)key * a.W + (s >> 5), 1u << (s & 31));
       } else {
-        key = a.sh_node[h];
-        if (key >= a.N) continue;
-        rank = 2 * i;
+        atomicMin(tab, rank);
       }
     }
-    uint32_t* tab = (dm ? a.dm_tab : a.rm_tab) + (uint64_t)s * a.K + key;
-    if (pass == 0) {
-      *tab = 0xffffffffu;
-      atomicOr((dm ? a.dm_mask : a.rm_mask) + (uint64_t)key * a.W + (s >> 5), 1u << (s & 31));
-    } else {
-      atomicMin(tab, rank);
-    }
+    __syncthreads();
   }
 }
 
@@ -499,36 +541,44 @@ __global__ void walk_kernel(RArgs a) {
   }
 }
 
-// 5. one copy per chunk from the diff that owns it
+// 5. one copy per chunk from the diff that owns it; one thread per 16-byte
+//    unit of the output (chunk sizes that are not multiples of 16 go byte by byte)
 __global__ void gather_kernel(RArgs a) {
   const uint64_t cs = a.cs;
-  const uint32_t lanes = 32;
-  const uint32_t lane = threadIdx.x & 31;
-  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t c = warp; c < a.N; c += nwarps) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (cs % 16 == 0) {
+    const uint64_t units = (a.datalen + 15) / 16;
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += stride) {
+      const uint64_t byte = u * 16, c = byte / cs, within = byte - c * cs;
+      const uint64_t r = a.res[c];
+      if (r == kNone) continue;
+      const DiffInfo& d = a.di[r >> kOffBits];
+      const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1)) + within;
+      uint64_t n = 16;
+      if (byte + n > a.datalen) n = a.datalen - byte;
+      if (c * cs + cs > a.datalen && within + n > a.datalen - c * cs) n = a.datalen - c * cs - within;
+      if (off >= d.len) continue;
+      if (off + n > d.len) n = d.len - off;
+      const uint8_t* src = d.base + off;
+      uint8_t* dst = a.out + byte;
+      if (n == 16 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+        *reinterpret_cast<uint4*>(dst) = __ldcs(reinterpret_cast<const uint4*>(src));
+      } else if (n == 16 && (((uintptr_t)src | (uintptr_t)dst) & 3) == 0) {
+        const uint32_t* s4 = reinterpret_cast<const uint32_t*>(src);
+        *reinterpret_cast<uint4*>(dst) = make_uint4(s4[0], s4[1], s4[2], s4[3]);
+      } else {
+        for (uint64_t b = 0; b < n; b++) dst[b] = src[b];
+      }
+    }
+    return;
+  }
+  for (uint64_t byte = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; byte < a.datalen; byte += stride) {
+    const uint64_t c = byte / cs, within = byte - c * cs;
     const uint64_t r = a.res[c];
     if (r == kNone) continue;
     const DiffInfo& d = a.di[r >> kOffBits];
-    const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1));
-    uint64_t n = cs;
-    if (c * cs + n > a.datalen) n = a.datalen - c * cs;
-    if (off >= d.len) continue;
-    if (off + n > d.len) n = d.len - off;
-    const uint8_t* src = d.base + off;
-    uint8_t* dst = a.out + c * cs;
-    if ((((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
-      const uint64_t nv = n / 16;
-      for (uint64_t k = lane; k < nv; k += lanes)
-        reinterpret_cast<uint4*>(dst)[k] = __ldcs(reinterpret_cast<const uint4*>(src) + k);
-      for (uint64_t b = nv * 16 + lane; b < n; b += lanes) dst[b] = src[b];
-    } else if ((((uintptr_t)src | (uintptr_t)dst) & 3) == 0) {
-      const uint64_t nv = n / 4;
-      for (uint64_t k = lane; k < nv; k += lanes) reinterpret_cast<uint32_t*>(dst)[k] = reinterpret_cast<const uint32_t*>(src)[k];
-      for (uint64_t b = nv * 4 + lane; b < n; b += lanes) dst[b] = src[b];
-    } else {
-      for (uint64_t b = lane; b < n; b += lanes) dst[b] = src[b];
-    }
+    const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1)) + within;
+    if (off < d.len) a.out[byte] = d.base[off];
   }
 }
 
@@ -702,9 +752,10 @@ int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint
     MTC_CUDA_R(grid_scan(MainShiftLen{R.sh_prev.p, M, tree ? 1 : 0}, StoreExcl{R.sh_excl.p}, nullptr, di[0].S,
                          R.scan.p, R.tot.p + 3, s));
   }
-  main_cover_kernel<<<gsz(N), 256, 0, s>>>(a);
+  main_cover_kernel<<<num_sms() * 4, 256, 0, s>>>(a, 0);
+  main_cover_kernel<<<num_sms() * 4, 256, 0, s>>>(a, 1);
   main_resolve_kernel<<<gsz(N), 256, 0, s>>>(a);
-  note_launch(2);
+  note_launch(3);
   // chain
   if (nsteps) {
     MTC_CUDA_R(cudaMemsetAsync(R.dm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
@@ -714,12 +765,13 @@ int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint
       MTC_CUDA_R(grid_scan(ChainDmCount{a}, StoreExcl{R.dm_excl.p}, nullptr, nfo_chain, R.scan.p, R.tot.p + 0, s));
     if (nsh_chain && !basic)
       MTC_CUDA_R(grid_scan(ChainRmCount{a}, StoreExcl{R.rm_excl.p}, nullptr, nsh_chain, R.scan.p, R.tot.p + 1, s));
-    chain_tables_kernel<<<gsz((uint64_t)N * 2), 256, 0, s>>>(a, 0);
-    chain_tables_kernel<<<gsz((uint64_t)N * 2), 256, 0, s>>>(a, 1);
+    for (int pass = 0; pass < 2; pass++)
+      for (int which = 0; which < 2; which++)
+        chain_tables_kernel<<<num_sms() * 4, 256, 0, s>>>(a, pass, which);
     walk_kernel<<<gsz(N), 256, 0, s>>>(a);
-    note_launch(3);
+    note_launch(5);
   }
-  gather_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
+  gather_kernel<<<num_sms() * 16, 256, 0, s>>>(a);
   note_launch();
   cudaEventRecord(e1, s);
   uint32_t herr = 0;
