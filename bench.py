@@ -46,6 +46,12 @@ def parse():
     p.add_argument("--restart-gib", type=float, default=1.0)
     p.add_argument("--restart-chunk", type=int, default=256)
     p.add_argument("--restart-chain", type=int, default=31)
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--batch-count", type=int, default=96)
+    p.add_argument("--batch-median-mib", type=float, default=72.0)
+    p.add_argument("--batch-steps", type=int, default=5)
+    p.add_argument("--batch-no-tune", action="store_true")
+    p.add_argument("--only-batch", action="store_true")
     return p.parse_args()
 
 
@@ -266,6 +272,130 @@ def run_reference(a, ws, rank):
     return 0
 
 
+class _DevView:
+    """A device address range as a torch tensor (via __cuda_array_interface__)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "|u1", "data": (int(ptr), False),
+                                         "version": 3}
+
+
+def batch_bench(torch, mc, dev, a):
+    """96 buffers of log-normal sizes (1-512 MiB, about 12 GiB), chunk sizes
+    {64, 128, 512, 4096}, Murmur3/MD5 alternating, tree approach, 5 checkpoints
+    of the 4 GiB update pattern with a per-buffer change rate of 0.1-10%:
+    (i) one buffer per call through lone handles, (ii) one batched call per
+    step (eager baseline, CUDA graph replays after), on the same device
+    buffers; every member's diff compared byte for byte on the device."""
+    from mtcheck_gb300 import workloads
+    mix = workloads.batch_mix(count=a.batch_count, median_mib=a.batch_median_mib)
+    total = sum(m["nbytes"] for m in mix)
+    gens, bufs = [], []
+    for m in mix:
+        z = (m["nbytes"] // 4, m["nbytes"] // 4 + m["nbytes"] // 8)
+        g = workloads.pattern2(m["nbytes"], m["chunk_size"], a.batch_steps, seed=m["seed"], device=dev,
+                               rate=(m["rate"], m["rate"]), zero_range=z)
+        gens.append(g)
+        bufs.append(next(g))
+    lone = [mc.TreeDeduplicator(m["chunk_size"], m["hash"]) for m in mix]
+    b = mc.Batch([(mc.TREE, m["hash"], m["chunk_size"]) for m in mix])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if not a.batch_no_tune:
+        b.autotune(bufs)
+    tune_s = time.perf_counter() - t0
+    tunes = [m.tuning() for m in b.members]
+    per_call, batched, batched_dev, identical, diff_total = [], [], [], True, 0
+    per_call_dev, host_parts, mismatches = [], [], []
+    all_pc, all_b = [], []
+    l0 = mc.launch_count()
+    for step in range(a.batch_steps):
+        if step:
+            for i, g in enumerate(gens):
+                bufs[i] = next(g)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lens, pdev = [], 0.0
+        for d, x in zip(lone, bufs):
+            lens.append(d.checkpoint_device(x, step == 0))
+            pdev += sum(d.info().timers[:3])
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        blens = b.checkpoint(bufs, make_baseline=(step == 0))
+        t2 = time.perf_counter()
+        info = b.info()
+        all_pc.append(t1 - t0)
+        all_b.append(t2 - t1)
+        if step:
+            per_call.append(t1 - t0)
+            per_call_dev.append(pdev)
+            batched.append(t2 - t1)
+            batched_dev.append(info.last_device_ms / 1e3)
+            host_parts.append(list(info.host_ms))
+        for i, (d, mem, n, bn) in enumerate(zip(lone, b.members, lens, blens)):
+            pa, na = d.diff_device()
+            pb, nb = mem.diff_device()
+            same = na == nb and n == bn
+            if same:
+                ta = torch.as_tensor(_DevView(pa, na), device=dev)
+                tb = torch.as_tensor(_DevView(pb, nb), device=dev)
+                same = bool(torch.equal(ta, tb))
+                if not same and len(mismatches) < 8:
+                    first = int(torch.nonzero(ta != tb)[0].item())
+                    mismatches.append({"member": i, "step": step, "len": na, "first_byte": first,
+                                       "chunk_size": mix[i]["chunk_size"], "hash": mix[i]["hash"],
+                                       "nbytes": mix[i]["nbytes"], "tune": tunes[i]})
+            elif len(mismatches) < 8:
+                mismatches.append({"member": i, "step": step, "len": [n, na, bn, nb],
+                                   "chunk_size": mix[i]["chunk_size"], "hash": mix[i]["hash"],
+                                   "nbytes": mix[i]["nbytes"], "tune": tunes[i]})
+            identical = identical and same
+            diff_total += nb
+    launches = mc.launch_count() - l0
+    info = b.info()
+    inc = a.batch_steps - 1
+    pc = sum(per_call) / inc
+    bt = sum(batched) / inc
+    steady = sum(batched[1:]) / max(1, inc - 1)
+    res = {
+        "workload": "%d buffers, log-normal sizes %.0f MiB median clipped to [1, 512] MiB (%.2f GiB total), chunk "
+                    "sizes {64,128,512,4096}, Murmur3/MD5 alternating, tree approach, %d checkpoints, change rate "
+                    "0.1-10%% per buffer, 4 GiB update pattern" % (len(mix), a.batch_median_mib, total / GIB,
+                                                                   a.batch_steps),
+        "unit": "GB/s",
+        "per_call_value": round(total / pc / 1e9, 3),
+        "batched_value": round(total / bt / 1e9, 3),
+        "batched_steady_value": round(total / steady / 1e9, 3),
+        "batched_device_value": round(total / (sum(batched_dev) / inc) / 1e9, 3),
+        "speedup": round(sum(all_pc) / sum(all_b), 3),
+        "speedup_incremental": round(pc / bt, 3),
+        "speedup_steady": round(pc / steady, 3),
+        "job_s": {"per_call": round(sum(all_pc), 4), "batched": round(sum(all_b), 4)},
+        "per_call_ms": round(pc * 1e3, 3), "batched_ms": round(bt * 1e3, 3),
+        "batched_steady_ms": round(steady * 1e3, 3),
+        "identical_to_per_call": identical,
+        "mismatches": mismatches,
+        "per_call_device_ms": round(sum(per_call_dev) / inc * 1e3, 3),
+        "batched_host_ms": {k: round(sum(h[j] for h in host_parts) / inc, 3)
+                            for j, k in enumerate(["prepare", "capture", "issue", "wait", "complete"])},
+        "diff_bytes_total": int(diff_total),
+        "graph": {"captures": int(info.graph_captures), "nodes": int(info.graph_nodes),
+                  "kernels_per_step": int(info.kernels_per_step)},
+        "autotune": {"seconds": round(tune_s, 2),
+                     "distinct_choices": sorted({json.dumps(t, sort_keys=True) for t in tunes})},
+        "gpu_launches": int(launches),
+        "note": "per_call: one mtc_checkpoint per buffer through lone handles (host wall time incl. its "
+                "synchronisation); batched: one mtc_batch_checkpoint per step (wall time; the first incremental "
+                "step includes the graph capture). speedup: whole job (all checkpoints, baseline included); "
+                "*_value, speedup_incremental: incremental steps; steady: incremental steps after the first; "
+                "device: fork-to-join CUDA events of the batched step",
+    }
+    for d in lone:
+        d.close()
+    b.close()
+    return res
+
+
 def main():
     a = parse()
     ws, rank, local = dist_setup()
@@ -281,6 +411,9 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     mc.load()
     kind = mc.MD5 if a.hash == "md5" else mc.MURMUR3
+    if a.only_batch:
+        print(json.dumps({"batched": batch_bench(torch, mc, torch.device("cuda", local), a)}), flush=True)
+        return 0
     cs = a.chunk
     nbytes = int(a.size_gib * GIB) // cs * cs
     N = (nbytes + cs - 1) // cs
@@ -373,6 +506,12 @@ def main():
         torch.cuda.empty_cache()
         rst = restart_bench(torch, mc, dev, a, kind)
 
+    bat = None
+    if not a.no_batch and rank == 0:
+        torch.cuda.empty_cache()
+        bat = batch_bench(torch, mc, dev, a)
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu:
         v, nsteps = cpu_sample(1 if a.hash == "md5" else 0, cs)
@@ -402,6 +541,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "restart": rst,
+            "batched": bat,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }

@@ -165,6 +165,66 @@ int mtc_basic_checkpoint_noalloc(int hash, const void* dev_data, uint64_t len, u
                                  void* dev_digests, uint32_t ref_id, uint32_t chkpt_id, int first, void* dev_diff,
                                  uint64_t diff_capacity, uint64_t* diff_len, void* cuda_stream);
 
+/* ---- batched checkpoints (no counterpart in the reference: its drivers
+ * checkpoint one buffer per call, src/dedup_files.cpp:86-102) ----
+ * A batch holds n deduplicators of any approach, hash and chunk size, each on
+ * its own stream.  mtc_batch_checkpoint checkpoints every member in one call:
+ * the baseline step runs eagerly with all members overlapped; later steps
+ * replay one CUDA graph holding every member's kernels as parallel branches
+ * (captured again only when a member's device buffers move).  Each member's
+ * diff, header and counters are byte-identical to those of a lone handle
+ * given the same buffers; read them through the member handles. */
+typedef struct mtc_batch mtc_batch_t;
+typedef struct mtc_batch_info {
+  uint64_t steps;
+  uint64_t graph_captures;
+  uint64_t graph_nodes;
+  uint64_t kernels_per_step;
+  double last_device_ms;   /* fork to join of the last step (CUDA events) */
+  double last_call_ms;     /* host wall time of the last mtc_batch_checkpoint */
+  double host_ms[5];       /* its parts: prepare (allocation, validation), graph
+                              capture, issue, wait for the join, completion */
+  int32_t last_used_graph;
+  int32_t reserved;
+} mtc_batch_info_t;
+int mtc_batch_create(uint32_t n, const int* approaches, const int* hashes, const uint32_t* chunk_sizes,
+                     mtc_batch_t** out);
+int mtc_batch_destroy(mtc_batch_t* b);
+/* member i as an ordinary handle (owned by the batch: do not mtc_destroy it;
+ * mtc_set_stream on it is refused) */
+int mtc_batch_member(mtc_batch_t* b, uint32_t i, mtc_dedup_t** member);
+/* checkpoint(data_i, len_i, diff_h, make_baseline) of every member, current_id
+ * advanced; diff_lens (may be NULL) receives the n diff sizes */
+int mtc_batch_checkpoint(mtc_batch_t* b, const void* const* dev_data, const uint64_t* lens, int make_baseline,
+                         uint64_t* diff_lens);
+/* use_graph 0: issue every step eagerly (still overlapped across members);
+ * id_headroom: checkpoint ids one captured graph serves before re-capture */
+int mtc_batch_set_options(mtc_batch_t* b, int use_graph, uint32_t id_headroom);
+int mtc_batch_get_info(const mtc_batch_t* b, mtc_batch_info_t* out);
+/* run the autotuner for every member (cached per approach, hash, chunk size
+ * and power-of-two length; lengths above 64 MiB share one 64 MiB trial) and
+ * apply the winners */
+int mtc_batch_autotune(mtc_batch_t* b, const uint64_t* lens);
+
+/* ---- launch tuning (no counterpart in the reference) ----
+ * Shape of the chunk-hashing kernel and the digest map's load factor.  Any
+ * setting gives identical output; only the speed changes. */
+typedef struct mtc_tune {
+  int32_t rows;         /* chunks per CTA tile: 128 or 256 */
+  int32_t ctas_per_sm;  /* 0: as many as fit (at most 3) */
+  int32_t direct;       /* 1: per-thread global loads instead of TMA staging */
+  int32_t reserved;
+  double max_load;      /* digest-map load factor bound, (0.1, 0.95] */
+} mtc_tune_t;
+int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t);
+int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* out);
+/* time the candidate shapes on a seeded synthetic buffer of `len` bytes
+ * (allocated and freed inside) and return the fastest; best_ms and
+ * default_ms (may be NULL) receive the mean incremental checkpoint device
+ * time of the winner and of the default shape */
+int mtc_autotune(int approach, int hash, uint32_t chunk_size, uint64_t len, mtc_tune_t* best, double* best_ms,
+                 double* default_ms);
+
 /* kernels launched by the library so far (all handles) */
 uint64_t mtc_launch_count(void);
 /* message for the last failing call on this thread */

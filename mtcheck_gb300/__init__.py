@@ -49,6 +49,23 @@ class Info(ctypes.Structure):
                 ("device_error", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("graph_captures", ctypes.c_uint64), ("graph_nodes", ctypes.c_uint64),
+                ("kernels_per_step", ctypes.c_uint64), ("last_device_ms", ctypes.c_double),
+                ("last_call_ms", ctypes.c_double), ("host_ms", ctypes.c_double * 5),
+                ("last_used_graph", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("direct", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("max_load", ctypes.c_double)]
+
+    def as_dict(self):
+        return {"rows": self.rows, "ctas_per_sm": self.ctas_per_sm, "direct": self.direct,
+                "max_load": self.max_load}
+
+
 # every symbol of include/mtcheck.h with its ctypes signature
 _VP, _U32, _U64, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
 SIGNATURES = {
@@ -74,6 +91,18 @@ SIGNATURES = {
     "mtc_digest_hex": (_I, [_VP, ctypes.c_char_p]),
     "mtc_basic_checkpoint_noalloc": (_I, [_I, _VP, _U64, _U32, _VP, _U32, _U32, _I, _VP, _U64,
                                          ctypes.POINTER(_U64), _VP]),
+    "mtc_batch_create": (_I, [_U32, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_U32),
+                              ctypes.POINTER(_VP)]),
+    "mtc_batch_destroy": (_I, [_VP]),
+    "mtc_batch_member": (_I, [_VP, _U32, ctypes.POINTER(_VP)]),
+    "mtc_batch_checkpoint": (_I, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(_U64), _I, ctypes.POINTER(_U64)]),
+    "mtc_batch_set_options": (_I, [_VP, _I, _U32]),
+    "mtc_batch_get_info": (_I, [_VP, ctypes.POINTER(BatchInfo)]),
+    "mtc_batch_autotune": (_I, [_VP, ctypes.POINTER(_U64)]),
+    "mtc_set_tuning": (_I, [_VP, ctypes.POINTER(Tune)]),
+    "mtc_get_tuning": (_I, [_VP, ctypes.POINTER(Tune)]),
+    "mtc_autotune": (_I, [_I, _I, _U32, _U64, ctypes.POINTER(Tune), ctypes.POINTER(ctypes.c_double),
+                          ctypes.POINTER(ctypes.c_double)]),
     "mtc_launch_count": (_U64, []),
     "mtc_last_error": (ctypes.c_char_p, []),
 }
@@ -240,6 +269,16 @@ class Deduplicator:
     def write_restart_log(self, select_chkpt, logname):
         _check(load().mtc_write_restart_log(self.h, select_chkpt, logname.encode()))
 
+    # -- tuning ------------------------------------------------------------
+    def set_tuning(self, rows=256, ctas_per_sm=0, direct=0, max_load=0.75):
+        t = Tune(rows, ctas_per_sm, direct, 0, max_load)
+        _check(load().mtc_set_tuning(self.h, ctypes.byref(t)))
+
+    def tuning(self):
+        t = Tune()
+        _check(load().mtc_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
 
 class TreeDeduplicator(Deduplicator):
     approach = TREE
@@ -259,3 +298,84 @@ class BasicDeduplicator(Deduplicator):
 
 class FullDeduplicator(Deduplicator):
     approach = FULL
+
+
+class _Member(Deduplicator):
+    """A batch member: an ordinary handle owned by its batch."""
+
+    def __init__(self, handle, approach, chunk_size, owner):
+        self.h = handle
+        self.approach = approach
+        self.chunk_size = chunk_size
+        self._owner = owner  # keeps the batch alive
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Many deduplicators checkpointed in one call (mtc_batch_*): the baseline
+    step overlaps every member's kernels on separate streams, later steps
+    replay one CUDA graph.  `members` is a list of (approach, hash, chunk_size)."""
+
+    def __init__(self, members):
+        L = load()
+        n = len(members)
+        ap = (_I * n)(*[int(m[0]) for m in members])
+        hs = (_I * n)(*[int(m[1]) for m in members])
+        cs = (_U32 * n)(*[int(m[2]) for m in members])
+        b = _VP()
+        _check(L.mtc_batch_create(n, ap, hs, cs, ctypes.byref(b)))
+        self.b = b
+        self.members = []
+        for i, m in enumerate(members):
+            h = _VP()
+            _check(L.mtc_batch_member(b, i, ctypes.byref(h)))
+            self.members.append(_Member(h, int(m[0]), int(m[2]), self))
+
+    def __len__(self):
+        return len(self.members)
+
+    def close(self):
+        if getattr(self, "b", None):
+            for m in self.members:
+                m.h = None
+            load().mtc_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_options(self, use_graph=True, id_headroom=64):
+        _check(load().mtc_batch_set_options(self.b, int(use_graph), int(id_headroom)))
+
+    def autotune(self, bufs):
+        lens = (_U64 * len(bufs))(*[_dev_ptr(x)[1] for x in bufs])
+        _check(load().mtc_batch_autotune(self.b, lens))
+
+    def checkpoint(self, bufs, make_baseline=False):
+        """One checkpoint of every member; returns the list of diff sizes."""
+        n = len(bufs)
+        pl = [_dev_ptr(x) for x in bufs]
+        ptrs = (_VP * n)(*[p for p, _ in pl])
+        lens = (_U64 * n)(*[l for _, l in pl])
+        out = (_U64 * n)()
+        _check(load().mtc_batch_checkpoint(self.b, ptrs, lens, int(make_baseline), out))
+        return [int(x) for x in out]
+
+    def info(self):
+        i = BatchInfo()
+        _check(load().mtc_batch_get_info(self.b, ctypes.byref(i)))
+        return i
+
+
+def autotune(approach, hash, chunk_size, nbytes):
+    """Fastest launch shape for one configuration: (tuning dict, best ms, default ms)."""
+    t = Tune()
+    best, dflt = ctypes.c_double(), ctypes.c_double()
+    _check(load().mtc_autotune(approach, hash, chunk_size, nbytes, ctypes.byref(t), ctypes.byref(best),
+                               ctypes.byref(dflt)))
+    return t.as_dict(), best.value, dflt.value

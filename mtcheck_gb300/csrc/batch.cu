@@ -1,0 +1,320 @@
+// batch.cu -- Batch (many engines, one CUDA graph per step) and the autotuner.
+#include <chrono>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "batch.hpp"
+
+namespace mtc {
+
+namespace {
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+Batch::Batch() {
+  cudaStreamCreateWithFlags(&origin_, cudaStreamNonBlocking);
+  cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&in_, cudaEventDisableTiming);
+  cudaEventCreate(&t0_);
+  cudaEventCreate(&t1_);
+}
+
+Batch::~Batch() {
+  if (origin_) cudaStreamSynchronize(origin_);
+  for (auto s : streams_) cudaStreamSynchronize(s);
+  drop_graph();
+  for (auto* e : engs_) delete e;
+  for (auto s : streams_) cudaStreamDestroy(s);
+  for (auto e : joins_) cudaEventDestroy(e);
+  if (fork_) cudaEventDestroy(fork_);
+  if (in_) cudaEventDestroy(in_);
+  if (t0_) cudaEventDestroy(t0_);
+  if (t1_) cudaEventDestroy(t1_);
+  if (origin_) cudaStreamDestroy(origin_);
+}
+
+int Batch::fail(int code, const std::string& msg) {
+  last_error = msg;
+  return code;
+}
+
+void Batch::drop_graph() {
+  for (auto& x : execs_)
+    if (x) cudaGraphExecDestroy(x);
+  execs_.assign(engs_.size(), nullptr);
+  sigs_.assign(engs_.size(), 0);
+  nodes_.assign(engs_.size(), 0);
+  kernels_.assign(engs_.size(), 0);
+}
+
+int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
+  cudaStream_t s = nullptr;
+  cudaEvent_t j = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return -1;
+  if (cudaEventCreateWithFlags(&j, cudaEventDisableTiming) != cudaSuccess) {
+    cudaStreamDestroy(s);
+    return -1;
+  }
+  auto* e = new Engine(mode, hash_kind, chunk_size);
+  e->set_stream(s);
+  e->set_order_after_legacy(true);
+  engs_.push_back(e);
+  streams_.push_back(s);
+  joins_.push_back(j);
+  drop_graph();
+  return (int)engs_.size() - 1;
+}
+
+#define MTC_BCUDA(call)                                                                              \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return fail(e_ == cudaErrorMemoryAllocation ? ST_ENOMEM : ST_ECUDA,       \
+                                       std::string(#call) + ": " + cudaGetErrorString(e_));          \
+  } while (0)
+
+int Batch::capture_member(size_t i, const uint8_t* data, uint64_t len) {
+  if (execs_[i]) cudaGraphExecDestroy(execs_[i]);
+  execs_[i] = nullptr;
+  const uint64_t l0 = launch_count();
+  MTC_BCUDA(cudaStreamBeginCapture(streams_[i], cudaStreamCaptureModeRelaxed));
+  int rc = engs_[i]->enqueue(data, len, false);
+  cudaGraph_t g = nullptr;
+  cudaError_t ee = cudaStreamEndCapture(streams_[i], &g);
+  if (rc != ST_OK || ee != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc != ST_OK) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
+    return fail(ST_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
+  }
+  cudaError_t ie = cudaGraphInstantiate(&execs_[i], g, 0);
+  size_t n = 0;
+  cudaGraphGetNodes(g, nullptr, &n);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    execs_[i] = nullptr;
+    return fail(ST_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+  }
+  nodes_[i] = n;
+  kernels_[i] = launch_count() - l0;
+  sigs_[i] = engs_[i]->signature(data, len);
+  stats_.captures++;
+  return ST_OK;
+}
+
+int Batch::checkpoint(const uint8_t* const* data, const uint64_t* lens, bool make_baseline, uint64_t* diff_lens) {
+  const double t_call = now_ms();
+  if (engs_.empty()) return fail(ST_EINVAL, "empty batch");
+  if (!data || !lens) return fail(ST_EINVAL, "NULL argument");
+  // 1. allocations, validation, map growth: outside any capture
+  bool any_fresh = false;
+  for (size_t i = 0; i < engs_.size(); i++) {
+    int rc = engs_[i]->prepare(data[i], lens[i], make_baseline, headroom_);
+    if (rc) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
+    any_fresh = any_fresh || engs_[i]->fresh();
+  }
+  // prepare's own stream work (map rehash) is ordered before the step on
+  // each member's stream; nothing waits for it here
+  const double t_prep = now_ms();
+  const bool graph = use_graph_ && !any_fresh;
+  // 2. (re)capture the members whose device buffers moved
+  if (graph) {
+    for (size_t i = 0; i < engs_.size(); i++)
+      if (!execs_[i] || sigs_[i] != engs_[i]->signature(data[i], lens[i])) {
+        int rc = capture_member(i, data[i], lens[i]);
+        if (rc) return rc;
+      }
+  }
+  // 3. issue: the step starts after the work already on the legacy default
+  // stream (where the inputs are usually written), every member on its own
+  // stream between a fork and a join on the origin stream
+  const double t_cap = now_ms();
+  const uint64_t l0 = launch_count();
+  MTC_BCUDA(cudaEventRecord(in_, cudaStreamLegacy));
+  MTC_BCUDA(cudaStreamWaitEvent(origin_, in_, 0));
+  MTC_BCUDA(cudaEventRecord(t0_, origin_));
+  MTC_BCUDA(cudaEventRecord(fork_, origin_));
+  uint64_t nodes = 0, kernels = 0;
+  for (size_t i = 0; i < engs_.size(); i++) {
+    MTC_BCUDA(cudaStreamWaitEvent(streams_[i], fork_, 0));
+    engs_[i]->stage_params();
+    if (graph) {
+      MTC_BCUDA(cudaGraphLaunch(execs_[i], streams_[i]));
+      nodes += nodes_[i];
+      kernels += kernels_[i];
+    } else {
+      int rc = engs_[i]->enqueue(data[i], lens[i], false);
+      if (rc) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
+    }
+    MTC_BCUDA(cudaEventRecord(joins_[i], streams_[i]));
+    MTC_BCUDA(cudaStreamWaitEvent(origin_, joins_[i], 0));
+  }
+  MTC_BCUDA(cudaEventRecord(t1_, origin_));
+  if (graph) {
+    note_launch((uint32_t)kernels);
+    stats_.graph_nodes = nodes;
+    stats_.kernels_per_step = kernels;
+  } else {
+    stats_.kernels_per_step = launch_count() - l0;
+  }
+  stats_.last_used_graph = graph ? 1 : 0;
+  const double t_issue = now_ms();
+  MTC_BCUDA(cudaEventSynchronize(t1_));
+  const double t_wait = now_ms();
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0_, t1_);
+  stats_.last_device_ms = ms;
+  // 4. per-member completion, then advance like checkpoint(data, len, diff_h, make_baseline)
+  for (size_t i = 0; i < engs_.size(); i++) {
+    engs_[i]->release_retired();
+    int rc = engs_[i]->complete(lens[i], nullptr);
+    if (rc) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
+    if (diff_lens) diff_lens[i] = engs_[i]->diff_len();
+  }
+  for (auto* e : engs_) e->current_id += 1;
+  stats_.steps++;
+  const double t_end = now_ms();
+  stats_.last_call_ms = t_end - t_call;
+  stats_.host_ms[0] = t_prep - t_call;
+  stats_.host_ms[1] = t_cap - t_prep;
+  stats_.host_ms[2] = t_issue - t_cap;
+  stats_.host_ms[3] = t_wait - t_issue;
+  stats_.host_ms[4] = t_end - t_wait;
+  return ST_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  // SplitMix64 finaliser (Steele, Lea, Flood 2014)
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void tune_fill_kernel(uint8_t* p, uint64_t len, uint64_t seed) {
+  const uint64_t words = len / 8;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<uint64_t*>(p)[i] = mix64(seed + i);
+  if (blockIdx.x == 0 && threadIdx.x < (len & 7)) p[words * 8 + threadIdx.x] = (uint8_t)mix64(seed ^ threadIdx.x);
+}
+
+// Rewrite the first word of about 1/stride of the chunks.
+__global__ void tune_touch_kernel(uint8_t* p, uint64_t len, uint32_t cs, uint32_t stride, uint64_t seed) {
+  const uint64_t n = len / cs;
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x)
+    if (mix64(seed + c) % stride == 0) p[c * cs] ^= (uint8_t)(1 + (mix64(c ^ seed) & 0x7f));
+}
+
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, uint32_t, int>, TuneResult> g_tune_cache;
+
+int log2_bucket(uint64_t len) {
+  int b = 0;
+  while ((1ull << (b + 1)) <= len) b++;
+  return b;
+}
+
+}  // namespace
+
+int autotune(int mode, int hash_kind, uint32_t chunk_size, uint64_t len, bool use_cache, TuneResult* out,
+             std::string* err) {
+  const auto key = std::make_tuple(mode, hash_kind, chunk_size, log2_bucket(len));
+  if (use_cache) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      *out = it->second;
+      return ST_OK;
+    }
+  }
+  if (mode == MODE_FULL) {  // a device-to-device copy: nothing to tune
+    *out = TuneResult{};
+    return ST_OK;
+  }
+  uint8_t* buf = nullptr;
+  if (cudaMalloc(&buf, len) != cudaSuccess) {
+    if (err) *err = "autotune: cannot allocate the sample buffer";
+    return ST_ENOMEM;
+  }
+  cudaStream_t s = nullptr;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const uint32_t grid = (uint32_t)num_sms() * 8;
+
+  struct Cand {
+    LeafTune t;
+    double load;
+  };
+  std::vector<Cand> cands;
+  cands.push_back({LeafTune{256, 0, 0}, 0.75});  // the default shape first
+  const double loads_tree[] = {0.5, 0.75, 0.9};
+  const bool has_map = mode != MODE_BASIC && mode != MODE_FULL;
+  for (int rows : {256, 128})
+    for (int per_sm : {1, 2, 3, 4}) cands.push_back({LeafTune{rows, per_sm, 0}, 0.75});
+  cands.push_back({LeafTune{256, 0, 1}, 0.75});
+  if (has_map)
+    for (double l : loads_tree)
+      if (l != 0.75) cands.push_back({LeafTune{256, 0, 0}, l});
+
+  TuneResult best;
+  best.ms = 1e30;
+  int rc = ST_OK;
+  const int kSteps = 3;
+  for (size_t ci = 0; ci < cands.size() && rc == ST_OK; ci++) {
+    Engine e(mode, hash_kind, chunk_size);
+    e.set_stream(s);
+    e.set_leaf_tune(cands[ci].t);
+    e.set_max_load(cands[ci].load);
+    tune_fill_kernel<<<grid, 256, 0, s>>>(buf, len, 0x5eed);
+    HeaderHost h;
+    rc = e.checkpoint(buf, len, true, &h);
+    if (rc) break;
+    e.current_id++;
+    double sum = 0;
+    for (int st = 0; st < kSteps; st++) {
+      tune_touch_kernel<<<grid, 256, 0, s>>>(buf, len, chunk_size, 50, 0x1000 + st);
+      cudaEventRecord(a, s);
+      rc = e.checkpoint(buf, len, false, &h);
+      cudaEventRecord(b, s);
+      if (rc) break;
+      cudaEventSynchronize(b);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      sum += ms;
+      e.current_id++;
+    }
+    if (rc) break;
+    const double mean = sum / kSteps;
+    if (ci == 0) best.default_ms = mean;  // first candidate: the default shape
+    if (mean < best.ms) {
+      best.ms = mean;
+      best.leaf = cands[ci].t;
+      best.max_load = cands[ci].load;
+    }
+  }
+  best.candidates = (int)cands.size();
+  cudaStreamSynchronize(s);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaStreamDestroy(s);
+  cudaFree(buf);
+  if (rc) {
+    if (err) *err = "autotune: a trial checkpoint failed";
+    return rc;
+  }
+  *out = best;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune_cache[key] = best;
+  return ST_OK;
+}
+
+}  // namespace mtc

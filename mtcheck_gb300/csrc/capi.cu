@@ -7,12 +7,19 @@
 #include <vector>
 
 #include "../../include/mtcheck.h"
+#include "batch.hpp"
 #include "engine.hpp"
 #include "host_digest.hpp"
 #include "logs.hpp"
 
 struct mtc_dedup {
   mtc::Engine* eng;
+  bool borrowed = false;  // a batch member: the batch owns the engine
+};
+
+struct mtc_batch {
+  mtc::Batch* b = nullptr;
+  std::vector<mtc_dedup> members;
 };
 
 namespace {
@@ -49,6 +56,7 @@ int mtc_create(int approach, int hash, uint32_t chunk_size, mtc_dedup_t** out) {
 
 int mtc_destroy(mtc_dedup_t* h) {
   if (!h) return MTC_OK;
+  if (h->borrowed) return ret(MTC_EINVAL, "batch members are destroyed with their batch");
   delete h->eng;
   delete h;
   return MTC_OK;
@@ -56,6 +64,7 @@ int mtc_destroy(mtc_dedup_t* h) {
 
 int mtc_set_stream(mtc_dedup_t* h, void* s) {
   if (!h) return ret(MTC_EINVAL, "NULL handle");
+  if (h->borrowed) return ret(MTC_EINVAL, "a batch member runs on the batch's stream");
   h->eng->set_stream(reinterpret_cast<cudaStream_t>(s));
   return MTC_OK;
 }
@@ -290,6 +299,138 @@ int mtc_digest_hex(const uint8_t d[16], char out[37]) {
     if (k % 4 == 3) *c++ = ' ';
   }
   *c = 0;
+  return MTC_OK;
+}
+
+// ---- batch ----
+int mtc_batch_create(uint32_t n, const int* approaches, const int* hashes, const uint32_t* chunk_sizes,
+                     mtc_batch_t** out) {
+  if (!out) return ret(MTC_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (n == 0 || !approaches || !hashes || !chunk_sizes) return ret(MTC_EINVAL, "empty or NULL member list");
+  for (uint32_t i = 0; i < n; i++) {
+    if (!valid_mode(approaches[i])) return ret(MTC_EINVAL, "unknown approach for member " + std::to_string(i));
+    if (hashes[i] != MTC_HASH_MURMUR3 && hashes[i] != MTC_HASH_MD5)
+      return ret(MTC_EINVAL, "unknown hash for member " + std::to_string(i));
+    if (chunk_sizes[i] == 0) return ret(MTC_EINVAL, "chunk size 0 for member " + std::to_string(i));
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ret(MTC_ECUDA, "no CUDA device");
+  auto* b = new (std::nothrow) mtc_batch;
+  if (!b) return ret(MTC_ENOMEM, "out of host memory");
+  b->b = new (std::nothrow) mtc::Batch();
+  if (!b->b) { delete b; return ret(MTC_ENOMEM, "out of host memory"); }
+  for (uint32_t i = 0; i < n; i++) {
+    if (b->b->add(approaches[i], hashes[i], chunk_sizes[i]) < 0) {
+      delete b->b;
+      delete b;
+      return ret(MTC_ECUDA, "cannot create a member stream");
+    }
+  }
+  b->members.resize(n);
+  for (uint32_t i = 0; i < n; i++) b->members[i] = mtc_dedup{b->b->member(i), true};
+  *out = b;
+  return MTC_OK;
+}
+
+int mtc_batch_destroy(mtc_batch_t* b) {
+  if (!b) return MTC_OK;
+  delete b->b;
+  delete b;
+  return MTC_OK;
+}
+
+int mtc_batch_member(mtc_batch_t* b, uint32_t i, mtc_dedup_t** member) {
+  if (!b || !member) return ret(MTC_EINVAL, "NULL argument");
+  if (i >= b->members.size()) return ret(MTC_EINVAL, "member index out of range");
+  *member = &b->members[i];
+  return MTC_OK;
+}
+
+int mtc_batch_checkpoint(mtc_batch_t* b, const void* const* dev_data, const uint64_t* lens, int make_baseline,
+                         uint64_t* diff_lens) {
+  if (!b || !dev_data || !lens) return ret(MTC_EINVAL, "NULL argument");
+  int rc = b->b->checkpoint(reinterpret_cast<const uint8_t* const*>(dev_data), lens, make_baseline != 0, diff_lens);
+  return rc ? ret(rc, b->b->last_error) : MTC_OK;
+}
+
+int mtc_batch_set_options(mtc_batch_t* b, int use_graph, uint32_t id_headroom) {
+  if (!b) return ret(MTC_EINVAL, "NULL batch");
+  b->b->set_use_graph(use_graph != 0);
+  b->b->set_id_headroom(id_headroom);
+  return MTC_OK;
+}
+
+int mtc_batch_get_info(const mtc_batch_t* b, mtc_batch_info_t* o) {
+  if (!b || !o) return ret(MTC_EINVAL, "NULL argument");
+  const mtc::BatchStats& s = b->b->stats();
+  std::memset(o, 0, sizeof(*o));
+  o->steps = s.steps;
+  o->graph_captures = s.captures;
+  o->graph_nodes = s.graph_nodes;
+  o->kernels_per_step = s.kernels_per_step;
+  o->last_device_ms = s.last_device_ms;
+  o->last_call_ms = s.last_call_ms;
+  for (int k = 0; k < 5; k++) o->host_ms[k] = s.host_ms[k];
+  o->last_used_graph = s.last_used_graph;
+  return MTC_OK;
+}
+
+int mtc_batch_autotune(mtc_batch_t* b, const uint64_t* lens) {
+  if (!b || !lens) return ret(MTC_EINVAL, "NULL argument");
+  for (uint32_t i = 0; i < b->b->size(); i++) {
+    mtc::Engine* e = b->b->member(i);
+    mtc::TuneResult r;
+    std::string err;
+    // members above 64 MiB share one 64 MiB trial (they fill every SM)
+    const uint64_t trial = lens[i] < (64ull << 20) ? lens[i] : (64ull << 20);
+    int rc = mtc::autotune(e->mode(), e->hash_kind(), e->chunk_size(), trial, true, &r, &err);
+    if (rc) return ret(rc, err);
+    e->set_leaf_tune(r.leaf);
+    e->set_max_load(r.max_load);
+  }
+  return MTC_OK;
+}
+
+// ---- tuning ----
+int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t) {
+  if (!h || !t) return ret(MTC_EINVAL, "NULL argument");
+  if (t->rows != 128 && t->rows != 256) return ret(MTC_EINVAL, "rows must be 128 or 256");
+  if (t->ctas_per_sm < 0 || t->ctas_per_sm > 8) return ret(MTC_EINVAL, "ctas_per_sm out of range");
+  if (!(t->max_load > 0.1 && t->max_load <= 0.95)) return ret(MTC_EINVAL, "max_load outside (0.1, 0.95]");
+  h->eng->set_leaf_tune(mtc::LeafTune{t->rows, t->ctas_per_sm, t->direct ? 1 : 0});
+  h->eng->set_max_load(t->max_load);
+  return MTC_OK;
+}
+
+int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* o) {
+  if (!h || !o) return ret(MTC_EINVAL, "NULL argument");
+  std::memset(o, 0, sizeof(*o));
+  const mtc::LeafTune& t = h->eng->leaf_tune();
+  o->rows = t.rows;
+  o->ctas_per_sm = t.ctas_per_sm;
+  o->direct = t.direct;
+  o->max_load = h->eng->max_load();
+  return MTC_OK;
+}
+
+int mtc_autotune(int approach, int hash, uint32_t chunk_size, uint64_t len, mtc_tune_t* best, double* best_ms,
+                 double* default_ms) {
+  if (!best) return ret(MTC_EINVAL, "NULL argument");
+  if (!valid_mode(approach)) return ret(MTC_EINVAL, "unknown approach");
+  if (hash != MTC_HASH_MURMUR3 && hash != MTC_HASH_MD5) return ret(MTC_EINVAL, "unknown hash");
+  if (chunk_size == 0 || len == 0) return ret(MTC_EINVAL, "empty buffer or chunk size 0");
+  mtc::TuneResult r;
+  std::string err;
+  int rc = mtc::autotune(approach, hash, chunk_size, len, false, &r, &err);
+  if (rc) return ret(rc, err);
+  std::memset(best, 0, sizeof(*best));
+  best->rows = r.leaf.rows;
+  best->ctas_per_sm = r.leaf.ctas_per_sm;
+  best->direct = r.leaf.direct;
+  best->max_load = r.max_load;
+  if (best_ms) *best_ms = r.ms;
+  if (default_ms) *default_ms = r.default_ms;
   return MTC_OK;
 }
 

@@ -33,6 +33,7 @@ Engine::~Engine() {
   if (lay_host_) cudaFreeHost(lay_host_);
   if (err_host_) cudaFreeHost(err_host_);
   if (sp_host_) cudaFreeHost(sp_host_);
+  release_retired();
   destroy_restart_scratch(rs_);
 }
 
@@ -49,8 +50,9 @@ int Engine::fail(int code, const std::string& msg) {
   } while (0)
 
 int Engine::ensure_map(uint64_t want_entries, bool reset) {
-  // load factor <= 3/4 after the worst-case number of inserts of one checkpoint
-  const uint64_t need = next_pow2(std::max<uint64_t>(1024, (want_entries * 4 + 2) / 3));
+  // load factor <= max_load after the worst-case number of inserts of one
+  // checkpoint (3/4 unless tuned)
+  uint64_t need = next_pow2(std::max<uint64_t>(1024, (uint64_t)((double)want_entries / max_load_) + 1));
   if (reset) {
     if (slots_.n < need || slots_.n > 4 * need) {
       slots_.release();
@@ -63,6 +65,9 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
     return ST_OK;
   }
   if (map_cap_ >= need) return ST_OK;
+  // an existing map grows to twice the bound, so that it grows rarely (each
+  // growth moves the table, which a captured launch sequence bakes in)
+  need *= 2;
   DevBuf<MapSlot> fresh;
   MTC_CUDA(fresh.ensure(need, stream_));
   MTC_CUDA(cudaMemsetAsync(fresh.p, 0, sizeof(MapSlot) * need, stream_));
@@ -70,11 +75,20 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
   DigestMap from{slots_.p, map_cap_ - 1, map_size_.p};
   DigestMap to{fresh.p, need - 1, map_size_.p};
   MTC_CUDA(launch_map_rehash(from, map_cap_, to, err_.p, stream_));
-  MTC_CUDA(cudaStreamSynchronize(stream_));
-  std::swap(slots_.p, fresh.p);
-  std::swap(slots_.n, fresh.n);
+  // the old table is freed once the stream has drained (release_retired):
+  // cudaFree here would wait for the whole device
+  retired_.push_back(slots_.p);
+  slots_.p = fresh.p;
+  slots_.n = fresh.n;
+  fresh.p = nullptr;
+  fresh.n = 0;
   map_cap_ = need;
   return ST_OK;
+}
+
+void Engine::release_retired() {
+  for (void* p : retired_) cudaFree(p);
+  retired_.clear();
 }
 
 int Engine::ensure_sort(uint32_t K) {
@@ -93,7 +107,7 @@ int Engine::ensure_sort(uint32_t K) {
   return ST_OK;
 }
 
-int Engine::ensure_state(uint32_t N, bool fresh) {
+int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
   const uint32_t M = 2 * N - 1;
   const bool tree = mode_ == MODE_TREE || mode_ == MODE_TREE_LOW_OFFSET || mode_ == MODE_TREE_LOW_OFFSET_REF;
   if (fresh) {
@@ -132,7 +146,7 @@ int Engine::ensure_state(uint32_t N, bool fresh) {
     int rc = ensure_map((uint64_t)map_size_host_ + (tree ? M_ : N_), false);
     if (rc) return rc;
   }
-  return ensure_sort(current_id + 1);
+  return ensure_sort(current_id + 1 + id_headroom);
 }
 
 GatherArgs Engine::gather_args(const uint8_t* data, uint64_t len) {
@@ -190,8 +204,8 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.changed_list = changed_list_.p;
   la.changed_count = changed_count_.p;
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, sizeof(uint32_t), stream_));
-  MTC_CUDA(launch_leaves(la, &tma_, stream_));
-  MTC_CUDA(cudaEventRecord(ev_[4], stream_));
+  MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
+  if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   MTC_CUDA(launch_leaf_inserts(la, stream_));
 
   ForestArgs fa{};
@@ -227,95 +241,120 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.err = err_.p;
   la.hash_kind = hash_kind_;
   la.epi = mode_ == MODE_LIST ? EPI_LIST : EPI_BASIC;
-  la.basic_first = current_id == 0 ? 1 : 0;
+  la.basic_first = current_id == 0 ? 1 : 0;  // never true in a captured sequence
   la.changed_list = changed_list_.p;
   la.changed_count = changed_count_.p;
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, sizeof(uint32_t), stream_));
-  MTC_CUDA(launch_leaves(la, &tma_, stream_));
-  MTC_CUDA(cudaEventRecord(ev_[4], stream_));
+  MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
+  if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   if (mode_ == MODE_LIST) MTC_CUDA(launch_leaf_inserts(la, stream_));
   MTC_CUDA(launch_chunk_compaction(labels_.p, N_, mode_ == MODE_BASIC ? 1 : 0, fo_list_.p, sh_list_.p, lay_.p, scan_.p,
                                    scan_total_.p, stream_));
   return ST_OK;
 }
 
-int Engine::checkpoint(const uint8_t* data, uint64_t len, bool make_baseline, HeaderHost* header) {
+int Engine::prepare(const uint8_t* data, uint64_t len, bool make_baseline, uint32_t id_headroom) {
   if (!data || len == 0) return fail(ST_EINVAL, "empty buffer");
   const uint64_t n64 = (len + cs_ - 1) / cs_;
   if (n64 >= (1ull << 31)) return fail(ST_ENOTSUP, "more than 2^31 chunks");
   const uint32_t N = (uint32_t)n64;
-  const bool fresh = make_baseline || !allocated_;
-  if (mode_ != MODE_FULL && !fresh && len != data_len)
+  fresh_ = make_baseline || !allocated_;
+  if (mode_ != MODE_FULL && !fresh_ && len != data_len)
     return fail(ST_EINVAL, "buffer length changed without a new baseline");
-  MTC_CUDA(cudaEventRecord(ev_[0], stream_));
   if (mode_ == MODE_FULL) {
-    // FullDeduplicator: the checkpoint is the raw buffer (src/full_approach.cpp:66-72)
     MTC_CUDA(stage_.ensure(len + 64, stream_));
-    MTC_CUDA(cudaEventRecord(ev_[1], stream_));
-    MTC_CUDA(cudaEventRecord(ev_[2], stream_));
-    MTC_CUDA(cudaMemcpyAsync(stage_.p, data, len, cudaMemcpyDeviceToDevice, stream_));
-    MTC_CUDA(cudaEventRecord(ev_[3], stream_));
-    MTC_CUDA(cudaEventSynchronize(ev_[3]));
     allocated_ = true;
-    data_len = len;
-    diff_len_ = len;
-    diff_pad_ = 0;
-    datasizes[0] = len;
-    datasizes[1] = 0;
-    float ms[3];
-    cudaEventElapsedTime(&ms[0], ev_[0], ev_[1]);
-    cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
-    cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
-    timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
-    if (header) std::memset(header, 0, sizeof(*header));
-    return ST_OK;
+  } else {
+    int rc = ensure_state(N, fresh_, id_headroom);
+    if (rc) return rc;
   }
-  int rc = ensure_state(N, fresh);
-  if (rc) return rc;
   data_len = len;
+  // TreeLowOffsetRef follows include/reference_impl.hpp:16-132, which has no
+  // baseline special case; the tree modes follow dedup_data_baseline for
+  // checkpoint 0 and every requested baseline (src/tree_approach.cpp:1644-1653)
+  baseline_path_ = mode_ != MODE_TREE_LOW_OFFSET_REF && (current_id == 0 || make_baseline);
   if (current_id == 0 || make_baseline) baseline_id = current_id;
-  // the previous call synchronised the stream, so the pinned block is free
+  return ST_OK;
+}
+
+void Engine::stage_params() {
+  // the previous checkpoint of this engine has completed, so the pinned
+  // block is free to rewrite
   sp_host_->cur = current_id;
   sp_host_->baseline_id = baseline_id;
   sp_host_->epoch = epoch_ + 1;
   epoch_ += kEpochsPerCheckpoint;
-  MTC_CUDA(cudaMemcpyAsync(sp_.p, sp_host_, sizeof(StepParams), cudaMemcpyHostToDevice, stream_));
-  MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
-  MTC_CUDA(cudaEventRecord(ev_[1], stream_));
-  if (mode_ == MODE_LIST || mode_ == MODE_BASIC) {
-    rc = run_list_basic(data, len);
-  } else {
-    // TreeLowOffsetRef follows include/reference_impl.hpp:16-132, which has
-    // no baseline special case; the tree modes follow dedup_data_baseline for
-    // checkpoint 0 and every requested baseline (src/tree_approach.cpp:1644-1653)
-    const bool baseline_path = mode_ != MODE_TREE_LOW_OFFSET_REF && (current_id == 0 || make_baseline);
-    rc = run_tree(data, len, baseline_path);
-  }
-  if (rc) return rc;
-  MTC_CUDA(cudaEventRecord(ev_[2], stream_));
-  MTC_CUDA(launch_assemble(gather_args(data, len), (uint64_t)N_ + 1, stream_));
-  MTC_CUDA(cudaEventRecord(ev_[3], stream_));
-  return finish(data, len, header);
 }
 
-int Engine::finish(const uint8_t* data, uint64_t len, HeaderHost* header) {
-  (void)data;
+int Engine::enqueue(const uint8_t* data, uint64_t len, bool timed) {
+  timed_ = timed;
+  if (timed) MTC_CUDA(cudaEventRecord(ev_[0], stream_));
+  if (mode_ == MODE_FULL) {
+    // FullDeduplicator: the checkpoint is the raw buffer (src/full_approach.cpp:66-72)
+    if (timed) MTC_CUDA(cudaEventRecord(ev_[1], stream_));
+    if (timed) MTC_CUDA(cudaEventRecord(ev_[2], stream_));
+    MTC_CUDA(cudaMemcpyAsync(stage_.p, data, len, cudaMemcpyDeviceToDevice, stream_));
+    if (timed) MTC_CUDA(cudaEventRecord(ev_[3], stream_));
+    return ST_OK;
+  }
+  MTC_CUDA(cudaMemcpyAsync(sp_.p, sp_host_, sizeof(StepParams), cudaMemcpyHostToDevice, stream_));
+  MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
+  if (timed) MTC_CUDA(cudaEventRecord(ev_[1], stream_));
+  int rc = (mode_ == MODE_LIST || mode_ == MODE_BASIC) ? run_list_basic(data, len) : run_tree(data, len, baseline_path_);
+  if (rc) return rc;
+  if (timed) MTC_CUDA(cudaEventRecord(ev_[2], stream_));
+  MTC_CUDA(launch_assemble(gather_args(data, len), (uint64_t)N_ + 1, stream_));
+  if (timed) MTC_CUDA(cudaEventRecord(ev_[3], stream_));
   MTC_CUDA(cudaMemcpyAsync(lay_host_, lay_.p, sizeof(Layout), cudaMemcpyDeviceToHost, stream_));
   MTC_CUDA(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
   if (map_size_.p) MTC_CUDA(cudaMemcpyAsync(err_host_ + 1, map_size_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+  return ST_OK;
+}
+
+int Engine::order_inputs() {
+  if (!order_after_legacy_) return ST_OK;
+  MTC_CUDA(cudaEventRecord(ev_[5], cudaStreamLegacy));
+  MTC_CUDA(cudaStreamWaitEvent(stream_, ev_[5], 0));
+  return ST_OK;
+}
+
+int Engine::checkpoint(const uint8_t* data, uint64_t len, bool make_baseline, HeaderHost* header) {
+  int rc = prepare(data, len, make_baseline, 0);
+  if (rc) return rc;
+  if ((rc = order_inputs()) != ST_OK) return rc;
+  if (mode_ != MODE_FULL) stage_params();
+  rc = enqueue(data, len, true);
+  if (rc) return rc;
   MTC_CUDA(cudaStreamSynchronize(stream_));
+  release_retired();
+  return complete(len, header);
+}
+
+int Engine::complete(uint64_t len, HeaderHost* header) {
+  float ms[3] = {0, 0, 0};
+  if (timed_) {
+    cudaEventElapsedTime(&ms[0], ev_[0], ev_[1]);
+    cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
+    cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
+    timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
+  }
+  if (mode_ == MODE_FULL) {
+    diff_len_ = len;
+    diff_pad_ = 0;
+    datasizes[0] = len;
+    datasizes[1] = 0;
+    if (header) std::memset(header, 0, sizeof(*header));
+    return ST_OK;
+  }
   const Layout& L = *lay_host_;
   last_device_error = err_host_[0];
   if (map_size_.p) map_size_host_ = err_host_[1];
-  float ms[3];
-  cudaEventElapsedTime(&ms[0], ev_[0], ev_[1]);
-  cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
-  cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
-  timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
-  float leaf = 0, rest = 0;
-  cudaEventElapsedTime(&leaf, ev_[1], ev_[4]);
-  cudaEventElapsedTime(&rest, ev_[4], ev_[2]);
-  phase_times[0] = leaf * 1e-3; phase_times[1] = rest * 1e-3; phase_times[2] = ms[2] * 1e-3;
+  if (timed_) {
+    float leaf = 0, rest = 0;
+    cudaEventElapsedTime(&leaf, ev_[1], ev_[4]);
+    cudaEventElapsedTime(&rest, ev_[4], ev_[2]);
+    phase_times[0] = leaf * 1e-3; phase_times[1] = rest * 1e-3; phase_times[2] = ms[2] * 1e-3;
+  }
   if (last_device_error & DERR_SPIN) return fail(ST_ETIMEOUT, "bounded device wait expired");
   if (last_device_error & (DERR_MAP_FULL | DERR_CAPACITY)) return fail(ST_ENOMEM, "device table or staging buffer full");
   if (last_device_error & DERR_MISSING) return fail(ST_EINTERNAL, "root digest missing from the map");
@@ -338,6 +377,33 @@ int Engine::finish(const uint8_t* data, uint64_t len, HeaderHost* header) {
     header->num_shift_dupl = num_shift_dupl;
   }
   return ST_OK;
+}
+
+uint64_t Engine::signature(const uint8_t* data, uint64_t len) const {
+  // everything a captured launch sequence bakes in: the input, every device
+  // buffer, the map and sort capacities, the baseline branch
+  const uint64_t v[] = {(uint64_t)data, len, (uint64_t)digests_.p, (uint64_t)labels_.p, (uint64_t)rflag_.p,
+                        (uint64_t)chunk_slot_.p, (uint64_t)changed_list_.p, (uint64_t)changed_count_.p,
+                        (uint64_t)slots_.p, map_cap_, (uint64_t)map_size_.p, (uint64_t)err_.p, (uint64_t)fo_list_.p,
+                        (uint64_t)sh_list_.p, (uint64_t)reg_chunk_.p, (uint64_t)reg_slot_.p, (uint64_t)reg_len_.p,
+                        (uint64_t)sh_key_.p, (uint64_t)sh_prev_.p, (uint64_t)hist_.p, hist_.n, (uint64_t)rep_.p,
+                        (uint64_t)rank_.p, (uint64_t)fo_val_.p, (uint64_t)sort_mat_.p, sort_mat_.n, (uint64_t)scan_.p,
+                        (uint64_t)scan_total_.p, (uint64_t)scan2_.p, (uint64_t)scan_total2_.p, (uint64_t)stage_.p,
+                        stage_.n, (uint64_t)lay_.p, (uint64_t)sp_.p, (uint64_t)baseline_path_, (uint64_t)mode_,
+                        (uint64_t)leaf_tune_.rows, (uint64_t)leaf_tune_.ctas_per_sm, (uint64_t)leaf_tune_.direct};
+  uint64_t h = 1469598103934665603ull;
+  for (uint64_t x : v) h = (h ^ x) * 1099511628211ull;
+  return h;
+}
+
+uint64_t Engine::device_bytes() const {
+  return sizeof(Digest) * digests_.n + labels_.n + rflag_.n +
+         sizeof(uint32_t) * (chunk_slot_.n + changed_list_.n + changed_count_.n + map_size_.n + err_.n + fo_list_.n +
+                             sh_list_.n + reg_chunk_.n + reg_slot_.n + reg_len_.n + sh_key_.n + sh_prev_.n + hist_.n +
+                             rep_.n + rank_.n) +
+         sizeof(MapSlot) * slots_.n +
+         sizeof(uint64_t) * (fo_val_.n + sort_mat_.n + scan_.n + scan_total_.n + scan2_.n + scan_total2_.n) + stage_.n +
+         sizeof(Layout) * lay_.n + sizeof(StepParams) * sp_.n;
 }
 
 const uint8_t* Engine::diff_device() const { return stage_.p ? stage_.p + diff_pad_ : nullptr; }

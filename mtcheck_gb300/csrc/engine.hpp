@@ -75,6 +75,33 @@ class Engine {
   // checkpoint(header_t&, ...) of the reference: the diff is assembled in
   // device memory; current_id is not advanced.
   int checkpoint(const uint8_t* dev_data, uint64_t len, bool make_baseline, HeaderHost* header);
+  // The same checkpoint in three parts, for callers that batch engines or
+  // capture the work into a CUDA graph:
+  //   prepare      -- validation and every allocation; may synchronise
+  //   stage_params -- host-side step values (id, epochs) for the next enqueue
+  //   enqueue      -- stream-ordered work only (capturable once prepared):
+  //                   reads the step values, writes the diff and the layout
+  //                   readback into pinned host memory
+  //   complete     -- after the stream has drained: error mapping, counters
+  // id_headroom sizes the per-source-checkpoint tables for that many further
+  // checkpoints, so that one captured sequence serves them all.
+  int prepare(const uint8_t* dev_data, uint64_t len, bool make_baseline, uint32_t id_headroom);
+  void stage_params();
+  int enqueue(const uint8_t* dev_data, uint64_t len, bool timed);
+  int complete(uint64_t len, HeaderHost* header);
+  // Fingerprint of everything a captured sequence depends on.
+  uint64_t signature(const uint8_t* dev_data, uint64_t len) const;
+  bool fresh() const { return fresh_; }
+  void set_max_load(double f) { max_load_ = f; }
+  double max_load() const { return max_load_; }
+  void set_leaf_tune(const LeafTune& t) { leaf_tune_ = t; }
+  const LeafTune& leaf_tune() const { return leaf_tune_; }
+  uint64_t map_capacity() const { return map_cap_; }
+  // Free device buffers replaced by map growth; call once the stream has
+  // drained (the single-call path does it itself).
+  void release_retired();
+  uint64_t device_bytes() const;
+
   // Copy the staged diff to host memory (pinned or pageable).
   int copy_diff(void* host, uint64_t cap);
   const uint8_t* diff_device() const;
@@ -100,22 +127,29 @@ class Engine {
 
   cudaStream_t stream() const { return stream_; }
   void set_stream(cudaStream_t s) { stream_ = s; }
+  // For engines on a non-blocking stream of the library (batch members,
+  // server processes): single calls first wait for the work already issued
+  // to the legacy default stream, where callers usually write their buffers.
+  void set_order_after_legacy(bool on) { order_after_legacy_ = on; }
+  int order_inputs();
   uint32_t launches() const { return launches_; }
 
  private:
   int fail(int code, const std::string& msg);
-  int ensure_state(uint32_t N, bool fresh);
+  int ensure_state(uint32_t N, bool fresh, uint32_t id_headroom);
   int ensure_map(uint64_t want_entries, bool reset);
   int ensure_sort(uint32_t K);
   int run_tree(const uint8_t* data, uint64_t len, bool baseline_path);
   int run_list_basic(const uint8_t* data, uint64_t len);
-  int finish(const uint8_t* data, uint64_t len, HeaderHost* header);
   GatherArgs gather_args(const uint8_t* data, uint64_t len);
 
   int mode_, hash_kind_;
   uint32_t cs_;
   cudaStream_t stream_ = nullptr;
   bool allocated_ = false;
+  bool fresh_ = false, baseline_path_ = false, timed_ = true, order_after_legacy_ = false;
+  double max_load_ = 0.75;
+  LeafTune leaf_tune_{};
   uint32_t N_ = 0, M_ = 0;
   uint32_t epoch_ = 0;
   uint64_t map_cap_ = 0;
@@ -139,6 +173,7 @@ class Engine {
   TmaCache tma_;
   cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   RestartScratch* rs_ = nullptr;  // restart buffers, created on first use
+  std::vector<void*> retired_;    // replaced map tables awaiting cudaFree
 };
 
 }  // namespace mtc

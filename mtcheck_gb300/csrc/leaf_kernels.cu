@@ -24,9 +24,9 @@
 namespace mtc {
 
 namespace {
-constexpr int kRows = 256;    // consumer threads = chunks per tile = TMA box rows
+// R (template) = consumer threads = chunks per tile = TMA box rows; one
+// producer warp more per CTA
 constexpr int kStages = 3;    // boxes in flight per CTA
-constexpr int kThreads = kRows + 32;
 
 template <int W>
 __device__ __forceinline__ uint32_t swz(uint32_t logical) {
@@ -138,9 +138,9 @@ __device__ __forceinline__ bool needs_old(const LeafArgs& a) {
 // ---------------------------------------------------------------------------
 // TMA pipeline kernel.
 // ---------------------------------------------------------------------------
-template <int HK, int EPI, int W>
-__global__ void __launch_bounds__(kThreads) leaf_tma_kernel(const __grid_constant__ CUtensorMap tmap, LeafArgs a,
-                                                            uint32_t n_full) {
+template <int HK, int EPI, int W, int kRows>
+__global__ void __launch_bounds__(kRows + 32) leaf_tma_kernel(const __grid_constant__ CUtensorMap tmap, LeafArgs a,
+                                                              uint32_t n_full) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr uint32_t kStageBytes = kRows * W;
@@ -223,6 +223,8 @@ __global__ void __launch_bounds__(kThreads) leaf_tma_kernel(const __grid_constan
           mm.block(v.x, v.y, v.z, v.w);
         }
       }
+      // release the stage: this thread's reads before the refill's TMA write
+      fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
@@ -282,13 +284,13 @@ int tma_width(uint32_t cs) {
   return 0;
 }
 
-bool make_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, int W, uint32_t n_full) {
-  if (c->ptr == data && c->len == len && c->cs == cs && c->width == W) return true;
+bool make_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, int W, int rows, uint32_t n_full) {
+  if (c->ptr == data && c->len == len && c->cs == cs && c->width == W && c->rows == rows) return true;
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {cs, n_full};
   cuuint64_t strides[1] = {cs};
-  cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)kRows};
+  cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)rows};
   cuuint32_t estr[2] = {1, 1};
   CUtensorMapSwizzle sw = W == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
                         : W == 64  ? CU_TENSOR_MAP_SWIZZLE_64B
@@ -298,43 +300,51 @@ bool make_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, int 
                   CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) { c->ptr = nullptr; return false; }
-  c->ptr = data; c->len = len; c->cs = cs; c->width = W;
+  c->ptr = data; c->len = len; c->cs = cs; c->width = W; c->rows = rows;
   return true;
 }
 
-template <int HK, int EPI, int W>
-cudaError_t launch_tma_t(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, cudaStream_t s) {
-  auto k = leaf_tma_kernel<HK, EPI, W>;
-  const size_t smem = 1024 + (size_t)kStages * kRows * W + 2 * kStages * sizeof(uint64_t);
-  static bool attr_set = false;
-  if (!attr_set) {
+template <int HK, int EPI, int W, int R>
+cudaError_t launch_tma_t(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int ctas_per_sm, cudaStream_t s) {
+  auto k = leaf_tma_kernel<HK, EPI, W, R>;
+  const size_t smem = 1024 + (size_t)kStages * R * W + 2 * kStages * sizeof(uint64_t);
+  static std::atomic<bool> attr_set{false};
+  if (!attr_set.load(std::memory_order_acquire)) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_set.store(true, std::memory_order_release);
   }
-  const uint32_t ntiles = (n_full + kRows - 1) / kRows;
-  int per_sm = W >= 128 ? 2 : 3;
+  const uint32_t ntiles = (n_full + R - 1) / R;
+  // resident CTAs per SM that fit in 227 KB of shared memory, at most 3 by default
+  const int fit = (int)((227u * 1024u) / smem);
+  int per_sm = ctas_per_sm > 0 ? ctas_per_sm : 3;
+  if (per_sm > fit) per_sm = fit > 0 ? fit : 1;
   uint32_t grid = (uint32_t)(num_sms() * per_sm);
   if (grid > ntiles) grid = ntiles;
-  k<<<grid, kThreads, smem, s>>>(m, a, n_full);
+  k<<<grid, R + 32, smem, s>>>(m, a, n_full);
   note_launch();
   return cudaGetLastError();
 }
 
-template <int HK, int EPI>
-cudaError_t launch_tma_w(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, cudaStream_t s) {
+template <int HK, int EPI, int R>
+cudaError_t launch_tma_w(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, int per_sm, cudaStream_t s) {
   switch (W) {
-    case 128: return launch_tma_t<HK, EPI, 128>(a, m, n_full, s);
-    case 64: return launch_tma_t<HK, EPI, 64>(a, m, n_full, s);
-    case 32: return launch_tma_t<HK, EPI, 32>(a, m, n_full, s);
-    default: return launch_tma_t<HK, EPI, 16>(a, m, n_full, s);
+    case 128: return launch_tma_t<HK, EPI, 128, R>(a, m, n_full, per_sm, s);
+    case 64: return launch_tma_t<HK, EPI, 64, R>(a, m, n_full, per_sm, s);
+    case 32: return launch_tma_t<HK, EPI, 32, R>(a, m, n_full, per_sm, s);
+    default: return launch_tma_t<HK, EPI, 16, R>(a, m, n_full, per_sm, s);
   }
 }
 
 template <int EPI>
-cudaError_t launch_tma_e(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, cudaStream_t s) {
-  if (a.hash_kind == HASH_MD5) return launch_tma_w<HASH_MD5, EPI>(a, m, n_full, W, s);
-  return launch_tma_w<HASH_MURMUR3, EPI>(a, m, n_full, W, s);
+cudaError_t launch_tma_e(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, const LeafTune& t,
+                         cudaStream_t s) {
+  if (t.rows == 128) {
+    if (a.hash_kind == HASH_MD5) return launch_tma_w<HASH_MD5, EPI, 128>(a, m, n_full, W, t.ctas_per_sm, s);
+    return launch_tma_w<HASH_MURMUR3, EPI, 128>(a, m, n_full, W, t.ctas_per_sm, s);
+  }
+  if (a.hash_kind == HASH_MD5) return launch_tma_w<HASH_MD5, EPI, 256>(a, m, n_full, W, t.ctas_per_sm, s);
+  return launch_tma_w<HASH_MURMUR3, EPI, 256>(a, m, n_full, W, t.ctas_per_sm, s);
 }
 
 template <int EPI>
@@ -357,12 +367,13 @@ cudaError_t dispatch_direct(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStr
     default: return launch_direct<EPI_HASH>(a, c0, c1, s);
   }
 }
-cudaError_t dispatch_tma(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, cudaStream_t s) {
+cudaError_t dispatch_tma(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int W, const LeafTune& t,
+                         cudaStream_t s) {
   switch (a.epi) {
-    case EPI_TREE: return launch_tma_e<EPI_TREE>(a, m, n_full, W, s);
-    case EPI_LIST: return launch_tma_e<EPI_LIST>(a, m, n_full, W, s);
-    case EPI_BASIC: return launch_tma_e<EPI_BASIC>(a, m, n_full, W, s);
-    default: return launch_tma_e<EPI_HASH>(a, m, n_full, W, s);
+    case EPI_TREE: return launch_tma_e<EPI_TREE>(a, m, n_full, W, t, s);
+    case EPI_LIST: return launch_tma_e<EPI_LIST>(a, m, n_full, W, t, s);
+    case EPI_BASIC: return launch_tma_e<EPI_BASIC>(a, m, n_full, W, t, s);
+    default: return launch_tma_e<EPI_HASH>(a, m, n_full, W, t, s);
   }
 }
 }  // namespace
@@ -382,14 +393,16 @@ int num_sms() {
   return n;
 }
 
-cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s) {
+cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, const LeafTune& tune) {
   if (a.n_chunks == 0) return cudaSuccess;
   const uint32_t n_full = (uint32_t)(a.len / a.cs);
   const int W = tma_width(a.cs);
   const bool aligned = (reinterpret_cast<uintptr_t>(a.data) & 15) == 0;
+  LeafTune t = tune;
+  if (t.rows != 128) t.rows = 256;
   uint32_t done = 0;
-  if (W && aligned && n_full > 0 && cache && make_tmap(cache, a.data, a.len, a.cs, W, n_full)) {
-    cudaError_t e = dispatch_tma(a, cache->map, n_full, W, s);
+  if (!t.direct && W && aligned && n_full > 0 && cache && make_tmap(cache, a.data, a.len, a.cs, W, t.rows, n_full)) {
+    cudaError_t e = dispatch_tma(a, cache->map, n_full, W, t, s);
     if (e != cudaSuccess) return e;
     done = n_full;
   }

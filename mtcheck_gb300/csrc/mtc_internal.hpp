@@ -57,13 +57,27 @@ struct TmaCache {
   uint64_t len = 0;
   uint32_t cs = 0;
   int width = 0;
+  int rows = 0;
   CUtensorMap map;
+};
+
+// Launch shape of the leaf hashing kernel.  Every choice gives the same
+// digests and labels; only the speed differs.
+//   rows        -- chunks per CTA tile (TMA box height): 128 or 256
+//   ctas_per_sm -- resident CTAs per SM of the persistent grid (0: the most
+//                  that fit in shared memory, at most 3)
+//   direct      -- 1: every thread loads its own chunk from global memory
+//                  instead of the TMA-staged shared-memory pipeline
+struct LeafTune {
+  int rows = 256;
+  int ctas_per_sm = 0;
+  int direct = 0;
 };
 
 // Launch the leaf hashing kernel(s) over every chunk.  Uses the TMA pipeline
 // for chunk sizes that are a multiple of 128 bytes (or 16/32/64) on 16-byte
 // aligned buffers, and a thread-per-chunk kernel otherwise and for the tail.
-cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s);
+cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, const LeafTune& tune = LeafTune{});
 // Tree / list: map inserts of the changed chunks collected by launch_leaves,
 // then the lowest-offset demotion (src/tree_approach.cpp:356-369; for the
 // list a changed chunk is a first occurrence only if it owns its digest).

@@ -606,6 +606,7 @@ int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint
                     const std::vector<uint64_t>& lens, const std::vector<HeaderHost>& headers, uint32_t id) {
   cudaStream_t s = stream_;
   if (id >= dev_diffs.size()) return fail(ST_EINVAL, "checkpoint id outside the chain");
+  if (int rc = order_inputs()) return rc;
   cudaEvent_t e0 = ev_[0], e1 = ev_[1];
   cudaEventRecord(e0, s);
   if (mode_ == MODE_FULL) {

@@ -156,3 +156,20 @@ def pattern2(nbytes, cs, steps, seed=2, device=None, rate=(0.001, 0.05), run_max
         if zero_range:
             buf[zero_range[0]:zero_range[1]] = 0
         yield buf
+
+
+def batch_mix(count=96, seed=4, median_mib=72.0, sigma=1.2, lo_mib=1, hi_mib=512,
+              chunk_sizes=(64, 128, 512, 4096), rate=(0.001, 0.10)):
+    """Members of the batched workload: sizes log-normal (median `median_mib`,
+    log-sigma `sigma`) clipped to [lo_mib, hi_mib] MiB, chunk size uniform over
+    `chunk_sizes`, Murmur3 and MD5 alternating, one change rate per member
+    drawn uniformly from `rate`.  Returns a list of dicts."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        mib = float(np.clip(rng.lognormal(np.log(median_mib), sigma), lo_mib, hi_mib))
+        cs = int(rng.choice(chunk_sizes))
+        nbytes = int(mib * (1 << 20))
+        out.append({"nbytes": nbytes, "chunk_size": cs, "hash": i % 2, "rate": float(rng.uniform(*rate)),
+                    "seed": int(seed * 1000 + i)})
+    return out
