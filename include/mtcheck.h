@@ -206,6 +206,72 @@ int mtc_batch_get_info(const mtc_batch_t* b, mtc_batch_info_t* out);
  * apply the winners */
 int mtc_batch_autotune(mtc_batch_t* b, const uint64_t* lens);
 
+/* ---- request serving (no counterpart in the reference: its MPI driver runs
+ * one process per rank, src/dedup_files_mpi.cpp:54-120) ----
+ * A server owns many deduplicators ("processes") and one worker thread that
+ * admits checkpoint and restart requests continuously: a request starts when
+ * its process has nothing else on the GPU, an in-flight slot is free and its
+ * memory fits the HBM budget, so requests of different processes overlap on
+ * the device.  Each process keeps its digest state and its chain of
+ * incremental checkpoints in HBM; beyond the budget the least recently used
+ * idle processes spill (archived checkpoints first, then digest state) to
+ * pinned host memory and come back on their next request.  Results equal
+ * those of a lone handle given the same requests in the same order.
+ * Inputs are read after the work already issued to the legacy default stream
+ * when the request was submitted; they must not change until it completes. */
+typedef struct mtc_server mtc_server_t;
+typedef struct mtc_server_options {
+  uint64_t hbm_budget;     /* bytes of device memory for all process state (0: 120 GB) */
+  uint32_t max_inflight;   /* requests on the GPU at once (0: 64) */
+  uint32_t id_headroom;    /* checkpoint ids one captured graph serves (0: 64) */
+  int32_t use_graph;       /* replay a per-process CUDA graph for incremental checkpoints;
+                              while the worker captures one, no thread of the application
+                              may synchronise the whole device (cudaDeviceSynchronize) */
+  int32_t reserved;
+} mtc_server_options_t;
+#define MTC_REQ_CHECKPOINT 0
+#define MTC_REQ_RESTART 1
+typedef struct mtc_completion {
+  uint64_t ticket;
+  uint32_t pid;
+  int32_t kind;            /* MTC_REQ_* */
+  int32_t status;          /* MTC_* */
+  uint32_t chkpt_id;       /* checkpoint written, or restarted */
+  uint64_t diff_len;       /* size of the incremental checkpoint written */
+  double t_submit_ms, t_admit_ms, t_done_ms;  /* mtc_now_ms() clock */
+} mtc_completion_t;
+typedef struct mtc_server_stats {
+  uint64_t submitted, completed, failed, checkpoints, restarts;
+  uint64_t bytes_checkpointed, bytes_restarted;
+  uint64_t spilled_diffs, spilled_states, restored_states, staged_diffs, spilled_bytes;
+  uint64_t graph_captures, graph_replays;
+  uint64_t hbm_used, hbm_peak, pinned_reserved, deferred_admissions;
+  uint32_t inflight_peak;
+  uint32_t reserved;
+} mtc_server_stats_t;
+int mtc_server_create(const mtc_server_options_t* opt, mtc_server_t** out);
+/* waits for every submitted request, then frees everything */
+int mtc_server_destroy(mtc_server_t* s);
+int mtc_server_add_process(mtc_server_t* s, int approach, int hash, uint32_t chunk_size, uint32_t* pid);
+/* checkpoint(data, len, diff_h, make_baseline) of process pid; the
+ * incremental checkpoint is kept in the process's chain */
+int mtc_server_submit_checkpoint(mtc_server_t* s, uint32_t pid, const void* dev_data, uint64_t len,
+                                 int make_baseline, uint64_t* ticket);
+/* restart of checkpoint chkpt_id of process pid into dev_out (len bytes) */
+int mtc_server_submit_restart(mtc_server_t* s, uint32_t pid, uint32_t chkpt_id, void* dev_out, uint64_t len,
+                              uint64_t* ticket);
+/* up to max completions into out (*n of them), waiting up to wait_ms for one */
+int mtc_server_poll(mtc_server_t* s, mtc_completion_t* out, uint32_t max, uint32_t* n, double wait_ms);
+/* wait until every submitted request has completed (MTC_ETIMEOUT on timeout) */
+int mtc_server_drain(mtc_server_t* s, double timeout_ms);
+int mtc_server_chain_length(mtc_server_t* s, uint32_t pid, uint32_t* n);
+/* copy checkpoint chkpt_id of process pid to host memory (host NULL: size only) */
+int mtc_server_copy_diff(mtc_server_t* s, uint32_t pid, uint32_t chkpt_id, void* host, uint64_t capacity,
+                         uint64_t* len);
+int mtc_server_get_stats(mtc_server_t* s, mtc_server_stats_t* out);
+/* the clock of the completion times (milliseconds, monotonic) */
+double mtc_now_ms(void);
+
 /* ---- launch tuning (no counterpart in the reference) ----
  * Shape of the chunk-hashing kernel and the digest map's load factor.  Any
  * setting gives identical output; only the speed changes. */

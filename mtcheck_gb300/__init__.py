@@ -66,6 +66,28 @@ class Tune(ctypes.Structure):
                 "max_load": self.max_load}
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32), ("id_headroom", ctypes.c_uint32),
+                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_uint64), ("pid", ctypes.c_uint32), ("kind", ctypes.c_int32),
+                ("status", ctypes.c_int32), ("chkpt_id", ctypes.c_uint32), ("diff_len", ctypes.c_uint64),
+                ("t_submit_ms", ctypes.c_double), ("t_admit_ms", ctypes.c_double), ("t_done_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "submitted", "completed", "failed", "checkpoints", "restarts", "bytes_checkpointed", "bytes_restarted",
+        "spilled_diffs", "spilled_states", "restored_states", "staged_diffs", "spilled_bytes", "graph_captures",
+        "graph_replays", "hbm_used", "hbm_peak", "pinned_reserved", "deferred_admissions")] + \
+        [("inflight_peak", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
 # every symbol of include/mtcheck.h with its ctypes signature
 _VP, _U32, _U64, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
 SIGNATURES = {
@@ -99,6 +121,17 @@ SIGNATURES = {
     "mtc_batch_set_options": (_I, [_VP, _I, _U32]),
     "mtc_batch_get_info": (_I, [_VP, ctypes.POINTER(BatchInfo)]),
     "mtc_batch_autotune": (_I, [_VP, ctypes.POINTER(_U64)]),
+    "mtc_server_create": (_I, [ctypes.POINTER(ServerOptions), ctypes.POINTER(_VP)]),
+    "mtc_server_destroy": (_I, [_VP]),
+    "mtc_server_add_process": (_I, [_VP, _I, _I, _U32, ctypes.POINTER(_U32)]),
+    "mtc_server_submit_checkpoint": (_I, [_VP, _U32, _VP, _U64, _I, ctypes.POINTER(_U64)]),
+    "mtc_server_submit_restart": (_I, [_VP, _U32, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
+    "mtc_server_poll": (_I, [_VP, ctypes.POINTER(Completion), _U32, ctypes.POINTER(_U32), ctypes.c_double]),
+    "mtc_server_drain": (_I, [_VP, ctypes.c_double]),
+    "mtc_server_chain_length": (_I, [_VP, _U32, ctypes.POINTER(_U32)]),
+    "mtc_server_copy_diff": (_I, [_VP, _U32, _U32, _VP, _U64, ctypes.POINTER(_U64)]),
+    "mtc_server_get_stats": (_I, [_VP, ctypes.POINTER(ServerStats)]),
+    "mtc_now_ms": (ctypes.c_double, []),
     "mtc_set_tuning": (_I, [_VP, ctypes.POINTER(Tune)]),
     "mtc_get_tuning": (_I, [_VP, ctypes.POINTER(Tune)]),
     "mtc_autotune": (_I, [_I, _I, _U32, _U64, ctypes.POINTER(Tune), ctypes.POINTER(ctypes.c_double),
@@ -370,6 +403,83 @@ class Batch:
         i = BatchInfo()
         _check(load().mtc_batch_get_info(self.b, ctypes.byref(i)))
         return i
+
+
+class Server:
+    """Request-serving loop (mtc_server_*): processes submit checkpoint and
+    restart requests; a worker thread admits them continuously under an HBM
+    budget, spilling cold state to pinned host memory."""
+
+    def __init__(self, hbm_budget=0, max_inflight=0, id_headroom=0, use_graph=False):
+        o = ServerOptions(int(hbm_budget), int(max_inflight), int(id_headroom), int(use_graph), 0)
+        s = _VP()
+        _check(load().mtc_server_create(ctypes.byref(o), ctypes.byref(s)))
+        self.s = s
+        self._buf = (Completion * 256)()
+
+    def close(self):
+        if getattr(self, "s", None):
+            load().mtc_server_destroy(self.s)
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_process(self, approach, hash, chunk_size):
+        pid = _U32()
+        _check(load().mtc_server_add_process(self.s, approach, hash, chunk_size, ctypes.byref(pid)))
+        return int(pid.value)
+
+    def submit_checkpoint(self, pid, buf, make_baseline=False):
+        ptr, n = _dev_ptr(buf)
+        t = _U64()
+        _check(load().mtc_server_submit_checkpoint(self.s, pid, ptr, n, int(make_baseline), ctypes.byref(t)))
+        return int(t.value)
+
+    def submit_restart(self, pid, chkpt_id, out):
+        ptr, n = _dev_ptr(out)
+        t = _U64()
+        _check(load().mtc_server_submit_restart(self.s, pid, chkpt_id, ptr, n, ctypes.byref(t)))
+        return int(t.value)
+
+    def poll(self, wait_ms=0.0):
+        """List of completions (dicts), waiting up to wait_ms for the first."""
+        n = _U32()
+        _check(load().mtc_server_poll(self.s, self._buf, len(self._buf), ctypes.byref(n), float(wait_ms)))
+        out = []
+        for i in range(n.value):
+            c = self._buf[i]
+            out.append({"ticket": c.ticket, "pid": c.pid, "kind": c.kind, "status": c.status,
+                        "chkpt_id": c.chkpt_id, "diff_len": c.diff_len, "t_submit_ms": c.t_submit_ms,
+                        "t_admit_ms": c.t_admit_ms, "t_done_ms": c.t_done_ms})
+        return out
+
+    def drain(self, timeout_ms=600000.0):
+        _check(load().mtc_server_drain(self.s, float(timeout_ms)))
+
+    def chain_length(self, pid):
+        n = _U32()
+        _check(load().mtc_server_chain_length(self.s, pid, ctypes.byref(n)))
+        return int(n.value)
+
+    def diff(self, pid, chkpt_id):
+        n = _U64()
+        _check(load().mtc_server_copy_diff(self.s, pid, chkpt_id, None, 0, ctypes.byref(n)))
+        host = np.empty(n.value, np.uint8)
+        _check(load().mtc_server_copy_diff(self.s, pid, chkpt_id, host.ctypes.data, n.value, ctypes.byref(n)))
+        return host.tobytes()
+
+    def stats(self):
+        s = ServerStats()
+        _check(load().mtc_server_get_stats(self.s, ctypes.byref(s)))
+        return s.as_dict()
+
+
+def now_ms():
+    return float(load().mtc_now_ms())
 
 
 def autotune(approach, hash, chunk_size, nbytes):

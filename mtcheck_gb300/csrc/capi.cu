@@ -9,12 +9,17 @@
 #include "../../include/mtcheck.h"
 #include "batch.hpp"
 #include "engine.hpp"
+#include "server.hpp"
 #include "host_digest.hpp"
 #include "logs.hpp"
 
 struct mtc_dedup {
   mtc::Engine* eng;
   bool borrowed = false;  // a batch member: the batch owns the engine
+};
+
+struct mtc_server {
+  mtc::Server* s = nullptr;
 };
 
 struct mtc_batch {
@@ -391,6 +396,99 @@ int mtc_batch_autotune(mtc_batch_t* b, const uint64_t* lens) {
   }
   return MTC_OK;
 }
+
+// ---- server ----
+int mtc_server_create(const mtc_server_options_t* opt, mtc_server_t** out) {
+  if (!out) return ret(MTC_EINVAL, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ret(MTC_ECUDA, "no CUDA device");
+  mtc::ServerOptions o;
+  if (opt) {
+    if (opt->hbm_budget) o.hbm_budget = opt->hbm_budget;
+    if (opt->max_inflight) o.max_inflight = opt->max_inflight;
+    if (opt->id_headroom) o.id_headroom = opt->id_headroom;
+    o.use_graph = opt->use_graph;
+  }
+  auto* h = new (std::nothrow) mtc_server;
+  if (!h) return ret(MTC_ENOMEM, "out of host memory");
+  h->s = new (std::nothrow) mtc::Server(o);
+  if (!h->s) { delete h; return ret(MTC_ENOMEM, "out of host memory"); }
+  *out = h;
+  return MTC_OK;
+}
+
+int mtc_server_destroy(mtc_server_t* s) {
+  if (!s) return MTC_OK;
+  s->s->drain(1e12);
+  delete s->s;
+  delete s;
+  return MTC_OK;
+}
+
+int mtc_server_add_process(mtc_server_t* s, int approach, int hash, uint32_t chunk_size, uint32_t* pid) {
+  if (!s || !pid) return ret(MTC_EINVAL, "NULL argument");
+  if (!valid_mode(approach)) return ret(MTC_EINVAL, "unknown approach");
+  if (hash != MTC_HASH_MURMUR3 && hash != MTC_HASH_MD5) return ret(MTC_EINVAL, "unknown hash");
+  if (chunk_size == 0) return ret(MTC_EINVAL, "chunk size is 0");
+  int rc = s->s->add_process(approach, hash, chunk_size, pid);
+  return rc ? ret(rc, s->s->error()) : MTC_OK;
+}
+
+int mtc_server_submit_checkpoint(mtc_server_t* s, uint32_t pid, const void* dev_data, uint64_t len,
+                                 int make_baseline, uint64_t* ticket) {
+  if (!s) return ret(MTC_EINVAL, "NULL server");
+  int rc = s->s->submit_checkpoint(pid, static_cast<const uint8_t*>(dev_data), len, make_baseline != 0, ticket);
+  return rc ? ret(rc, s->s->error()) : MTC_OK;
+}
+
+int mtc_server_submit_restart(mtc_server_t* s, uint32_t pid, uint32_t chkpt_id, void* dev_out, uint64_t len,
+                              uint64_t* ticket) {
+  if (!s) return ret(MTC_EINVAL, "NULL server");
+  int rc = s->s->submit_restart(pid, chkpt_id, static_cast<uint8_t*>(dev_out), len, ticket);
+  return rc ? ret(rc, s->s->error()) : MTC_OK;
+}
+
+int mtc_server_poll(mtc_server_t* s, mtc_completion_t* out, uint32_t max, uint32_t* n, double wait_ms) {
+  if (!s || !n || (max && !out)) return ret(MTC_EINVAL, "NULL argument");
+  static_assert(sizeof(mtc_completion_t) == sizeof(mtc::Completion), "completion layout");
+  *n = s->s->poll(reinterpret_cast<mtc::Completion*>(out), max, wait_ms);
+  return MTC_OK;
+}
+
+int mtc_server_drain(mtc_server_t* s, double timeout_ms) {
+  if (!s) return ret(MTC_EINVAL, "NULL server");
+  return s->s->drain(timeout_ms) ? MTC_OK : ret(MTC_ETIMEOUT, "requests still in flight");
+}
+
+int mtc_server_chain_length(mtc_server_t* s, uint32_t pid, uint32_t* n) {
+  if (!s || !n) return ret(MTC_EINVAL, "NULL argument");
+  return s->s->chain_length(pid, n) ? ret(MTC_EINVAL, "unknown process") : MTC_OK;
+}
+
+int mtc_server_copy_diff(mtc_server_t* s, uint32_t pid, uint32_t chkpt_id, void* host, uint64_t capacity,
+                         uint64_t* len) {
+  if (!s) return ret(MTC_EINVAL, "NULL server");
+  int rc = s->s->copy_diff(pid, chkpt_id, host, capacity, len);
+  return rc ? ret(rc, "unknown process or checkpoint, or short buffer") : MTC_OK;
+}
+
+int mtc_server_get_stats(mtc_server_t* s, mtc_server_stats_t* o) {
+  if (!s || !o) return ret(MTC_EINVAL, "NULL argument");
+  const mtc::ServerStats t = s->s->stats();
+  std::memset(o, 0, sizeof(*o));
+  o->submitted = t.submitted; o->completed = t.completed; o->failed = t.failed;
+  o->checkpoints = t.checkpoints; o->restarts = t.restarts;
+  o->bytes_checkpointed = t.bytes_checkpointed; o->bytes_restarted = t.bytes_restarted;
+  o->spilled_diffs = t.spilled_diffs; o->spilled_states = t.spilled_states; o->restored_states = t.restored_states;
+  o->staged_diffs = t.staged_diffs; o->spilled_bytes = t.spilled_bytes;
+  o->graph_captures = t.graph_captures; o->graph_replays = t.graph_replays;
+  o->hbm_used = t.hbm_used; o->hbm_peak = t.hbm_peak; o->pinned_reserved = t.pinned_reserved;
+  o->deferred_admissions = t.deferred_admissions; o->inflight_peak = t.inflight_peak;
+  return MTC_OK;
+}
+
+double mtc_now_ms(void) { return mtc::Server::now_ms(); }
 
 // ---- tuning ----
 int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t) {

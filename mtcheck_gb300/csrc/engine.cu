@@ -12,6 +12,8 @@
 
 namespace mtc {
 
+static __global__ void set_word_kernel(uint32_t* p, uint32_t v) { *p = v; }
+
 static uint64_t next_pow2(uint64_t v) {
   uint64_t c = 1;
   while (c < v) c <<= 1;
@@ -75,9 +77,11 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
   DigestMap from{slots_.p, map_cap_ - 1, map_size_.p};
   DigestMap to{fresh.p, need - 1, map_size_.p};
   MTC_CUDA(launch_map_rehash(from, map_cap_, to, err_.p, stream_));
-  // the old table is freed once the stream has drained (release_retired):
+  // the old table is freed after the rehash: stream-ordered from a pool,
+  // otherwise once the stream has drained (release_retired), because
   // cudaFree here would wait for the whole device
-  retired_.push_back(slots_.p);
+  if (pool_) cudaFreeAsync(slots_.p, stream_);
+  else retired_.push_back(slots_.p);
   slots_.p = fresh.p;
   slots_.n = fresh.n;
   fresh.p = nullptr;
@@ -255,6 +259,7 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
 
 int Engine::prepare(const uint8_t* data, uint64_t len, bool make_baseline, uint32_t id_headroom) {
   if (!data || len == 0) return fail(ST_EINVAL, "empty buffer");
+  if (spilled_) return fail(ST_EINVAL, "state spilled to host: restore it first");
   const uint64_t n64 = (len + cs_ - 1) / cs_;
   if (n64 >= (1ull << 31)) return fail(ST_ENOTSUP, "more than 2^31 chunks");
   const uint32_t N = (uint32_t)n64;
@@ -394,6 +399,72 @@ uint64_t Engine::signature(const uint8_t* data, uint64_t len) const {
   uint64_t h = 1469598103934665603ull;
   for (uint64_t x : v) h = (h ^ x) * 1099511628211ull;
   return h;
+}
+
+template <class F>
+void Engine::for_each_buf(F f) {
+  f(digests_); f(labels_); f(rflag_); f(chunk_slot_); f(changed_list_); f(changed_count_); f(slots_);
+  f(map_size_); f(err_); f(fo_list_); f(sh_list_); f(reg_chunk_); f(reg_slot_); f(reg_len_); f(sh_key_);
+  f(sh_prev_); f(hist_); f(rep_); f(rank_); f(fo_val_); f(sort_mat_); f(scan_); f(scan_total_); f(scan2_);
+  f(scan_total2_); f(stage_); f(lay_); f(sp_);
+}
+
+void Engine::set_pool(cudaMemPool_t pool) {
+  pool_ = pool;
+  for_each_buf([&](auto& b) { b.pool = pool; });
+}
+
+uint64_t Engine::spill_bytes() const {
+  const bool tree = mode_ == MODE_TREE || mode_ == MODE_TREE_LOW_OFFSET || mode_ == MODE_TREE_LOW_OFFSET_REF;
+  return sizeof(Digest) * (uint64_t)(tree ? M_ : N_) + sizeof(MapSlot) * map_cap_ + 16;
+}
+
+int Engine::spill_to_host(uint8_t* host) {
+  if (spilled_) return ST_OK;
+  if (!pool_) return fail(ST_ENOTSUP, "spilling needs stream-ordered allocation (a memory pool)");
+  if (!allocated_ || mode_ == MODE_FULL) return fail(ST_EINVAL, "nothing to spill");
+  const bool tree = mode_ == MODE_TREE || mode_ == MODE_TREE_LOW_OFFSET || mode_ == MODE_TREE_LOW_OFFSET_REF;
+  const uint64_t nd = tree ? M_ : N_;  // the digests in use (the buffer may be larger)
+  MTC_CUDA(cudaMemcpyAsync(host, digests_.p, sizeof(Digest) * nd, cudaMemcpyDeviceToHost, stream_));
+  uint8_t* q = host + sizeof(Digest) * nd;
+  if (slots_.p) MTC_CUDA(cudaMemcpyAsync(q, slots_.p, sizeof(MapSlot) * map_cap_, cudaMemcpyDeviceToHost, stream_));
+  q += sizeof(MapSlot) * map_cap_;
+  std::memcpy(q, &map_size_host_, sizeof(uint32_t));
+  spill_nd_ = nd;
+  spill_cap_ = map_cap_;
+  for_each_buf([&](auto& b) { b.release(stream_); });
+  if (rs_) {
+    destroy_restart_scratch(rs_);  // stream-ordered frees
+    rs_ = nullptr;
+  }
+  spilled_ = true;
+  return ST_OK;
+}
+
+int Engine::restore_from_host(const uint8_t* host) {
+  if (!spilled_) return ST_OK;
+  spilled_ = false;
+  const bool tree = mode_ == MODE_TREE || mode_ == MODE_TREE_LOW_OFFSET || mode_ == MODE_TREE_LOW_OFFSET_REF;
+  const uint32_t saved_size = [&] { uint32_t v; std::memcpy(&v, host + sizeof(Digest) * spill_nd_ + sizeof(MapSlot) * spill_cap_, 4); return v; }();
+  int rc = ensure_state(N_, true, 0);  // every buffer, zeroed; map sized for M
+  if (rc) return rc;
+  if (mode_ != MODE_BASIC && slots_.n != spill_cap_) {
+    slots_.release(stream_);
+    MTC_CUDA(slots_.ensure(spill_cap_, stream_));
+  }
+  map_cap_ = mode_ != MODE_BASIC ? spill_cap_ : map_cap_;
+  (void)tree;
+  MTC_CUDA(cudaMemcpyAsync(digests_.p, host, sizeof(Digest) * spill_nd_, cudaMemcpyHostToDevice, stream_));
+  if (mode_ != MODE_BASIC && spill_cap_) {
+    MTC_CUDA(cudaMemcpyAsync(slots_.p, host + sizeof(Digest) * spill_nd_, sizeof(MapSlot) * spill_cap_,
+                             cudaMemcpyHostToDevice, stream_));
+    // the map's size word lives in device memory too
+    set_word_kernel<<<1, 1, 0, stream_>>>(map_size_.p, saved_size);
+    note_launch();
+    MTC_CUDA(cudaGetLastError());
+  }
+  map_size_host_ = saved_size;
+  return ST_OK;
 }
 
 uint64_t Engine::device_bytes() const {

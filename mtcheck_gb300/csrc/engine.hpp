@@ -40,27 +40,42 @@ struct HeaderHost {  // header_t, include/utils.hpp:29-37
 };
 static_assert(sizeof(HeaderHost) == 32, "header_t is 32 bytes");
 
-// Grow-only device array.
+// Grow-only device array.  With a memory pool set, allocation and release
+// are stream-ordered (cudaMallocFromPoolAsync / cudaFreeAsync on the stream
+// of the call) and never wait for the device; without one, cudaMalloc and
+// cudaFree.
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;  // elements
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t owner = nullptr;  // stream of the last pool allocation
   cudaError_t ensure(size_t want, cudaStream_t s, bool keep = false) {
     if (want <= n && p) return cudaSuccess;
     T* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, sizeof(T) * (want ? want : 1));
+    const size_t bytes = sizeof(T) * (want ? want : 1);
+    cudaError_t e = pool ? cudaMallocFromPoolAsync(reinterpret_cast<void**>(&q), bytes, pool, s)
+                         : cudaMalloc(&q, bytes);
     if (e != cudaSuccess) return e;
     if (keep && p && n) cudaMemcpyAsync(q, p, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
     if (p) {
-      cudaStreamSynchronize(s);
-      cudaFree(p);
+      if (pool) {
+        cudaFreeAsync(p, s);
+      } else {
+        cudaStreamSynchronize(s);
+        cudaFree(p);
+      }
     }
     p = q;
     n = want;
+    owner = s;
     return cudaSuccess;
   }
-  void release() {
-    if (p) cudaFree(p);
+  void release(cudaStream_t s = nullptr) {
+    if (p) {
+      if (pool) cudaFreeAsync(p, s ? s : owner);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
   }
@@ -101,6 +116,17 @@ class Engine {
   // drained (the single-call path does it itself).
   void release_retired();
   uint64_t device_bytes() const;
+  // Stream-ordered allocation from `pool` for every device buffer of this
+  // engine (set before the first checkpoint).
+  void set_pool(cudaMemPool_t pool);
+  // Move the persistent state (chunk digests, digest map) to pinned host
+  // memory and free every device buffer; restore it before the next call.
+  // The copies run on the engine's stream; spill_to_host() returns once they
+  // are issued, the host copy is valid after the stream drains.
+  bool spilled() const { return spilled_; }
+  uint64_t spill_bytes() const;
+  int spill_to_host(uint8_t* host);
+  int restore_from_host(const uint8_t* host);
 
   // Copy the staged diff to host memory (pinned or pageable).
   int copy_diff(void* host, uint64_t cap);
@@ -110,6 +136,11 @@ class Engine {
   // of the chain (the main one is index `id`).
   int restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint8_t*>& dev_diffs,
               const std::vector<uint64_t>& lens, const std::vector<HeaderHost>& headers, uint32_t id);
+  // The same in two parts: stream-ordered work, then (after the stream has
+  // drained) timers and error mapping.  The chain must stay valid until then.
+  int restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<const uint8_t*>& dev_diffs,
+                      const std::vector<uint64_t>& lens, const std::vector<HeaderHost>& headers, uint32_t id);
+  int restart_complete();
 
   int mode() const { return mode_; }
   int hash_kind() const { return hash_kind_; }
@@ -147,7 +178,9 @@ class Engine {
   uint32_t cs_;
   cudaStream_t stream_ = nullptr;
   bool allocated_ = false;
-  bool fresh_ = false, baseline_path_ = false, timed_ = true, order_after_legacy_ = false;
+  bool fresh_ = false, baseline_path_ = false, timed_ = true, order_after_legacy_ = false, spilled_ = false;
+  cudaMemPool_t pool_ = nullptr;
+  template <class F> void for_each_buf(F f);
   double max_load_ = 0.75;
   LeafTune leaf_tune_{};
   uint32_t N_ = 0, M_ = 0;
@@ -174,6 +207,8 @@ class Engine {
   cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   RestartScratch* rs_ = nullptr;  // restart buffers, created on first use
   std::vector<void*> retired_;    // replaced map tables awaiting cudaFree
+  uint64_t spill_nd_ = 0, spill_cap_ = 0;
+  bool restart_raw_ = false;
 };
 
 }  // namespace mtc

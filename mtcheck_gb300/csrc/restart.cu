@@ -602,22 +602,50 @@ struct RestartScratch {
 
 void destroy_restart_scratch(RestartScratch* r) { delete r; }
 
+static void set_scratch_pool(RestartScratch* r, cudaMemPool_t pool) {
+  r->di.pool = pool;
+  for (auto* b : {&r->fo_node, &r->fo_seg, &r->fo_clen, &r->sh_node, &r->sh_prev, &r->sh_tree, &r->sh_seg, &r->rrs,
+                  &r->fo_at, &r->dm_tab, &r->rm_tab, &r->dm_mask, &r->rm_mask})
+    b->pool = pool;
+  for (auto* b : {&r->fo_excl, &r->sh_off, &r->sh_excl, &r->nl, &r->res, &r->nl_rank, &r->cp_rank, &r->dm_excl,
+                  &r->rm_excl, &r->tot, &r->scan, &r->scan_total})
+    b->pool = pool;
+}
+
 int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint8_t*>& dev_diffs,
                     const std::vector<uint64_t>& lens, const std::vector<HeaderHost>& headers, uint32_t id) {
+  if (int rc = order_inputs()) return rc;
+  int rc = restart_enqueue(dev_out, len, dev_diffs, lens, headers, id);
+  if (rc) return rc;
+  MTC_CUDA_R(cudaStreamSynchronize(stream_));
+  return restart_complete();
+}
+
+int Engine::restart_complete() {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+  restart_timers[1] = ms * 1e-3;
+  if (restart_raw_) return ST_OK;
+  const uint32_t herr = err_host_[0];
+  last_device_error = herr;
+  if (herr & DERR_RANGE) return fail(ST_ECORRUPT, "restart metadata out of range");
+  if (herr & DERR_INTERIOR) return fail(ST_ENOTSUP, "restart provenance names an interior node");
+  return ST_OK;
+}
+
+int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<const uint8_t*>& dev_diffs,
+                            const std::vector<uint64_t>& lens, const std::vector<HeaderHost>& headers, uint32_t id) {
   cudaStream_t s = stream_;
   if (id >= dev_diffs.size()) return fail(ST_EINVAL, "checkpoint id outside the chain");
-  if (int rc = order_inputs()) return rc;
+  if (spilled_) return fail(ST_EINVAL, "state spilled to host: restore it first");
   cudaEvent_t e0 = ev_[0], e1 = ev_[1];
   cudaEventRecord(e0, s);
+  restart_raw_ = mode_ == MODE_FULL;
   if (mode_ == MODE_FULL) {
     // FullDeduplicator::restart copies the raw checkpoint (src/full_approach.cpp:122-141)
     if (lens[id] != len) return fail(ST_EINVAL, "output length differs from the checkpoint");
     MTC_CUDA_R(cudaMemcpyAsync(dev_out, dev_diffs[id], len, cudaMemcpyDeviceToDevice, s));
     cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    restart_timers[1] = ms * 1e-3;
     return ST_OK;
   }
   const int approach = mode_ == MODE_LIST ? APPROACH_LIST : mode_ == MODE_BASIC ? APPROACH_BASIC : APPROACH_TREE;
@@ -675,7 +703,10 @@ int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint
   }
   const uint32_t W = (nsteps + 31) / 32 ? (nsteps + 31) / 32 : 1;
   const uint32_t K = approach == APPROACH_TREE ? N + 1 : N;
-  if (!rs_) rs_ = new RestartScratch();
+  if (!rs_) {
+    rs_ = new RestartScratch();
+    if (pool_) set_scratch_pool(rs_, pool_);
+  }
   RestartScratch& R = *rs_;
   MTC_CUDA_R(R.di.ensure(di.size(), s));
   MTC_CUDA_R(cudaMemcpyAsync(R.di.p, di.data(), sizeof(DiffInfo) * di.size(), cudaMemcpyHostToDevice, s));
@@ -775,16 +806,7 @@ int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint
   gather_kernel<<<num_sms() * 16, 256, 0, s>>>(a);
   note_launch();
   cudaEventRecord(e1, s);
-  uint32_t herr = 0;
   MTC_CUDA_R(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  MTC_CUDA_R(cudaStreamSynchronize(s));
-  herr = err_host_[0];
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
-  restart_timers[1] = ms * 1e-3;
-  last_device_error = herr;
-  if (herr & DERR_RANGE) return fail(ST_ECORRUPT, "restart metadata out of range");
-  if (herr & DERR_INTERIOR) return fail(ST_ENOTSUP, "restart provenance names an interior node");
   return ST_OK;
 }
 

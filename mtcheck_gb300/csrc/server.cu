@@ -1,0 +1,618 @@
+// server.cu -- the request-serving loop (see server.hpp).
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <limits>
+#include <set>
+
+#include "server.hpp"
+
+namespace mtc {
+
+// ---------------------------------------------------------------------------
+// PinnedArena
+// ---------------------------------------------------------------------------
+PinnedArena::~PinnedArena() {
+  for (uint8_t* p : all_) cudaFreeHost(p);
+}
+
+uint64_t PinnedArena::cls(uint64_t n) {
+  uint64_t c = 64ull << 10;
+  while (c < n) c <<= 1;
+  return c;
+}
+
+uint8_t* PinnedArena::alloc(uint64_t n) {
+  const uint64_t c = cls(n);
+  auto& fl = free_[c];
+  if (!fl.empty()) {
+    uint8_t* p = fl.back();
+    fl.pop_back();
+    return p;
+  }
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, c, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  all_.push_back(static_cast<uint8_t*>(p));
+  reserved_ += c;
+  return static_cast<uint8_t*>(p);
+}
+
+void PinnedArena::free(uint8_t* p, uint64_t n) {
+  if (p) free_[cls(n)].push_back(p);
+}
+
+// ---------------------------------------------------------------------------
+// Server
+// ---------------------------------------------------------------------------
+double Server::now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+Server::Server(const ServerOptions& o) : opt_(o) {
+  if (opt_.max_inflight == 0) opt_.max_inflight = 1;
+  if (opt_.id_headroom == 0) opt_.id_headroom = 1;
+  cudaGetDevice(&device_);
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device_;
+  if (cudaMemPoolCreate(&pool_, &props) == cudaSuccess) {
+    // keep freed memory in the pool: returning it to the driver would
+    // synchronise at every stream synchronisation point
+    uint64_t keep = std::numeric_limits<uint64_t>::max();
+    cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep);
+  } else {
+    pool_ = nullptr;
+    cudaGetLastError();
+  }
+  thread_ = std::thread([this] { worker(); });
+}
+
+Server::~Server() {
+  {
+    std::lock_guard<std::mutex> g(mu_);
+    stop_ = true;
+  }
+  cv_work_.notify_all();
+  if (thread_.joinable()) thread_.join();
+  for (auto& pp : procs_) {
+    Proc& p = *pp;
+    cudaStreamSynchronize(p.s);
+    if (p.exec) cudaGraphExecDestroy(p.exec);
+    for (auto& a : p.chain)
+      if (a.dev) cudaFreeAsync(a.dev, p.s);
+    p.eng.reset();  // stream-ordered frees on p.s
+    cudaStreamSynchronize(p.s);
+    cudaStreamDestroy(p.s);
+  }
+  procs_.clear();
+  for (auto e : events_) cudaEventDestroy(e);
+  cudaDeviceSynchronize();
+  if (pool_) cudaMemPoolDestroy(pool_);
+}
+
+void Server::set_error(const std::string& e) {
+  std::lock_guard<std::mutex> g(mu_);
+  err_ = e;
+}
+
+std::string Server::error() {
+  std::lock_guard<std::mutex> g(mu_);
+  return err_;
+}
+
+cudaEvent_t Server::get_event() {
+  // caller holds mu_
+  if (!events_.empty()) {
+    cudaEvent_t e = events_.back();
+    events_.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  return e;
+}
+
+void Server::put_event(cudaEvent_t e) {
+  std::lock_guard<std::mutex> g(mu_);
+  events_.push_back(e);
+}
+
+int Server::add_process(int mode, int hash_kind, uint32_t chunk_size, uint32_t* pid) {
+  if (!pool_) {
+    set_error("no stream-ordered memory pool on this device");
+    return ST_ENOTSUP;
+  }
+  auto p = std::make_unique<Proc>();
+  if (cudaStreamCreateWithFlags(&p->s, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cannot create a stream");
+    return ST_ECUDA;
+  }
+  p->eng = std::make_unique<Engine>(mode, hash_kind, chunk_size);
+  p->eng->set_stream(p->s);
+  p->eng->set_pool(pool_);
+  std::lock_guard<std::mutex> g(mu_);
+  procs_.push_back(std::move(p));
+  *pid = (uint32_t)procs_.size() - 1;
+  return ST_OK;
+}
+
+int Server::submit_checkpoint(uint32_t pid, const uint8_t* data, uint64_t len, bool make_baseline, uint64_t* ticket) {
+  if (!data || len == 0) {
+    set_error("empty buffer");
+    return ST_EINVAL;
+  }
+  std::unique_lock<std::mutex> g(mu_);
+  if (pid >= procs_.size()) {
+    err_ = "unknown process";
+    return ST_EINVAL;
+  }
+  if (stop_) return ST_EINVAL;
+  Req r{next_ticket_++, pid, REQ_CHECKPOINT, data, nullptr, len, make_baseline, 0, now_ms(), get_event()};
+  // the buffer is complete once the work already on the legacy default
+  // stream (where the caller wrote it) has run
+  cudaEventRecord(r.ready, cudaStreamLegacy);
+  inbox_.push_back(r);
+  outstanding_++;
+  st_.submitted++;
+  if (ticket) *ticket = r.ticket;
+  g.unlock();
+  cv_work_.notify_one();
+  return ST_OK;
+}
+
+int Server::submit_restart(uint32_t pid, uint32_t chkpt_id, uint8_t* out, uint64_t len, uint64_t* ticket) {
+  if (!out || len == 0) {
+    set_error("empty output buffer");
+    return ST_EINVAL;
+  }
+  std::unique_lock<std::mutex> g(mu_);
+  if (pid >= procs_.size()) {
+    err_ = "unknown process";
+    return ST_EINVAL;
+  }
+  if (stop_) return ST_EINVAL;
+  Req r{next_ticket_++, pid, REQ_RESTART, nullptr, out, len, false, chkpt_id, now_ms(), get_event()};
+  cudaEventRecord(r.ready, cudaStreamLegacy);
+  inbox_.push_back(r);
+  outstanding_++;
+  st_.submitted++;
+  if (ticket) *ticket = r.ticket;
+  g.unlock();
+  cv_work_.notify_one();
+  return ST_OK;
+}
+
+uint32_t Server::poll(Completion* out, uint32_t max, double wait_ms) {
+  std::unique_lock<std::mutex> g(mu_);
+  if (done_.empty() && wait_ms > 0)
+    cv_done_.wait_for(g, std::chrono::microseconds((int64_t)(wait_ms * 1000)), [&] { return !done_.empty(); });
+  uint32_t n = 0;
+  while (n < max && !done_.empty()) {
+    out[n++] = done_.front();
+    done_.pop_front();
+  }
+  return n;
+}
+
+bool Server::drain(double timeout_ms) {
+  std::unique_lock<std::mutex> g(mu_);
+  return cv_done_.wait_for(g, std::chrono::microseconds((int64_t)(timeout_ms * 1000)),
+                           [&] { return outstanding_ == 0; });
+}
+
+int Server::chain_length(uint32_t pid, uint32_t* n) {
+  std::lock_guard<std::mutex> g(mu_);
+  if (pid >= procs_.size()) return ST_EINVAL;
+  *n = (uint32_t)procs_[pid]->chain.size();
+  return ST_OK;
+}
+
+int Server::copy_diff(uint32_t pid, uint32_t id, void* host, uint64_t cap, uint64_t* len) {
+  std::lock_guard<std::mutex> g(mu_);
+  if (pid >= procs_.size()) return ST_EINVAL;
+  Proc& p = *procs_[pid];
+  if (id >= p.chain.size()) return ST_EINVAL;
+  Archived& a = p.chain[id];
+  if (len) *len = a.len;
+  if (!host) return ST_OK;
+  if (cap < a.len) return ST_EINVAL;
+  // the archive copy and any spill of this entry run on the process's stream
+  if (cudaStreamSynchronize(p.s) != cudaSuccess) return ST_ECUDA;
+  if (a.dev) {
+    if (cudaMemcpy(host, a.dev, a.len, cudaMemcpyDeviceToHost) != cudaSuccess) return ST_ECUDA;
+  } else {
+    std::memcpy(host, a.host, a.len);
+  }
+  return ST_OK;
+}
+
+ServerStats Server::stats() {
+  std::lock_guard<std::mutex> g(mu_);
+  ServerStats s = st_;
+  s.pinned_reserved = arena_.reserved();
+  return s;
+}
+
+void Server::push_completion(const Completion& c) {
+  {
+    std::lock_guard<std::mutex> g(mu_);
+    done_.push_back(c);
+    outstanding_--;
+    st_.completed++;
+    if (c.status != ST_OK) st_.failed++;
+  }
+  cv_done_.notify_all();
+}
+
+// ---- memory accounting -----------------------------------------------------
+static uint64_t pow2_at_least(uint64_t v) {
+  uint64_t c = 1;
+  while (c < v) c <<= 1;
+  return c;
+}
+
+// Device bytes of an engine's state for a buffer of `len` bytes: digests,
+// labels, lists, digest map at load <= 3/4, staging for the largest diff.
+static uint64_t estimate_state(int mode, uint64_t len, uint32_t cs) {
+  const uint64_t N = (len + cs - 1) / cs, M = 2 * N;
+  if (mode == MODE_FULL) return len + 64;
+  const bool tree = mode == MODE_TREE || mode == MODE_TREE_LOW_OFFSET || mode == MODE_TREE_LOW_OFFSET_REF;
+  const uint64_t nd = tree ? M : N;
+  const uint64_t map = mode == MODE_BASIC ? 0 : pow2_at_least(nd * 4 / 3 + 1) * 2 * sizeof(MapSlot);
+  return nd * (sizeof(Digest) + 2) + N * 64 + map + (N + 1) * (cs + 12) + (1u << 20);
+}
+
+uint64_t Server::need_bytes(const Req& r, const Proc& p) const {
+  const Engine& e = *p.eng;
+  const uint64_t N = (r.len + e.chunk_size() - 1) / e.chunk_size();
+  uint64_t need = 0;
+  if (e.spilled()) need += p.spill_len + estimate_state(e.mode(), r.len, e.chunk_size()) / 2;
+  if (r.kind == REQ_CHECKPOINT) {
+    if (p.state_dev == 0 && !e.spilled()) need += estimate_state(e.mode(), r.len, e.chunk_size());
+    need += 32 + 12 * (N + 1) + (N + 1) * e.chunk_size();  // worst-case archived diff
+  } else {
+    for (uint32_t k = 0; k <= r.chkpt_id && k < p.chain.size(); k++)
+      if (!p.chain[k].dev) need += p.chain[k].len;  // staged back for the restart
+    need += N * 96 + (uint64_t)(r.chkpt_id + 1) * (N + 1) * 8;  // restart scratch
+  }
+  return need;
+}
+
+void Server::refresh_state_bytes(Proc& p) {
+  p.state_dev = p.eng->spilled() ? 0 : p.eng->device_bytes();
+}
+
+void Server::spill_diff(Proc& p, Archived& a) {
+  uint8_t* h = arena_.alloc(a.len);
+  if (!h) return;
+  cudaMemcpyAsync(h, a.dev, a.len, cudaMemcpyDeviceToHost, p.s);
+  cudaFreeAsync(a.dev, p.s);
+  std::lock_guard<std::mutex> g(mu_);
+  a.host = h;
+  a.dev = nullptr;
+  chain_dev_ -= a.len;
+  st_.spilled_diffs++;
+  st_.spilled_bytes += a.len;
+}
+
+void Server::spill_state(Proc& p) {
+  const uint64_t n = p.eng->spill_bytes();
+  uint8_t* h = arena_.alloc(n);
+  if (!h) return;
+  if (p.eng->spill_to_host(h) != ST_OK) {
+    arena_.free(h, n);
+    return;
+  }
+  p.spill = h;
+  p.spill_len = n;
+  if (p.exec) {
+    cudaGraphExecDestroy(p.exec);
+    p.exec = nullptr;
+  }
+  refresh_state_bytes(p);
+  std::lock_guard<std::mutex> g(mu_);
+  st_.spilled_states++;
+  st_.spilled_bytes += n;
+}
+
+int Server::restore_state(Proc& p) {
+  int rc = p.eng->restore_from_host(p.spill);
+  if (rc) return rc;
+  // the pinned copy is read by the stream; it returns to the arena when the
+  // request that restored it completes
+  refresh_state_bytes(p);
+  std::lock_guard<std::mutex> g(mu_);
+  st_.restored_states++;
+  return ST_OK;
+}
+
+bool Server::make_room(uint64_t need, uint32_t except) {
+  auto used = [&] {
+    uint64_t u = chain_dev_;
+    for (Proc* pp : view_) u += pp->state_dev;
+    return u;
+  };
+  while (used() + need > opt_.hbm_budget) {
+    // 1. the oldest archived checkpoint of the least recently used idle process
+    Proc* victim = nullptr;
+    for (uint32_t i = 0; i < view_.size(); i++) {
+      Proc& p = *view_[i];
+      if (p.busy || i == except) continue;
+      bool has = false;
+      for (auto& a : p.chain)
+        if (a.dev) { has = true; break; }
+      if (has && (!victim || p.lru < victim->lru)) victim = &p;
+    }
+    if (victim) {
+      for (auto& a : victim->chain)
+        if (a.dev) {
+          const uint64_t before = chain_dev_;
+          spill_diff(*victim, a);
+          if (chain_dev_ == before) return false;  // no pinned memory left
+          break;
+        }
+      continue;
+    }
+    // 2. the digest state of the least recently used idle process
+    for (uint32_t i = 0; i < view_.size(); i++) {
+      Proc& p = *view_[i];
+      if (p.busy || i == except || p.state_dev == 0 || p.eng->mode() == MODE_FULL) continue;
+      if (!victim || p.lru < victim->lru) victim = &p;
+    }
+    if (!victim) return false;
+    const uint64_t before = victim->state_dev;
+    spill_state(*victim);
+    if (victim->state_dev == before) return false;
+  }
+  return true;
+}
+
+// ---- request execution -------------------------------------------------------
+int Server::start_checkpoint(Req& r, Proc& p) {
+  Engine& e = *p.eng;
+  if (e.spilled()) {
+    int rc = restore_state(p);
+    if (rc) return rc;
+  }
+  if (cudaStreamWaitEvent(p.s, r.ready, 0) != cudaSuccess) return ST_ECUDA;
+  int rc = e.prepare(r.data, r.len, r.make_baseline, opt_.id_headroom);
+  if (rc) return rc;
+  const bool graph = opt_.use_graph && !e.fresh();
+  if (graph) {
+    const uint64_t sig = e.signature(r.data, r.len);
+    if (!p.exec || p.sig != sig) {
+      if (p.exec) cudaGraphExecDestroy(p.exec);
+      p.exec = nullptr;
+      if (cudaStreamBeginCapture(p.s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return ST_ECUDA;
+      rc = e.enqueue(r.data, r.len, false);
+      cudaGraph_t g = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(p.s, &g);
+      if (rc || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : ST_ECUDA;
+      }
+      ce = cudaGraphInstantiate(&p.exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        p.exec = nullptr;
+        return ST_ECUDA;
+      }
+      p.sig = sig;
+      std::lock_guard<std::mutex> lk(mu_);
+      st_.graph_captures++;
+    }
+    e.stage_params();
+    if (cudaGraphLaunch(p.exec, p.s) != cudaSuccess) return ST_ECUDA;
+    std::lock_guard<std::mutex> lk(mu_);
+    st_.graph_replays++;
+  } else {
+    if (e.mode() != MODE_FULL) e.stage_params();
+    rc = e.enqueue(r.data, r.len, false);
+    if (rc) return rc;
+  }
+  return ST_OK;
+}
+
+int Server::start_restart(Req& r, Proc& p, std::vector<uint8_t*>* temps) {
+  Engine& e = *p.eng;
+  if (r.chkpt_id >= p.chain.size()) return ST_EINVAL;
+  if (e.spilled()) {
+    int rc = restore_state(p);
+    if (rc) return rc;
+  }
+  const size_t n = p.chain.size();
+  std::vector<const uint8_t*> ptrs(n, nullptr);
+  std::vector<uint64_t> lens(n, 0);
+  std::vector<HeaderHost> hdrs(n);
+  for (size_t k = 0; k < n; k++) {
+    Archived& a = p.chain[k];
+    lens[k] = a.len;
+    hdrs[k] = a.hdr;
+    if (k > r.chkpt_id) continue;
+    if (a.dev) {
+      ptrs[k] = a.dev;
+    } else {
+      // a spilled checkpoint comes back for this restart only
+      uint8_t* t = nullptr;
+      if (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&t), a.len ? a.len : 1, pool_, p.s) != cudaSuccess)
+        return ST_ENOMEM;
+      cudaMemcpyAsync(t, a.host, a.len, cudaMemcpyHostToDevice, p.s);
+      temps->push_back(t);
+      ptrs[k] = t;
+      std::lock_guard<std::mutex> lk(mu_);
+      st_.staged_diffs++;
+    }
+  }
+  if (cudaStreamWaitEvent(p.s, r.ready, 0) != cudaSuccess) return ST_ECUDA;
+  int rc = e.restart_enqueue(r.out, r.len, ptrs, lens, hdrs, r.chkpt_id);
+  for (uint8_t* t : *temps) cudaFreeAsync(t, p.s);  // after the restart, in stream order
+  return rc;
+}
+
+bool Server::try_start(Req& r) {
+  Proc& p = *view_[r.pid];
+  const uint64_t need = need_bytes(r, p);
+  uint64_t used = chain_dev_;
+  for (Proc* pp : view_) used += pp->state_dev;
+  if (used + need > opt_.hbm_budget && !make_room(need, r.pid)) {
+    if (flights_.empty()) {
+      // nothing in flight will free memory: the request cannot fit
+      Completion c{r.ticket, r.pid, r.kind, ST_ENOMEM, 0, 0, r.t_submit, now_ms(), now_ms()};
+      put_event(r.ready);
+      set_error("request does not fit the HBM budget");
+      push_completion(c);
+      return true;
+    }
+    std::lock_guard<std::mutex> g(mu_);
+    st_.deferred_admissions++;
+    return false;
+  }
+  Flight f{r, nullptr, now_ms(), 0, {}};
+  p.busy = true;
+  p.lru = ++tick_;
+  // a failed start still completes in stream order, after what it issued
+  f.start_rc = r.kind == REQ_CHECKPOINT ? start_checkpoint(f.r, p) : start_restart(f.r, p, &f.temps);
+  {
+    std::lock_guard<std::mutex> g(mu_);
+    f.done = get_event();
+  }
+  cudaEventRecord(f.done, p.s);
+  flights_.push_back(f);
+  std::lock_guard<std::mutex> g(mu_);
+  st_.inflight_peak = std::max<uint32_t>(st_.inflight_peak, (uint32_t)flights_.size());
+  uint64_t u = chain_dev_;
+  for (Proc* pp : view_) u += pp->state_dev;
+  st_.hbm_used = u;
+  st_.hbm_peak = std::max(st_.hbm_peak, u);
+  return true;
+}
+
+void Server::finish(Flight& f) {
+  Proc& p = *view_[f.r.pid];
+  Engine& e = *p.eng;
+  Completion c{f.r.ticket, f.r.pid, f.r.kind, ST_OK, 0, 0, f.r.t_submit, f.t_admit, 0};
+  if (f.start_rc) {
+    c.status = f.start_rc;
+    set_error(e.last_error);
+  } else if (f.r.kind == REQ_CHECKPOINT) {
+    HeaderHost h{};
+    int rc = e.complete(f.r.len, &h);
+    e.release_retired();
+    c.status = rc;
+    if (rc == ST_OK) {
+      const uint64_t n = e.diff_len();
+      Archived a;
+      a.len = n;
+      a.hdr = h;
+      if (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&a.dev), n ? n : 1, pool_, p.s) == cudaSuccess) {
+        cudaMemcpyAsync(a.dev, e.diff_device(), n, cudaMemcpyDeviceToDevice, p.s);
+      } else {
+        // no device memory for the archive: keep it in pinned host memory
+        cudaGetLastError();
+        a.dev = nullptr;
+        a.host = arena_.alloc(n);
+        if (a.host) cudaMemcpyAsync(a.host, e.diff_device(), n, cudaMemcpyDeviceToHost, p.s);
+        else c.status = ST_ENOMEM;
+      }
+      if (c.status == ST_OK) {
+        c.chkpt_id = (uint32_t)p.chain.size();
+        c.diff_len = n;
+        std::lock_guard<std::mutex> g(mu_);
+        p.chain.push_back(a);
+        if (a.dev) chain_dev_ += n;
+        st_.checkpoints++;
+        st_.bytes_checkpointed += f.r.len;
+      }
+      e.current_id += 1;  // checkpoint(data, len, diff_h, make_baseline) advances
+    } else {
+      set_error(e.last_error);
+    }
+  } else {
+    int rc = e.restart_complete();
+    c.status = rc;
+    c.chkpt_id = f.r.chkpt_id;
+    if (rc == ST_OK) {
+      std::lock_guard<std::mutex> g(mu_);
+      st_.restarts++;
+      st_.bytes_restarted += f.r.len;
+    } else {
+      set_error(e.last_error);
+    }
+  }
+  if (p.spill && !e.spilled()) {  // the restore's pinned copy has been read
+    arena_.free(p.spill, p.spill_len);
+    p.spill = nullptr;
+    p.spill_len = 0;
+  }
+  refresh_state_bytes(p);
+  p.busy = false;
+  c.t_done_ms = now_ms();
+  put_event(f.r.ready);
+  put_event(f.done);
+  push_completion(c);
+}
+
+void Server::worker() {
+  cudaSetDevice(device_);
+  while (true) {
+    {
+      std::unique_lock<std::mutex> g(mu_);
+      if (stop_ && inbox_.empty() && pending_.empty() && flights_.empty()) break;
+      if (view_.size() != procs_.size()) {
+        view_.clear();
+        for (auto& pp : procs_) view_.push_back(pp.get());
+      }
+      while (!inbox_.empty()) {
+        pending_.push_back(inbox_.front());
+        inbox_.pop_front();
+      }
+    }
+    bool progress = false;
+    // 1. completions
+    for (size_t i = 0; i < flights_.size();) {
+      cudaError_t q = cudaEventQuery(flights_[i].done);
+      if (q == cudaErrorNotReady) {
+        i++;
+        continue;
+      }
+      if (q != cudaSuccess) {
+        flights_[i].start_rc = ST_ECUDA;
+        set_error(std::string("device error: ") + cudaGetErrorString(q));
+      }
+      Flight f = flights_[i];
+      flights_.erase(flights_.begin() + (long)i);
+      finish(f);
+      progress = true;
+    }
+    // 2. admission in submission order; one request per process at a time
+    std::set<uint32_t> seen;
+    for (auto it = pending_.begin(); it != pending_.end() && flights_.size() < opt_.max_inflight;) {
+      const uint32_t pid = it->pid;
+      if (seen.count(pid) || view_[pid]->busy) {
+        seen.insert(pid);
+        ++it;
+        continue;
+      }
+      seen.insert(pid);
+      if (try_start(*it)) {
+        it = pending_.erase(it);
+        progress = true;
+      } else {
+        ++it;
+      }
+    }
+    if (!progress) {
+      std::unique_lock<std::mutex> g(mu_);
+      if (inbox_.empty() && !stop_)
+        cv_work_.wait_for(g, flights_.empty() ? std::chrono::microseconds(2000) : std::chrono::microseconds(20));
+    }
+  }
+}
+
+}  // namespace mtc

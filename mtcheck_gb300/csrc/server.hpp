@@ -1,0 +1,176 @@
+// server.hpp -- a request-serving loop over many deduplicators.
+//
+// Clients (simulated application processes) submit checkpoint and restart
+// requests at any time from any thread.  One worker thread owns the GPU work:
+//   * continuous admission: a request is started as soon as its process has
+//     no other request on the GPU, an in-flight slot is free and its memory
+//     fits the HBM budget; requests of different processes overlap on the
+//     device (one CUDA stream per process), requests of one process run in
+//     submission order;
+//   * each process keeps its chunk digests (Merkle tree or hash list) and
+//     digest map resident in HBM, plus the chain of its incremental
+//     checkpoints for restarts;
+//   * when the budget is exceeded the least recently used idle processes are
+//     spilled to pinned host memory: first their archived checkpoints, then
+//     their digest state; a spilled process is restored on its next request;
+//   * incremental checkpoints of a process replay a per-process CUDA graph.
+// Every result is the one a lone deduplicator gives for the same sequence of
+// buffers: the launch sequence per process is the same, only its scheduling
+// differs.
+#pragma once
+#include <atomic>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace mtc {
+
+struct ServerOptions {
+  uint64_t hbm_budget = 120ull * 1000 * 1000 * 1000;
+  uint32_t max_inflight = 64;
+  uint32_t id_headroom = 64;
+  // Per-process CUDA graphs for incremental checkpoints.  The worker
+  // captures one when a process's buffers move; during that capture a
+  // device-wide synchronisation by any thread of the application fails.
+  int use_graph = 0;
+};
+
+enum : int { REQ_CHECKPOINT = 0, REQ_RESTART = 1 };
+
+struct Completion {
+  uint64_t ticket;
+  uint32_t pid;
+  int32_t kind;
+  int32_t status;
+  uint32_t chkpt_id;
+  uint64_t diff_len;
+  double t_submit_ms, t_admit_ms, t_done_ms;
+};
+
+struct ServerStats {
+  uint64_t submitted = 0, completed = 0, failed = 0, checkpoints = 0, restarts = 0;
+  uint64_t bytes_checkpointed = 0, bytes_restarted = 0;
+  uint64_t spilled_diffs = 0, spilled_states = 0, restored_states = 0, staged_diffs = 0;
+  uint64_t spilled_bytes = 0;
+  uint64_t graph_captures = 0, graph_replays = 0;
+  uint64_t hbm_used = 0, hbm_peak = 0, pinned_reserved = 0;
+  uint64_t deferred_admissions = 0;  // admission attempts refused for memory
+  uint32_t inflight_peak = 0;
+};
+
+// Pinned host memory in power-of-two blocks, reused, freed at destruction
+// (cudaFreeHost would wait for the whole device).
+class PinnedArena {
+ public:
+  ~PinnedArena();
+  uint8_t* alloc(uint64_t n);
+  void free(uint8_t* p, uint64_t n);
+  uint64_t reserved() const { return reserved_; }
+
+ private:
+  static uint64_t cls(uint64_t n);
+  std::map<uint64_t, std::vector<uint8_t*>> free_;
+  std::vector<uint8_t*> all_;
+  uint64_t reserved_ = 0;
+};
+
+class Server {
+ public:
+  explicit Server(const ServerOptions& o);
+  ~Server();
+  int add_process(int mode, int hash_kind, uint32_t chunk_size, uint32_t* pid);
+  int submit_checkpoint(uint32_t pid, const uint8_t* data, uint64_t len, bool make_baseline, uint64_t* ticket);
+  int submit_restart(uint32_t pid, uint32_t chkpt_id, uint8_t* out, uint64_t len, uint64_t* ticket);
+  // Up to `max` completions; waits up to wait_ms for the first one.
+  uint32_t poll(Completion* out, uint32_t max, double wait_ms);
+  // Wait until every submitted request has completed (false on timeout).
+  bool drain(double timeout_ms);
+  int chain_length(uint32_t pid, uint32_t* n);
+  int copy_diff(uint32_t pid, uint32_t chkpt_id, void* host, uint64_t cap, uint64_t* len);
+  ServerStats stats();
+  std::string error();
+  static double now_ms();
+
+ private:
+  struct Archived {
+    uint8_t* dev = nullptr;   // pool allocation, or null when spilled
+    uint8_t* host = nullptr;  // pinned copy when spilled
+    uint64_t len = 0;
+    HeaderHost hdr{};
+  };
+  struct Proc {
+    std::unique_ptr<Engine> eng;
+    cudaStream_t s = nullptr;
+    std::vector<Archived> chain;
+    bool busy = false;
+    uint64_t lru = 0;
+    uint64_t state_dev = 0;        // device bytes of the engine when resident
+    uint8_t* spill = nullptr;      // pinned copy of the digest state
+    uint64_t spill_len = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t sig = 0;
+  };
+  struct Req {
+    uint64_t ticket;
+    uint32_t pid;
+    int kind;
+    const uint8_t* data;
+    uint8_t* out;
+    uint64_t len;
+    bool make_baseline;
+    uint32_t chkpt_id;
+    double t_submit;
+    cudaEvent_t ready;
+  };
+  struct Flight {
+    Req r;
+    cudaEvent_t done;
+    double t_admit;
+    int start_rc;                 // nonzero: the start failed part-way
+    std::vector<uint8_t*> temps;  // staged spilled diffs of a restart
+  };
+
+  void worker();
+  bool try_start(Req& r);
+  int start_checkpoint(Req& r, Proc& p);
+  int start_restart(Req& r, Proc& p, std::vector<uint8_t*>* temps);
+  void finish(Flight& f);
+  uint64_t need_bytes(const Req& r, const Proc& p) const;
+  bool make_room(uint64_t need, uint32_t except);
+  void spill_diff(Proc& p, Archived& a);
+  void spill_state(Proc& p);
+  int restore_state(Proc& p);
+  void refresh_state_bytes(Proc& p);
+  cudaEvent_t get_event();
+  void put_event(cudaEvent_t e);
+  void push_completion(const Completion& c);
+  void set_error(const std::string& e);
+
+  ServerOptions opt_;
+  int device_ = 0;
+  cudaMemPool_t pool_ = nullptr;
+  PinnedArena arena_;
+  std::vector<std::unique_ptr<Proc>> procs_;  // owned; grows under mu_
+  std::vector<Proc*> view_;                   // the worker's copy of procs_
+  std::deque<Req> inbox_, pending_;
+  std::vector<Flight> flights_;
+  std::deque<Completion> done_;
+  std::vector<cudaEvent_t> events_;
+  std::mutex mu_;                  // inbox, completions, events, procs vector, chains
+  std::condition_variable cv_work_, cv_done_;
+  std::thread thread_;
+  std::atomic<bool> stop_{false};
+  uint64_t next_ticket_ = 1, outstanding_ = 0, tick_ = 0, chain_dev_ = 0;
+  ServerStats st_;
+  std::string err_;
+};
+
+}  // namespace mtc
