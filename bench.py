@@ -26,6 +26,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# more hardware work queues than the default 8, so that the kernels of many
+# concurrent streams (batch members, served processes) are not funnelled into
+# false dependencies; a per-process runtime setting, read at context creation
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "Dedup & restart GB/s on 1 GB300, % HBM roofline; batched vs per-call; p99 ms"
 GIB = 1 << 30
@@ -52,6 +56,15 @@ def parse():
     p.add_argument("--batch-steps", type=int, default=5)
     p.add_argument("--batch-no-tune", action="store_true")
     p.add_argument("--only-batch", action="store_true")
+    p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--only-serve", action="store_true")
+    p.add_argument("--serve-procs", type=int, default=256)
+    p.add_argument("--serve-rate", type=float, default=2000.0)
+    p.add_argument("--serve-seconds", type=float, default=4.0)
+    p.add_argument("--serve-budget-gb", type=float, default=120.0)
+    p.add_argument("--serve-inflight", type=int, default=64)
+    p.add_argument("--serve-verify-procs", type=int, default=4)
+    p.add_argument("--serve-pinned-gb", type=float, default=32.0)
     return p.parse_args()
 
 
@@ -396,6 +409,174 @@ def batch_bench(torch, mc, dev, a):
     return res
 
 
+def _digest2(mc, kind, buf):
+    """Digest of the 64 KiB-chunk digests of a device buffer (16 bytes, device)."""
+    d1 = mc.hash_chunks(kind, buf, 64 << 10)
+    return mc.hash_chunks(kind, d1, d1.numel())
+
+
+def serve_bench(torch, mc, dev, a):
+    """256 processes with buffers of 2^k bytes, k uniform in 22..28 (4-256 MiB),
+    128 B chunks, Murmur3, tree approach.  Requests arrive as a Poisson stream
+    at --serve-rate per second for --serve-seconds; 5% are restarts of a random
+    earlier checkpoint of the process; a checkpoint first applies one step of
+    the 4 GiB update pattern (change rate 0.5-5%).  A process has at most one
+    request on the server; later arrivals for it wait, and latency runs from
+    the arrival time to completion.  The update steps are drawn before the
+    stream starts (DeviceUpdates) so that the driver keeps up with the rate.
+    Every restart is verified against a digest of the state it restores; a
+    sample of processes is replayed alone through lone handles and compared
+    byte for byte with the served chain."""
+    from collections import deque
+    import numpy as np
+    from mtcheck_gb300 import workloads
+    mix = workloads.serve_mix(count=a.serve_procs)
+    P = len(mix)
+    kind = mc.MURMUR3
+    srv = mc.Server(hbm_budget=int(a.serve_budget_gb * 1e9), max_inflight=a.serve_inflight, use_graph=True,
+                    reserve_hbm=True, pinned_reserve=int(a.serve_pinned_gb * (1 << 30)))
+    pids = [srv.add_process(mc.TREE, kind, m["chunk_size"]) for m in mix]
+    assert pids == list(range(P))
+    zr = [(m["nbytes"] // 4, m["nbytes"] // 4 + m["nbytes"] // 8) for m in mix]
+    bufs = [workloads.init_device(torch.empty(m["nbytes"], dtype=torch.uint8, device=dev), m["seed"], zr[i])
+            for i, m in enumerate(mix)]
+    maxn = max(m["nbytes"] for m in mix)
+    outs = [torch.empty(maxn, dtype=torch.uint8, device=dev) for _ in range(8)]
+    free_outs = list(range(len(outs)))
+    rng = np.random.default_rng(11)
+    rates = [float(rng.uniform(*m["rate"])) for m in mix]
+    plans = [workloads.DeviceUpdates(bufs[i], m["chunk_size"], rates[i], m["seed"], zero_range=zr[i])
+             for i, m in enumerate(mix)]
+    # baselines (not timed)
+    t_base = time.perf_counter()
+    for i, pid in enumerate(pids):
+        srv.submit_checkpoint(pid, bufs[i], make_baseline=True)
+    srv.drain()
+    base = srv.poll(0)
+    while len(base) < P:
+        base += srv.poll(100)
+    assert all(c["status"] == 0 for c in base)
+    base_s = time.perf_counter() - t_base
+    step = [1] * P
+    # the request stream
+    n_req = int(a.serve_rate * a.serve_seconds)
+    arr = np.cumsum(rng.exponential(1.0 / a.serve_rate, n_req)) * 1e3
+    is_rst = rng.random(n_req) < 0.05
+    who = rng.integers(0, P, n_req)
+    queues = [deque() for _ in range(P)]
+    busy = [None] * P
+    ready = set()
+    lat = {"checkpoint": [], "restart": []}
+    nbytes_done = 0
+    rst_ok, rst_checked = True, 0
+    pending_checks = []
+    t0 = mc.now_ms() + 20.0
+    i = 0
+    t_last = t0
+    outstanding = 0
+    while i < n_req or outstanding or ready:
+        now = mc.now_ms()
+        while i < n_req and t0 + arr[i] <= now:
+            p = int(who[i])
+            queues[p].append((t0 + arr[i], bool(is_rst[i])))
+            if busy[p] is None:
+                ready.add(p)
+            i += 1
+        for p in list(ready):
+            arrival, r = queues[p][0]
+            if r:
+                if not free_outs:
+                    continue
+                slot = free_outs.pop()
+                target = int(rng.integers(0, step[p]))
+                n = mix[p]["nbytes"]
+                srv.submit_restart(pids[p], target, outs[slot][:n])
+                busy[p] = ("restart", arrival, target, slot)
+            else:
+                plans[p].apply(bufs[p], step[p])
+                srv.submit_checkpoint(pids[p], bufs[p])
+                busy[p] = ("checkpoint", arrival, step[p], None)
+                step[p] += 1
+            queues[p].popleft()
+            ready.discard(p)
+            outstanding += 1
+        done = srv.poll(0.0 if (ready or (i < n_req and t0 + arr[i] <= mc.now_ms() + 0.05)) else 0.2)
+        for c in done:
+            p = c["pid"]  # this server's process ids are 0..P-1 in order
+            what, arrival, target, slot = busy[p]
+            assert c["status"] == 0, c
+            lat[what].append(c["t_done_ms"] - arrival)
+            nbytes_done += mix[p]["nbytes"]
+            t_last = max(t_last, c["t_done_ms"])
+            if what == "restart":
+                pending_checks.append((p, target, _digest2(mc, kind, outs[slot][:mix[p]["nbytes"]])))
+                free_outs.append(slot)
+            busy[p] = None
+            outstanding -= 1
+            if queues[p]:
+                ready.add(p)
+    wall = (t_last - t0) / 1e3
+    st = srv.stats()
+    # every restart against the state it restores: replay each process's
+    # updates (deterministic per seed and step) into a scratch buffer
+    need = {}
+    for p, target, got in pending_checks:
+        need.setdefault(p, []).append((target, got))
+    scratch = torch.empty(maxn, dtype=torch.uint8, device=dev)
+    for p, items in need.items():
+        m = mix[p]
+        b = workloads.init_device(scratch[:m["nbytes"]], m["seed"], zr[p])
+        for k in range(max(t for t, _ in items) + 1):
+            if k:
+                plans[p].apply(b, k)
+            exp = None
+            for t, got in items:
+                if t == k:
+                    exp = _digest2(mc, kind, b) if exp is None else exp
+                    rst_checked += 1
+                    rst_ok = rst_ok and bool(torch.equal(got, exp))
+    del scratch
+    # a sample of processes alone, through lone handles: byte-identical chains
+    alone_ok, alone_checked = True, 0
+    sample = sorted(set(int(x) for x in np.linspace(0, P - 1, a.serve_verify_procs)))
+    for p in sample:
+        m = mix[p]
+        b = workloads.init_device(torch.empty(m["nbytes"], dtype=torch.uint8, device=dev), m["seed"], zr[p])
+        d = mc.TreeDeduplicator(m["chunk_size"], kind)
+        for k in range(step[p]):
+            if k:
+                plans[p].apply(b, k)
+            alone_ok = alone_ok and d.checkpoint(b, k == 0) == srv.diff(pids[p], k)
+            alone_checked += 1
+        d.close()
+        del b
+    srv.close()
+
+    def pct(v, q):
+        return round(float(np.percentile(v, q)), 3) if v else None
+    allv = lat["checkpoint"] + lat["restart"]
+    return {
+        "workload": "%d processes, buffers 2^k B with k uniform in 22..28 (%.1f GiB), 128 B chunks, Murmur3, tree "
+                    "approach; Poisson arrivals at %.0f requests/s for %.1f s, 5%% restarts of a random earlier "
+                    "checkpoint, change rate 0.5-5%% per checkpoint (4 GiB update pattern); %.0f GB HBM budget"
+                    % (P, sum(m["nbytes"] for m in mix) / GIB, a.serve_rate, a.serve_seconds, a.serve_budget_gb),
+        "value": round(nbytes_done / wall / 1e9, 3), "unit": "GB/s",
+        "requests": n_req, "achieved_rate": round(len(allv) / wall, 1),
+        "latency_ms": {"p50": pct(allv, 50), "p99": pct(allv, 99), "mean": round(float(np.mean(allv)), 3),
+                       "checkpoint_p50": pct(lat["checkpoint"], 50), "checkpoint_p99": pct(lat["checkpoint"], 99),
+                       "restart_p50": pct(lat["restart"], 50), "restart_p99": pct(lat["restart"], 99)},
+        "restarts_verified": rst_checked, "restarts_identical": rst_ok,
+        "alone_vs_mix": {"processes": len(sample), "checkpoints": alone_checked, "identical": alone_ok},
+        "baseline_s": round(base_s, 2),
+        "server": {k: st[k] for k in ("inflight_peak", "graph_captures", "graph_replays", "spilled_diffs",
+                                      "spilled_states", "restored_states", "staged_diffs", "hbm_peak",
+                                      "deferred_admissions", "failed", "worker_ms")},
+        "note": "value: bytes of all completed requests (checkpointed and restarted buffers) / time from the first "
+                "arrival to the last completion; latency: arrival to completion (diff archived in HBM, or "
+                "restarted buffer written)",
+    }
+
+
 def main():
     a = parse()
     ws, rank, local = dist_setup()
@@ -413,6 +594,9 @@ def main():
     kind = mc.MD5 if a.hash == "md5" else mc.MURMUR3
     if a.only_batch:
         print(json.dumps({"batched": batch_bench(torch, mc, torch.device("cuda", local), a)}), flush=True)
+        return 0
+    if a.only_serve:
+        print(json.dumps({"served": serve_bench(torch, mc, torch.device("cuda", local), a)}), flush=True)
         return 0
     cs = a.chunk
     nbytes = int(a.size_gib * GIB) // cs * cs
@@ -512,6 +696,12 @@ def main():
         bat = batch_bench(torch, mc, dev, a)
         torch.cuda.empty_cache()
 
+    srvd = None
+    if not a.no_serve and rank == 0:
+        torch.cuda.empty_cache()
+        srvd = serve_bench(torch, mc, dev, a)
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu:
         v, nsteps = cpu_sample(1 if a.hash == "md5" else 0, cs)
@@ -542,6 +732,7 @@ def main():
             "e2e": e2e,
             "restart": rst,
             "batched": bat,
+            "served": srvd,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }

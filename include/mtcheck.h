@@ -227,7 +227,8 @@ typedef struct mtc_server_options {
   int32_t use_graph;       /* replay a per-process CUDA graph for incremental checkpoints;
                               while the worker captures one, no thread of the application
                               may synchronise the whole device (cudaDeviceSynchronize) */
-  int32_t reserved;
+  int32_t reserve_hbm;     /* take the whole budget from the device at creation */
+  uint64_t pinned_reserve; /* bytes of pinned host memory for spills, pinned at creation */
 } mtc_server_options_t;
 #define MTC_REQ_CHECKPOINT 0
 #define MTC_REQ_RESTART 1
@@ -248,6 +249,8 @@ typedef struct mtc_server_stats {
   uint64_t hbm_used, hbm_peak, pinned_reserved, deferred_admissions;
   uint32_t inflight_peak;
   uint32_t reserved;
+  double worker_ms[4];     /* worker host time: starting requests, finishing them,
+                              making room (spills), waiting for work */
 } mtc_server_stats_t;
 int mtc_server_create(const mtc_server_options_t* opt, mtc_server_t** out);
 /* waits for every submitted request, then frees everything */

@@ -68,7 +68,7 @@ class Tune(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32), ("id_headroom", ctypes.c_uint32),
-                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("use_graph", ctypes.c_int32), ("reserve_hbm", ctypes.c_int32), ("pinned_reserve", ctypes.c_uint64)]
 
 
 class Completion(ctypes.Structure):
@@ -82,10 +82,12 @@ class ServerStats(ctypes.Structure):
         "submitted", "completed", "failed", "checkpoints", "restarts", "bytes_checkpointed", "bytes_restarted",
         "spilled_diffs", "spilled_states", "restored_states", "staged_diffs", "spilled_bytes", "graph_captures",
         "graph_replays", "hbm_used", "hbm_peak", "pinned_reserved", "deferred_admissions")] + \
-        [("inflight_peak", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+        [("inflight_peak", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("worker_ms", ctypes.c_double * 4)]
 
     def as_dict(self):
-        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n not in ("reserved", "worker_ms")}
+        d["worker_ms"] = {k: round(self.worker_ms[j], 2) for j, k in enumerate(("start", "finish", "room", "wait"))}
+        return d
 
 
 # every symbol of include/mtcheck.h with its ctypes signature
@@ -410,8 +412,10 @@ class Server:
     restart requests; a worker thread admits them continuously under an HBM
     budget, spilling cold state to pinned host memory."""
 
-    def __init__(self, hbm_budget=0, max_inflight=0, id_headroom=0, use_graph=False):
-        o = ServerOptions(int(hbm_budget), int(max_inflight), int(id_headroom), int(use_graph), 0)
+    def __init__(self, hbm_budget=0, max_inflight=0, id_headroom=0, use_graph=False, reserve_hbm=False,
+                 pinned_reserve=0):
+        o = ServerOptions(int(hbm_budget), int(max_inflight), int(id_headroom), int(use_graph), int(reserve_hbm),
+                          int(pinned_reserve))
         s = _VP()
         _check(load().mtc_server_create(ctypes.byref(o), ctypes.byref(s)))
         self.s = s

@@ -409,6 +409,8 @@ int mtc_server_create(const mtc_server_options_t* opt, mtc_server_t** out) {
     if (opt->max_inflight) o.max_inflight = opt->max_inflight;
     if (opt->id_headroom) o.id_headroom = opt->id_headroom;
     o.use_graph = opt->use_graph;
+    o.reserve_hbm = opt->reserve_hbm;
+    o.pinned_reserve = opt->pinned_reserve;
   }
   auto* h = new (std::nothrow) mtc_server;
   if (!h) return ret(MTC_ENOMEM, "out of host memory");
@@ -485,6 +487,7 @@ int mtc_server_get_stats(mtc_server_t* s, mtc_server_stats_t* o) {
   o->graph_captures = t.graph_captures; o->graph_replays = t.graph_replays;
   o->hbm_used = t.hbm_used; o->hbm_peak = t.hbm_peak; o->pinned_reserved = t.pinned_reserved;
   o->deferred_admissions = t.deferred_admissions; o->inflight_peak = t.inflight_peak;
+  for (int k = 0; k < 4; k++) o->worker_ms[k] = t.worker_ms[k];
   return MTC_OK;
 }
 

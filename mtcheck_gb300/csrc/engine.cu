@@ -67,9 +67,6 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
     return ST_OK;
   }
   if (map_cap_ >= need) return ST_OK;
-  // an existing map grows to twice the bound, so that it grows rarely (each
-  // growth moves the table, which a captured launch sequence bakes in)
-  need *= 2;
   DevBuf<MapSlot> fresh;
   MTC_CUDA(fresh.ensure(need, stream_));
   MTC_CUDA(cudaMemsetAsync(fresh.p, 0, sizeof(MapSlot) * need, stream_));
@@ -141,7 +138,9 @@ int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
     MTC_CUDA(lay_.ensure(1, stream_));
     MTC_CUDA(sp_.ensure(1, stream_));
     if (mode_ != MODE_BASIC) {
-      int rc = ensure_map(tree ? M : N, true);
+      // room for the baseline's inserts and the worst case of the next
+      // checkpoint, so that the first incremental checkpoint does not grow it
+      int rc = ensure_map(2ull * (tree ? M : N), true);
       if (rc) return rc;
     }
     allocated_ = true;

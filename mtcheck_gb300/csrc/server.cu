@@ -22,6 +22,28 @@ uint64_t PinnedArena::cls(uint64_t n) {
   return c;
 }
 
+bool PinnedArena::add_slab(uint64_t bytes) {
+  void* q = nullptr;
+  if (cudaHostAlloc(&q, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  all_.push_back(static_cast<uint8_t*>(q));
+  slabs_.push_back({static_cast<uint8_t*>(q), bytes});
+  reserved_ += bytes;
+  return true;
+}
+
+bool PinnedArena::reserve(uint64_t bytes) {
+  constexpr uint64_t kGiB = 1ull << 30, kMin = 256ull << 20;
+  while (reserved_ < bytes) {
+    const uint64_t left = bytes - reserved_;
+    const uint64_t slab = left < kMin ? kMin : (left < kGiB ? left : kGiB);
+    if (!add_slab(slab)) return false;
+  }
+  return true;
+}
+
 uint8_t* PinnedArena::alloc(uint64_t n) {
   const uint64_t c = cls(n);
   auto& fl = free_[c];
@@ -30,14 +52,19 @@ uint8_t* PinnedArena::alloc(uint64_t n) {
     fl.pop_back();
     return p;
   }
-  void* p = nullptr;
-  if (cudaHostAlloc(&p, c, cudaHostAllocDefault) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  all_.push_back(static_cast<uint8_t*>(p));
-  reserved_ += c;
-  return static_cast<uint8_t*>(p);
+  for (Slab& sl : slabs_)
+    if (sl.left >= c) {
+      uint8_t* p = sl.next;
+      sl.next += c;
+      sl.left -= c;
+      return p;
+    }
+  if (!add_slab(std::max<uint64_t>(c, 256ull << 20))) return nullptr;
+  Slab& sl = slabs_.back();
+  uint8_t* p = sl.next;
+  sl.next += c;
+  sl.left -= c;
+  return p;
 }
 
 void PinnedArena::free(uint8_t* p, uint64_t n) {
@@ -69,6 +96,17 @@ Server::Server(const ServerOptions& o) : opt_(o) {
     pool_ = nullptr;
     cudaGetLastError();
   }
+  if (pool_ && opt_.reserve_hbm) {
+    // grow the pool to the budget once; freed memory stays in the pool
+    cudaStream_t s = nullptr;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    void* p = nullptr;
+    if (cudaMallocFromPoolAsync(&p, opt_.hbm_budget, pool_, s) == cudaSuccess) cudaFreeAsync(p, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    cudaGetLastError();
+  }
+  if (opt_.pinned_reserve) arena_.reserve(opt_.pinned_reserve);
   thread_ = std::thread([this] { worker(); });
 }
 
@@ -274,7 +312,11 @@ uint64_t Server::need_bytes(const Req& r, const Proc& p) const {
   if (e.spilled()) need += p.spill_len + estimate_state(e.mode(), r.len, e.chunk_size()) / 2;
   if (r.kind == REQ_CHECKPOINT) {
     if (p.state_dev == 0 && !e.spilled()) need += estimate_state(e.mode(), r.len, e.chunk_size());
-    need += 32 + 12 * (N + 1) + (N + 1) * e.chunk_size();  // worst-case archived diff
+    // the archived diff: the worst case is the whole buffer (a baseline);
+    // afterwards twice the latest size, at least 1/16 of the buffer -- a
+    // larger diff overshoots the budget until the next admission spills
+    const uint64_t worst = 32 + 12 * (N + 1) + (N + 1) * e.chunk_size();
+    need += p.chain.empty() ? worst : std::min(worst, std::max(2 * p.last_diff, r.len / 16));
   } else {
     for (uint32_t k = 0; k <= r.chkpt_id && k < p.chain.size(); k++)
       if (!p.chain[k].dev) need += p.chain[k].len;  // staged back for the restart
@@ -296,6 +338,7 @@ void Server::spill_diff(Proc& p, Archived& a) {
   a.host = h;
   a.dev = nullptr;
   chain_dev_ -= a.len;
+  p.chain_dev -= a.len;
   st_.spilled_diffs++;
   st_.spilled_bytes += a.len;
 }
@@ -337,25 +380,21 @@ bool Server::make_room(uint64_t need, uint32_t except) {
     for (Proc* pp : view_) u += pp->state_dev;
     return u;
   };
-  while (used() + need > opt_.hbm_budget) {
-    // 1. the oldest archived checkpoint of the least recently used idle process
+  // spill down to 95% of the budget, so that the next admissions find room
+  const uint64_t target = opt_.hbm_budget - opt_.hbm_budget / 20;
+  while (used() + need > target) {
+    // 1. every archived checkpoint of the least recently used idle process
     Proc* victim = nullptr;
     for (uint32_t i = 0; i < view_.size(); i++) {
       Proc& p = *view_[i];
-      if (p.busy || i == except) continue;
-      bool has = false;
-      for (auto& a : p.chain)
-        if (a.dev) { has = true; break; }
-      if (has && (!victim || p.lru < victim->lru)) victim = &p;
+      if (p.busy || i == except || p.chain_dev == 0) continue;
+      if (!victim || p.lru < victim->lru) victim = &p;
     }
     if (victim) {
+      const uint64_t before = chain_dev_;
       for (auto& a : victim->chain)
-        if (a.dev) {
-          const uint64_t before = chain_dev_;
-          spill_diff(*victim, a);
-          if (chain_dev_ == before) return false;  // no pinned memory left
-          break;
-        }
+        if (a.dev) spill_diff(*victim, a);
+      if (chain_dev_ == before) return used() + need <= opt_.hbm_budget;  // no pinned memory left
       continue;
     }
     // 2. the digest state of the least recently used idle process
@@ -364,10 +403,10 @@ bool Server::make_room(uint64_t need, uint32_t except) {
       if (p.busy || i == except || p.state_dev == 0 || p.eng->mode() == MODE_FULL) continue;
       if (!victim || p.lru < victim->lru) victim = &p;
     }
-    if (!victim) return false;
+    if (!victim) return used() + need <= opt_.hbm_budget;
     const uint64_t before = victim->state_dev;
     spill_state(*victim);
-    if (victim->state_dev == before) return false;
+    if (victim->state_dev == before) return used() + need <= opt_.hbm_budget;
   }
   return true;
 }
@@ -460,7 +499,11 @@ bool Server::try_start(Req& r) {
   const uint64_t need = need_bytes(r, p);
   uint64_t used = chain_dev_;
   for (Proc* pp : view_) used += pp->state_dev;
-  if (used + need > opt_.hbm_budget && !make_room(need, r.pid)) {
+  const double t_room = now_ms();
+  const bool over = used + need > opt_.hbm_budget;
+  const bool room = !over || make_room(need, r.pid);
+  if (over) st_.worker_ms[2] += now_ms() - t_room;
+  if (!room) {
     if (flights_.empty()) {
       // nothing in flight will free memory: the request cannot fit
       Completion c{r.ticket, r.pid, r.kind, ST_ENOMEM, 0, 0, r.t_submit, now_ms(), now_ms()};
@@ -473,7 +516,8 @@ bool Server::try_start(Req& r) {
     st_.deferred_admissions++;
     return false;
   }
-  Flight f{r, nullptr, now_ms(), 0, {}};
+  const double t_start = now_ms();
+  Flight f{r, nullptr, t_start, 0, {}};
   p.busy = true;
   p.lru = ++tick_;
   // a failed start still completes in stream order, after what it issued
@@ -485,6 +529,7 @@ bool Server::try_start(Req& r) {
   cudaEventRecord(f.done, p.s);
   flights_.push_back(f);
   std::lock_guard<std::mutex> g(mu_);
+  st_.worker_ms[0] += now_ms() - t_start;
   st_.inflight_peak = std::max<uint32_t>(st_.inflight_peak, (uint32_t)flights_.size());
   uint64_t u = chain_dev_;
   for (Proc* pp : view_) u += pp->state_dev;
@@ -525,7 +570,11 @@ void Server::finish(Flight& f) {
         c.diff_len = n;
         std::lock_guard<std::mutex> g(mu_);
         p.chain.push_back(a);
-        if (a.dev) chain_dev_ += n;
+        p.last_diff = n;
+        if (a.dev) {
+          chain_dev_ += n;
+          p.chain_dev += n;
+        }
         st_.checkpoints++;
         st_.bytes_checkpointed += f.r.len;
       }
@@ -587,7 +636,9 @@ void Server::worker() {
       }
       Flight f = flights_[i];
       flights_.erase(flights_.begin() + (long)i);
+      const double t_fin = now_ms();
       finish(f);
+      st_.worker_ms[1] += now_ms() - t_fin;
       progress = true;
     }
     // 2. admission in submission order; one request per process at a time
@@ -608,9 +659,11 @@ void Server::worker() {
       }
     }
     if (!progress) {
+      const double t_wait = now_ms();
       std::unique_lock<std::mutex> g(mu_);
       if (inbox_.empty() && !stop_)
         cv_work_.wait_for(g, flights_.empty() ? std::chrono::microseconds(2000) : std::chrono::microseconds(20));
+      st_.worker_ms[3] += now_ms() - t_wait;
     }
   }
 }

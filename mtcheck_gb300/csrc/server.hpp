@@ -41,6 +41,11 @@ struct ServerOptions {
   // captures one when a process's buffers move; during that capture a
   // device-wide synchronisation by any thread of the application fails.
   int use_graph = 0;
+  // Allocate the HBM budget from the server's pool once at creation (and
+  // keep it there), and pin this much host memory for spills up front:
+  // growing either later costs milliseconds per allocation.
+  int reserve_hbm = 0;
+  uint64_t pinned_reserve = 0;
 };
 
 enum : int { REQ_CHECKPOINT = 0, REQ_RESTART = 1 };
@@ -64,21 +69,32 @@ struct ServerStats {
   uint64_t hbm_used = 0, hbm_peak = 0, pinned_reserved = 0;
   uint64_t deferred_admissions = 0;  // admission attempts refused for memory
   uint32_t inflight_peak = 0;
+  double worker_ms[4] = {0, 0, 0, 0};  // host time of the worker: starting requests,
+                                       // finishing them, making room, waiting
 };
 
 // Pinned host memory in power-of-two blocks, reused, freed at destruction
-// (cudaFreeHost would wait for the whole device).
+// (cudaFreeHost would wait for the whole device).  Blocks are carved from
+// slabs of at least 256 MiB, so that cudaHostAlloc -- slow -- runs rarely;
+// reserve() pins slabs ahead of use.
 class PinnedArena {
  public:
   ~PinnedArena();
   uint8_t* alloc(uint64_t n);
   void free(uint8_t* p, uint64_t n);
+  bool reserve(uint64_t bytes);
   uint64_t reserved() const { return reserved_; }
 
  private:
+  struct Slab {
+    uint8_t* next;
+    uint64_t left;
+  };
   static uint64_t cls(uint64_t n);
+  bool add_slab(uint64_t bytes);
   std::map<uint64_t, std::vector<uint8_t*>> free_;
   std::vector<uint8_t*> all_;
+  std::vector<Slab> slabs_;
   uint64_t reserved_ = 0;
 };
 
@@ -117,6 +133,8 @@ class Server {
     uint64_t spill_len = 0;
     cudaGraphExec_t exec = nullptr;
     uint64_t sig = 0;
+    uint64_t chain_dev = 0;        // device bytes of archived checkpoints
+    uint64_t last_diff = 0;        // size of the latest incremental checkpoint
   };
   struct Req {
     uint64_t ticket;

@@ -173,3 +173,129 @@ def batch_mix(count=96, seed=4, median_mib=72.0, sigma=1.2, lo_mib=1, hi_mib=512
         out.append({"nbytes": nbytes, "chunk_size": cs, "hash": i % 2, "rate": float(rng.uniform(*rate)),
                     "seed": int(seed * 1000 + i)})
     return out
+
+
+# ---------------------------------------------------------------------------
+# On-device update pattern for request streams: one call per checkpoint,
+# a handful of kernel launches, deterministic for (seed, step).
+# ---------------------------------------------------------------------------
+def init_device(buf, seed, zero_range=None):
+    """Fill a torch CUDA uint8 buffer with seeded random bytes."""
+    import torch
+    g = torch.Generator(device=buf.device)
+    g.manual_seed(int(seed) & 0x7FFFFFFFFFFFFFFF)
+    buf.copy_(torch.randint(0, 256, (buf.numel(),), dtype=torch.uint8, device=buf.device, generator=g))
+    if zero_range:
+        buf[zero_range[0]:zero_range[1]] = 0
+    return buf
+
+
+def mutate_device(buf, cs, rate, seed, run_max=4096, shift_frac=0.1, zero_range=None):
+    """One step of the 4 GiB update pattern applied in place to a torch CUDA
+    buffer: `rate` of the chunks change, half as sparse single chunks and half
+    as runs of up to `run_max` chunks (fresh random bytes); a further
+    `shift_frac` of the changed count become copies of chunks at earlier
+    offsets of the previous state; `zero_range` stays zero."""
+    import torch
+    dev = buf.device
+    nbytes = buf.numel()
+    full = nbytes // cs
+    if full < 2:
+        return buf
+    rng = np.random.default_rng(int(seed) & 0x7FFFFFFFFFFFFFFF)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(rng.integers(1 << 62)))
+    nchg = max(2, int(rate * full))
+    rows = buf[:full * cs].view(full, cs)
+    # shifted duplicates read the previous state: gather them first.  Every
+    # index set is made unique so that no two writes race (the result is the
+    # same on every run)
+    nshift = max(1, int(shift_frac * nchg))
+    dst = torch.unique(torch.randint(1, full, (nshift,), device=dev, generator=g))
+    src = (torch.rand(dst.numel(), device=dev, generator=g) * dst).long()
+    shifted = rows[src].clone()
+    # sparse chunks
+    sparse = torch.randint(0, full, (nchg // 2,), device=dev, generator=g)
+    # runs: lengths on the host, starts and expansion on the device
+    left = nchg - nchg // 2
+    lens = []
+    while left > 0:
+        ln = int(min(left, rng.integers(1, run_max + 1)))
+        lens.append(ln)
+        left -= ln
+    L = torch.tensor(lens, dtype=torch.long, device=dev)
+    hi = torch.clamp(full - L, min=1)
+    starts = (torch.rand(len(lens), device=dev, generator=g) * hi).long()
+    offs = torch.cumsum(L, 0) - L
+    total = int(sum(lens))
+    within = torch.arange(total, device=dev) - torch.repeat_interleave(offs, L, output_size=total)
+    runs = torch.repeat_interleave(starts, L, output_size=total) + within
+    idx = torch.unique(torch.cat([sparse, runs]))
+    rows[idx] = torch.randint(0, 256, (idx.numel(), cs), dtype=torch.uint8, device=dev, generator=g)
+    rows[dst] = shifted
+    if zero_range:
+        buf[zero_range[0]:zero_range[1]] = 0
+    return buf
+
+
+def serve_mix(count=256, seed=5, lo_log2=22, hi_log2=28, cs=128, rate=(0.005, 0.05)):
+    """Processes of the served workload: buffer sizes 2^k bytes with k uniform
+    over the integers [lo_log2, hi_log2] (4 MiB .. 256 MiB: a power-of-two
+    chunk count, for which the reference's tree restart is exact), chunk size
+    `cs`, one change-rate range for all."""
+    rng = np.random.default_rng(seed)
+    return [{"nbytes": 1 << int(rng.integers(lo_log2, hi_log2 + 1)), "chunk_size": cs, "rate": rate,
+             "seed": int(seed * 100000 + i)} for i in range(count)]
+
+
+class DeviceUpdates:
+    """Pre-generated steps of the 4 GiB update pattern for one device buffer,
+    for request streams where the update itself must cost little host time.
+    `count` variants are drawn once (changed chunk ids -- half sparse, half
+    runs of up to `run_max` chunks --, their new bytes, and `shift_frac` as
+    many shifted-duplicate destinations with earlier sources).  apply(step)
+    writes variant step % count, its bytes XOR-ed with the low byte of the
+    step so that repeated variants still write new content; four kernel
+    launches.  Deterministic for (seed, step)."""
+
+    def __init__(self, buf, cs, rate, seed, count=4, run_max=4096, shift_frac=0.1, zero_range=None):
+        import torch
+        self.cs = cs
+        self.full = buf.numel() // cs
+        self.zero_range = zero_range
+        dev = buf.device
+        rng = np.random.default_rng(int(seed) & 0x7FFFFFFFFFFFFFFF)
+        g = torch.Generator(device=dev)
+        g.manual_seed(int(rng.integers(1 << 62)))
+        full = self.full
+        self.variants = []
+        for _ in range(count):
+            nchg = max(2, int(rate * full))
+            sparse = torch.randint(0, full, (nchg // 2,), device=dev, generator=g)
+            left, lens = nchg - nchg // 2, []
+            while left > 0:
+                ln = int(min(left, rng.integers(1, run_max + 1)))
+                lens.append(ln)
+                left -= ln
+            L = torch.tensor(lens, dtype=torch.long, device=dev)
+            starts = (torch.rand(len(lens), device=dev, generator=g) * torch.clamp(full - L, min=1)).long()
+            total = int(sum(lens))
+            offs = torch.cumsum(L, 0) - L
+            runs = torch.repeat_interleave(starts, L, output_size=total) + \
+                torch.arange(total, device=dev) - torch.repeat_interleave(offs, L, output_size=total)
+            idx = torch.unique(torch.cat([sparse, runs]))
+            payload = torch.randint(0, 256, (idx.numel(), cs), dtype=torch.uint8, device=dev, generator=g)
+            dst = torch.unique(torch.randint(1, full, (max(1, int(shift_frac * nchg)),), device=dev, generator=g))
+            src = (torch.rand(dst.numel(), device=dev, generator=g) * dst).long()
+            self.variants.append((idx, payload, dst, src))
+
+    def apply(self, buf, step):
+        import torch
+        idx, payload, dst, src = self.variants[step % len(self.variants)]
+        rows = buf[:self.full * self.cs].view(self.full, self.cs)
+        shifted = rows[src]                         # earlier offsets of the previous state
+        rows[idx] = torch.bitwise_xor(payload, step & 0xFF)
+        rows[dst] = shifted
+        if self.zero_range:
+            buf[self.zero_range[0]:self.zero_range[1]] = 0
+        return buf

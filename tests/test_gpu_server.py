@@ -130,7 +130,7 @@ def test_each_process_alone(cuda, mtc, states, lone):
 
 def test_spill_under_small_budget(cuda, mtc, states, lone):
     # about one process's state fits: the others spill and come back
-    srv = mtc.Server(hbm_budget=24 << 20, max_inflight=4, use_graph=True)
+    srv = mtc.Server(hbm_budget=12 << 20, max_inflight=4, use_graph=True)
     pids, restarts = serve(cuda, mtc, states, PROCS, srv)
     check(mtc, srv, pids, restarts, lone)
     st = srv.stats()
@@ -172,3 +172,14 @@ def test_bad_arguments(cuda, mtc):
     c = srv.poll()
     assert c[0]["status"] == 1
     srv.close()
+
+
+def test_device_update_pattern_is_deterministic(cuda, mtc):
+    # the request-stream generator replays to the same states (no racing writes)
+    a = workloads.init_device(cuda.empty(3 << 20, dtype=cuda.uint8, device="cuda"), 9, (1 << 20, 3 << 19))
+    b = workloads.init_device(cuda.empty(3 << 20, dtype=cuda.uint8, device="cuda"), 9, (1 << 20, 3 << 19))
+    assert cuda.equal(a, b)
+    for k in range(1, 6):
+        workloads.mutate_device(a, 128, 0.05, seed=100 + k, run_max=512, zero_range=(1 << 20, 3 << 19))
+        workloads.mutate_device(b, 128, 0.05, seed=100 + k, run_max=512, zero_range=(1 << 20, 3 << 19))
+        assert cuda.equal(a, b), k
