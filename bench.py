@@ -157,13 +157,15 @@ def make_states(torch, nbytes, cs, count, seed, device):
     return states
 
 
-def restart_bench(torch, mc, dev, a, kind):
+def restart_bench(torch, mc, dev, a, kind, approach=None):
     """Restart of the last checkpoint of a chain (1 GiB, 256 B chunks, 30
-    incrementals after a baseline, 4 GiB update pattern), tree approach."""
+    incrementals after a baseline, 4 GiB update pattern); tree approach unless
+    `approach` is given."""
     from mtcheck_gb300 import workloads
+    approach = approach or mc.TREE
     nbytes = int(a.restart_gib * GIB) // a.restart_chunk * a.restart_chunk
     z = (nbytes // 4, nbytes // 4 + nbytes // 8)
-    d = mc.TreeDeduplicator(a.restart_chunk, kind)
+    d = mc.Deduplicator(a.restart_chunk, kind, approach=approach)
     chain_dev, chain_host, last = [], [], None
     for i, s in enumerate(workloads.pattern2(nbytes, a.restart_chunk, a.restart_chain, seed=303, device=dev,
                                              zero_range=z)):
@@ -179,7 +181,7 @@ def restart_bench(torch, mc, dev, a, kind):
     out = torch.empty(nbytes, dtype=torch.uint8, device=dev)
     ptrs = [(t.data_ptr(), t.numel()) for t in chain_dev]
     rid = len(chain_dev) - 1
-    r = mc.TreeDeduplicator(a.restart_chunk, kind)
+    r = mc.Deduplicator(a.restart_chunk, kind, approach=approach)
     r.restart_device(out, ptrs, rid)  # warm-up
     ok = bool(torch.equal(out, last))
     reps = 5
@@ -206,8 +208,9 @@ def restart_bench(torch, mc, dev, a, kind):
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
         ok = ok and bool(torch.equal(out, last))
-    return {"workload": "restart of checkpoint %d of a tree chain, %.3g GiB buffer, %d B chunks, 4 GiB update "
-                        "pattern" % (rid, a.restart_gib, a.restart_chunk),
+    name = {mc.TREE: "tree", mc.LIST: "list", mc.BASIC: "basic"}.get(approach, str(approach))
+    return {"workload": "restart of checkpoint %d of a %s chain, %.3g GiB buffer, %d B chunks, 4 GiB update "
+                        "pattern" % (rid, name, a.restart_gib, a.restart_chunk),
             "value": round(nbytes / dev_t / 1e9, 3), "unit": "GB/s", "ms": round(dev_t * 1e3, 3),
             "call_ms": round(call_t * 1e3, 3),
             "chain_bytes": int(chain_bytes), "verified_byte_identical": ok,
@@ -422,7 +425,9 @@ def serve_bench(torch, mc, dev, a):
     earlier checkpoint of the process; a checkpoint first applies one step of
     the 4 GiB update pattern (change rate 0.5-5%).  A process has at most one
     request on the server; later arrivals for it wait, and latency runs from
-    the arrival time to completion.  The update steps are drawn before the
+    the arrival time to completion.  Before the timed stream every process
+    makes one incremental checkpoint and every buffer size one restart
+    (warm-up).  The update steps are drawn before the
     stream starts (DeviceUpdates) so that the driver keeps up with the rate.
     Every restart is verified against a digest of the state it restores; a
     sample of processes is replayed alone through lone handles and compared
@@ -458,6 +463,25 @@ def serve_bench(torch, mc, dev, a):
     assert all(c["status"] == 0 for c in base)
     base_s = time.perf_counter() - t_base
     step = [1] * P
+    pending_checks = []
+    # warm-up, not timed: one incremental checkpoint per process, then one
+    # restart per buffer size (first use of every kernel, of the allocator
+    # sizes of the update step, of the restart scratch)
+    for p in range(P):
+        plans[p].apply(bufs[p], 1)
+        srv.submit_checkpoint(pids[p], bufs[p])
+    got = []
+    while len(got) < P:
+        got += srv.poll(100)
+    assert all(c["status"] == 0 for c in got)
+    step = [2] * P
+    for nb in sorted(set(m["nbytes"] for m in mix)):
+        p = next(i for i, m in enumerate(mix) if m["nbytes"] == nb)
+        srv.submit_restart(pids[p], 1, outs[0][:nb])
+        srv.drain()
+        c = srv.poll(100)
+        assert len(c) == 1 and c[0]["status"] == 0, c
+        pending_checks.append((p, 1, _digest2(mc, kind, outs[0][:nb])))
     # the request stream
     n_req = int(a.serve_rate * a.serve_seconds)
     arr = np.cumsum(rng.exponential(1.0 / a.serve_rate, n_req)) * 1e3
@@ -467,9 +491,9 @@ def serve_bench(torch, mc, dev, a):
     busy = [None] * P
     ready = set()
     lat = {"checkpoint": [], "restart": []}
+    lat_t = []                      # (arrival offset, latency) in ms
     nbytes_done = 0
     rst_ok, rst_checked = True, 0
-    pending_checks = []
     t0 = mc.now_ms() + 20.0
     i = 0
     t_last = t0
@@ -506,6 +530,7 @@ def serve_bench(torch, mc, dev, a):
             what, arrival, target, slot = busy[p]
             assert c["status"] == 0, c
             lat[what].append(c["t_done_ms"] - arrival)
+            lat_t.append((arrival - t0, c["t_done_ms"] - arrival))
             nbytes_done += mix[p]["nbytes"]
             t_last = max(t_last, c["t_done_ms"])
             if what == "restart":
@@ -555,19 +580,27 @@ def serve_bench(torch, mc, dev, a):
     def pct(v, q):
         return round(float(np.percentile(v, q)), 3) if v else None
     allv = lat["checkpoint"] + lat["restart"]
+    late = [v for t, v in lat_t if t >= 1000.0]
+    per_s = {}
+    for t, v in lat_t:
+        per_s.setdefault(int(t // 1000), []).append(v)
     return {
         "workload": "%d processes, buffers 2^k B with k uniform in 22..28 (%.1f GiB), 128 B chunks, Murmur3, tree "
                     "approach; Poisson arrivals at %.0f requests/s for %.1f s, 5%% restarts of a random earlier "
-                    "checkpoint, change rate 0.5-5%% per checkpoint (4 GiB update pattern); %.0f GB HBM budget"
+                    "checkpoint, change rate 0.5-5%% per checkpoint (4 GiB update pattern); %.0f GB HBM budget; "
+                    "timed after one untimed incremental checkpoint per process"
                     % (P, sum(m["nbytes"] for m in mix) / GIB, a.serve_rate, a.serve_seconds, a.serve_budget_gb),
         "value": round(nbytes_done / wall / 1e9, 3), "unit": "GB/s",
         "requests": n_req, "achieved_rate": round(len(allv) / wall, 1),
         "latency_ms": {"p50": pct(allv, 50), "p99": pct(allv, 99), "mean": round(float(np.mean(allv)), 3),
                        "checkpoint_p50": pct(lat["checkpoint"], 50), "checkpoint_p99": pct(lat["checkpoint"], 99),
-                       "restart_p50": pct(lat["restart"], 50), "restart_p99": pct(lat["restart"], 99)},
+                       "restart_p50": pct(lat["restart"], 50), "restart_p99": pct(lat["restart"], 99),
+                       "after_first_second_p50": pct(late, 50), "after_first_second_p99": pct(late, 99),
+                       "p99_per_second": [pct(per_s[k], 99) for k in sorted(per_s)]},
         "restarts_verified": rst_checked, "restarts_identical": rst_ok,
         "alone_vs_mix": {"processes": len(sample), "checkpoints": alone_checked, "identical": alone_ok},
         "baseline_s": round(base_s, 2),
+        "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
         "server": {k: st[k] for k in ("inflight_peak", "graph_captures", "graph_replays", "spilled_diffs",
                                       "spilled_states", "restored_states", "staged_diffs", "hbm_peak",
                                       "deferred_admissions", "failed", "worker_ms")},
@@ -689,6 +722,13 @@ def main():
         del states
         torch.cuda.empty_cache()
         rst = restart_bench(torch, mc, dev, a, kind)
+        torch.cuda.empty_cache()
+        rst["other_approaches"] = {}
+        for name, ap in (("list", mc.LIST), ("basic", mc.BASIC)):
+            r2 = restart_bench(torch, mc, dev, a, kind, ap)
+            rst["other_approaches"][name] = {k: r2[k] for k in ("value", "ms", "verified_byte_identical",
+                                                                 "host_chain_value", "chain_bytes")}
+            torch.cuda.empty_cache()
 
     bat = None
     if not a.no_batch and rank == 0:

@@ -412,40 +412,50 @@ bool Server::make_room(uint64_t need, uint32_t except) {
 }
 
 // ---- request execution -------------------------------------------------------
+int Server::ensure_graph(Proc& p, const uint8_t* data, uint64_t len) {
+  Engine& e = *p.eng;
+  const uint64_t sig = e.signature(data, len);
+  if (p.exec && p.sig == sig) return ST_OK;
+  if (p.exec) cudaGraphExecDestroy(p.exec);
+  p.exec = nullptr;
+  if (cudaStreamBeginCapture(p.s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return ST_ECUDA;
+  int rc = e.enqueue(data, len, false);
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(p.s, &g);
+  if (rc || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc ? rc : ST_ECUDA;
+  }
+  ce = cudaGraphInstantiate(&p.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) {
+    p.exec = nullptr;
+    return ST_ECUDA;
+  }
+  p.sig = sig;
+  std::lock_guard<std::mutex> lk(mu_);
+  st_.graph_captures++;
+  return ST_OK;
+}
+
 int Server::start_checkpoint(Req& r, Proc& p) {
   Engine& e = *p.eng;
+  bool restored = false;
   if (e.spilled()) {
     int rc = restore_state(p);
     if (rc) return rc;
+    restored = true;
   }
   if (cudaStreamWaitEvent(p.s, r.ready, 0) != cudaSuccess) return ST_ECUDA;
   int rc = e.prepare(r.data, r.len, r.make_baseline, opt_.id_headroom);
   if (rc) return rc;
-  const bool graph = opt_.use_graph && !e.fresh();
+  // a restored state has new device addresses: issuing it once costs less
+  // than capturing a graph that the next eviction may throw away
+  const bool graph = opt_.use_graph && !e.fresh() && !restored;
   if (graph) {
-    const uint64_t sig = e.signature(r.data, r.len);
-    if (!p.exec || p.sig != sig) {
-      if (p.exec) cudaGraphExecDestroy(p.exec);
-      p.exec = nullptr;
-      if (cudaStreamBeginCapture(p.s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return ST_ECUDA;
-      rc = e.enqueue(r.data, r.len, false);
-      cudaGraph_t g = nullptr;
-      cudaError_t ce = cudaStreamEndCapture(p.s, &g);
-      if (rc || ce != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        cudaGetLastError();
-        return rc ? rc : ST_ECUDA;
-      }
-      ce = cudaGraphInstantiate(&p.exec, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) {
-        p.exec = nullptr;
-        return ST_ECUDA;
-      }
-      p.sig = sig;
-      std::lock_guard<std::mutex> lk(mu_);
-      st_.graph_captures++;
-    }
+    rc = ensure_graph(p, r.data, r.len);
+    if (rc) return rc;
     e.stage_params();
     if (cudaGraphLaunch(p.exec, p.s) != cudaSuccess) return ST_ECUDA;
     std::lock_guard<std::mutex> lk(mu_);
@@ -579,6 +589,16 @@ void Server::finish(Flight& f) {
         st_.bytes_checkpointed += f.r.len;
       }
       e.current_id += 1;  // checkpoint(data, len, diff_h, make_baseline) advances
+      // get the next incremental checkpoint ready now, between requests:
+      // its allocations and its graph capture then cost the next request
+      // nothing (a new input pointer or baseline still re-prepares)
+      // (not under memory pressure: the process may be spilled before then)
+      uint64_t used = chain_dev_;
+      for (Proc* pp : view_) used += pp->state_dev;
+      if (c.status == ST_OK && opt_.use_graph && e.mode() != MODE_FULL &&
+          used < opt_.hbm_budget - opt_.hbm_budget / 10 &&
+          e.prepare(f.r.data, f.r.len, false, opt_.id_headroom) == ST_OK)
+        ensure_graph(p, f.r.data, f.r.len);
     } else {
       set_error(e.last_error);
     }

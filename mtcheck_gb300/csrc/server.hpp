@@ -13,7 +13,8 @@
 //   * when the budget is exceeded the least recently used idle processes are
 //     spilled to pinned host memory: first their archived checkpoints, then
 //     their digest state; a spilled process is restored on its next request;
-//   * incremental checkpoints of a process replay a per-process CUDA graph.
+//   * incremental checkpoints of a process replay a per-process CUDA graph,
+//     captured right after the previous checkpoint completes.
 // Every result is the one a lone deduplicator gives for the same sequence of
 // buffers: the launch sequence per process is the same, only its scheduling
 // differs.
@@ -159,6 +160,7 @@ class Server {
   void worker();
   bool try_start(Req& r);
   int start_checkpoint(Req& r, Proc& p);
+  int ensure_graph(Proc& p, const uint8_t* data, uint64_t len);
   int start_restart(Req& r, Proc& p, std::vector<uint8_t*>* temps);
   void finish(Flight& f);
   uint64_t need_bytes(const Req& r, const Proc& p) const;
