@@ -148,6 +148,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(torch, x, device, ws):
+    """The slowest rank's time (every rank gets it): the job ends when the
+    last replica does."""
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(bytes_per_rank, seconds, ws):
+    """GB/s of the whole job: every replica's bytes over the slowest time."""
+    return bytes_per_rank * ws / seconds / 1e9
+
+
 def make_states(torch, nbytes, cs, count, seed, device):
     from mtcheck_gb300 import workloads
     z = (GIB, GIB + GIB // 2) if nbytes >= 2 * GIB else (nbytes // 4, nbytes // 4 + nbytes // 8)
@@ -666,12 +680,8 @@ def main():
         stop.record()
         barrier()
     launches = mc.launch_count() - l0
-    elapsed = start.elapsed_time(stop) / 1e3
-    tmax = torch.tensor([elapsed], device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-    elapsed = float(tmax.item())
-    value = nbytes * K * ws / elapsed / 1e9
+    elapsed = max_over_ranks(torch, start.elapsed_time(stop) / 1e3, dev, ws)
+    value = whole_job_rate(nbytes * K, elapsed, ws)
 
     # roofline of the dominant kernel (leaf hashing): per chunk the chunk bytes,
     # the previous leaf digest read and the new leaf digest write
@@ -708,12 +718,8 @@ def main():
             de.copy_diff(pinned_out[i].numpy())
             d2h += n
         barrier()
-        te = time.perf_counter() - t0
-        te_t = torch.tensor([te], device=dev)
-        if ws > 1:
-            torch.distributed.all_reduce(te_t, op=torch.distributed.ReduceOp.MAX)
-        te = float(te_t.item())
-        e2e = {"value": round(nbytes * K * ws / te / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+        te = max_over_ranks(torch, time.perf_counter() - t0, dev, ws)
+        e2e = {"value": round(whole_job_rate(nbytes * K, te, ws), 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": int(d2h / K)}
         del host, pinned_out, outs
 

@@ -16,6 +16,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmtcheck_gb300.so")
+CLI_DIR = os.path.join(HERE, "cli")
+# command-line drivers of the reference (src/dedup_files.cpp,
+# src/restart_chkpt_files.cpp), built next to the library
+CLIS = ["dedup_chkpt_files", "restart_chkpt_files"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]
@@ -58,9 +62,28 @@ def build(verbose=False, extra=()):
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
         os.replace(LIB + ".tmp", LIB)
+    _build_clis()
     if verbose:
         print(LIB)
     return LIB
+
+
+def _build_clis():
+    """The CLI drivers: host C++ over include/mtcheck/deduplicator.hpp, linked
+    to the library with an $ORIGIN rpath."""
+    for name in CLIS:
+        src = os.path.join(CLI_DIR, name + ".cpp")
+        out = os.path.join(OUT_DIR, name)
+        deps = [src, LIB] + glob.glob(os.path.join(ROOT, "include", "*.h")) + \
+            glob.glob(os.path.join(ROOT, "include", "mtcheck", "*.hpp"))
+        if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+            continue
+        cmd = [nvcc(), "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o", out + ".tmp",
+               "-L", OUT_DIR, "-lmtcheck_gb300", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+        os.replace(out + ".tmp", out)
 
 
 if __name__ == "__main__":

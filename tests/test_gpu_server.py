@@ -140,7 +140,8 @@ def test_spill_under_small_budget(cuda, mtc, states, lone):
 
 
 def test_spill_without_graphs(cuda, mtc, states, lone):
-    srv = mtc.Server(hbm_budget=16 << 20, max_inflight=8)
+    # the six processes' states total about 12.5 MB: 8 MiB forces state spills
+    srv = mtc.Server(hbm_budget=8 << 20, max_inflight=8)
     pids, restarts = serve(cuda, mtc, states[:6], PROCS[:6], srv)
     check(mtc, srv, pids, restarts, lone[:6])
     st = srv.stats()
