@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--only-batch", action="store_true")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--only-serve", action="store_true")
+    p.add_argument("--only-restart", action="store_true")
     p.add_argument("--serve-procs", type=int, default=256)
     p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--serve-seconds", type=float, default=4.0)
@@ -644,6 +645,9 @@ def main():
         return 0
     if a.only_serve:
         print(json.dumps({"served": serve_bench(torch, mc, torch.device("cuda", local), a)}), flush=True)
+        return 0
+    if a.only_restart:
+        print(json.dumps({"restart": restart_bench(torch, mc, torch.device("cuda", local), a, kind)}), flush=True)
         return 0
     cs = a.chunk
     nbytes = int(a.size_gib * GIB) // cs * cs

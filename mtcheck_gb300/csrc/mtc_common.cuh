@@ -221,12 +221,29 @@ __device__ inline Digest hash_bytes(int kind, const uint8_t* p, uint64_t len) {
 // Merkle heap index arithmetic, include/kokkos_merkle_tree.hpp:102-142
 // (exact only for a power-of-two leaf count; restated as written).
 // ---------------------------------------------------------------------------
+// The reference descends from the node's children one level at a time until
+// the left index passes num_nodes (l = 2l+1, r = 2r+2), then steps back one
+// level.  After e doublings l = (node+1)*2^e - 1 and r = (node+2)*2^e - 2, so
+// the same result follows from the smallest e >= 1 with (node+1)*2^e >=
+// num_nodes+1, found from bit lengths; equal to the loop for every node of
+// every tree size (checked exhaustively in tests).
+__host__ __device__ __forceinline__ int bit_length64(uint64_t v) {
+#ifdef __CUDA_ARCH__
+  return 64 - __clzll((long long)v);
+#else
+  return v ? 64 - __builtin_clzll(v) : 0;
+#endif
+}
 __host__ __device__ __forceinline__ void leaf_range(uint32_t node, uint32_t num_nodes, uint32_t& lo, uint32_t& hi) {
-  uint32_t l = 2 * node + 1, r = 2 * node + 2;
-  while (l < num_nodes) { l = 2 * l + 1; r = 2 * r + 2; }
-  l = (l - 1) / 2; r = (r - 2) / 2;
-  if (r > num_nodes) r = num_nodes - 1;
-  lo = l; hi = r;
+  const uint64_t a = (uint64_t)node + 1, b = (uint64_t)num_nodes + 1;
+  int e = bit_length64(b) - bit_length64(a);
+  if (e < 1) e = 1;
+  if (e > 1 && (a << (e - 1)) >= b) e--;
+  if ((a << e) < b) e++;
+  uint64_t l = (a << (e - 1)) - 1, r = ((a + 1) << (e - 1)) - 2;
+  if (r > num_nodes) r = (uint64_t)num_nodes - 1;
+  lo = (uint32_t)l;
+  hi = (uint32_t)r;
 }
 __host__ __device__ __forceinline__ uint32_t num_leaf_descendents(uint32_t node, uint32_t num_nodes) {
   uint32_t l, r; leaf_range(node, num_nodes, l, r); return r - l + 1;

@@ -54,6 +54,9 @@ struct RArgs {
   uint32_t* fo_at;  // main checkpoint: lowest FO entry per node (tree) or chunk (list)
   uint32_t *dm_tab, *rm_tab, *dm_mask, *rm_mask;
   uint64_t *dm_excl, *rm_excl;  // per-entry item prefix of the chain tables
+  uint4* fo_rng;                // chain FO entries: leaf key ranges {lo0, n0, lo1, n1}
+  uint2 *bnd0, *bnd1;           // per expansion tile: first and last entry
+  uint32_t max_tiles;           // capacity of bnd0 / bnd1
   uint64_t *tot;                // [0] dm items, [1] rm items, [2] main FO chunks, [3] main shift chunks
   uint8_t* out;
   uint32_t* err;
@@ -247,10 +250,39 @@ struct ExpandTile {
   uint64_t ex[kExpandTile + 1];
   uint32_t e0, cnt;
 };
+// The first and last entry of every tile, for all tiles at once, written
+// from the entries' side: entry k owns items [excl[k], excl[k+1]) and records
+// itself for every tile that starts or ends inside that range.  No dependent
+// loads (a per-tile binary search would chain ~log2(n) of them).
+__global__ void expand_bounds_kernel(const uint64_t* excl, uint32_t n, const uint64_t* total, uint2* bounds,
+                                     uint32_t max_tiles) {
+  const uint64_t tot = *total;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = excl[k], e = k + 1 < n ? excl[k + 1] : tot;
+    if (e <= s) continue;  // no items: never the owner of one
+    for (uint64_t b = s / kExpandTile; b * kExpandTile < e && b < max_tiles; b++) {
+      const uint64_t first = b * kExpandTile;
+      const uint64_t last = (first + kExpandTile < tot ? first + kExpandTile : tot) - 1;
+      if (first >= s) bounds[b].x = (uint32_t)k;
+      if (last >= s && last < e) bounds[b].y = (uint32_t)k;
+    }
+  }
+}
+
 __device__ __forceinline__ void expand_stage(ExpandTile& T, const uint64_t* excl, uint32_t n, uint64_t t0,
-                                             uint64_t t1) {
+                                             uint64_t t1, const uint2* bounds = nullptr,
+                                             uint32_t max_tiles = 0) {
   if (threadIdx.x == 0) {
-    const uint32_t e0 = upper_entry(excl, n, t0), e1 = upper_entry(excl, n, t1 - 1);
+    const uint64_t b = t0 / kExpandTile;  // tiles start at multiples of kExpandTile
+    uint32_t e0, e1;
+    if (bounds && b < max_tiles) {
+      const uint2 v = bounds[b];
+      e0 = v.x;
+      e1 = v.y;
+    } else {
+      e0 = upper_entry(excl, n, t0);
+      e1 = upper_entry(excl, n, t1 - 1);
+    }
     T.e0 = e0;
     T.cnt = e1 - e0 + 1;
   }
@@ -283,7 +315,7 @@ __global__ void __launch_bounds__(256) main_cover_kernel(RArgs a, int which) {
   const bool tree = a.approach == APPROACH_TREE;
   for (uint64_t t0 = (uint64_t)blockIdx.x * kExpandTile; t0 < total; t0 += (uint64_t)gridDim.x * kExpandTile) {
     const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
-    expand_stage(T, excl, n, t0, t1);
+    expand_stage(T, excl, n, t0, t1, which ? a.bnd1 : a.bnd0, a.max_tiles);
     for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
       const uint32_t i = expand_entry(T, excl, n, t);
       const uint32_t j = (uint32_t)(t - excl[i]);
@@ -373,16 +405,31 @@ __device__ __forceinline__ int fo_leaf_ranges(uint32_t u, uint32_t N, uint32_t M
   return n;
 }
 
+// Per chain FO entry, once: the (at most two) leaf ranges its distinct map
+// covers, or for the list and basic approaches its one chunk.
+__global__ void chain_ranges_kernel(RArgs a, uint32_t n) {
+  const bool tree = a.approach == APPROACH_TREE;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t g = a.di[1].fo_begin + k;  // chain entries follow the main ones
+    uint4 r = make_uint4(0, 0, 0, 0);
+    if (tree) {
+      uint32_t lo[2], hi[2];
+      const int nr = fo_leaf_ranges(a.fo_node[g], a.N, a.M, lo, hi);
+      if (nr > 0) { r.x = lo[0]; r.y = hi[0] - lo[0] + 1; }
+      if (nr > 1) { r.z = lo[1]; r.w = hi[1] - lo[1] + 1; }
+    } else {
+      r.x = a.fo_node[g];
+      r.y = 1;
+    }
+    a.fo_rng[g] = r;
+  }
+}
+
 struct ChainDmCount {
   RArgs a;
   __device__ __forceinline__ uint64_t operator()(uint64_t k) const {
-    const uint64_t g = a.di[1].fo_begin + k;  // chain entries follow the main ones
-    if (a.approach != APPROACH_TREE) return 1;
-    uint32_t lo[2], hi[2];
-    int n = fo_leaf_ranges(a.fo_node[g], a.N, a.M, lo, hi);
-    uint64_t c = 0;
-    for (int r = 0; r < n; r++) c += hi[r] - lo[r] + 1;
-    return c;
+    const uint4 r = a.fo_rng[a.di[1].fo_begin + k];
+    return (uint64_t)r.y + r.w;
   }
 };
 struct ChainRmCount {
@@ -414,7 +461,7 @@ __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a, int pass, in
   const bool tree = a.approach == APPROACH_TREE;
   for (uint64_t t0 = (uint64_t)blockIdx.x * kExpandTile; t0 < total; t0 += (uint64_t)gridDim.x * kExpandTile) {
     const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
-    expand_stage(T, excl, n, t0, t1);
+    expand_stage(T, excl, n, t0, t1, which ? a.bnd1 : a.bnd0, a.max_tiles);
     for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
       const uint32_t k = expand_entry(T, excl, n, t);
       uint64_t j = t - excl[k];
@@ -423,18 +470,12 @@ __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a, int pass, in
         const uint64_t g = a.di[1].fo_begin + k;  // chain entries follow the main ones
         s = a.fo_seg[g] - 1;
         rank = (uint32_t)g - a.di[1 + s].fo_begin;
+        const uint4 r = a.fo_rng[g];
         if (tree) {
-          uint32_t lo[2], hi[2];
-          const int nr = fo_leaf_ranges(a.fo_node[g], a.N, a.M, lo, hi);
-          uint32_t x = 0;
-          for (int r = 0; r < nr; r++) {
-            const uint64_t sz = hi[r] - lo[r] + 1;
-            if (j < sz) { x = lo[r] + (uint32_t)j; break; }
-            j -= sz;
-          }
+          const uint32_t x = j < r.y ? r.x + (uint32_t)j : r.z + (uint32_t)(j - r.y);
           key = key_of_leaf(a, x);
         } else {
-          key = a.fo_node[g];
+          key = r.x;
           if (key >= a.N) continue;
         }
       } else {
@@ -598,12 +639,17 @@ struct RestartScratch {
   DevBuf<uint32_t> fo_node, fo_seg, fo_clen, sh_node, sh_prev, sh_tree, sh_seg, rrs, fo_at, dm_tab, rm_tab, dm_mask,
       rm_mask;
   DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl, res, nl_rank, cp_rank, dm_excl, rm_excl, tot, scan, scan_total;
+  DevBuf<uint4> fo_rng;
+  DevBuf<uint2> bnd0, bnd1;
 };
 
 void destroy_restart_scratch(RestartScratch* r) { delete r; }
 
 static void set_scratch_pool(RestartScratch* r, cudaMemPool_t pool) {
   r->di.pool = pool;
+  r->fo_rng.pool = pool;
+  r->bnd0.pool = pool;
+  r->bnd1.pool = pool;
   for (auto* b : {&r->fo_node, &r->fo_seg, &r->fo_clen, &r->sh_node, &r->sh_prev, &r->sh_tree, &r->sh_seg, &r->rrs,
                   &r->fo_at, &r->dm_tab, &r->rm_tab, &r->dm_mask, &r->rm_mask})
     b->pool = pool;
@@ -712,6 +758,12 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(cudaMemcpyAsync(R.di.p, di.data(), sizeof(DiffInfo) * di.size(), cudaMemcpyHostToDevice, s));
   MTC_CUDA_R(R.fo_node.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_seg.ensure(nfo + 1, s));
+  MTC_CUDA_R(R.fo_rng.ensure(nfo + 1, s));
+  // expansion tiles: a chain step covers at most every leaf of its tree twice
+  const uint64_t max_items = (uint64_t)(nsteps + 2) * 2ull * M + nfo + nsh + 16;
+  const uint32_t max_tiles = (uint32_t)std::min<uint64_t>(max_items / kExpandTile + 2, 1u << 26);
+  MTC_CUDA_R(R.bnd0.ensure(max_tiles, s));
+  MTC_CUDA_R(R.bnd1.ensure(max_tiles, s));
   MTC_CUDA_R(R.fo_clen.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_excl.ensure(nfo + 1, s));
   MTC_CUDA_R(R.sh_node.ensure(nsh + 1, s));
@@ -753,6 +805,10 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   a.fo_at = R.fo_at.p;
   a.dm_tab = R.dm_tab.p; a.rm_tab = R.rm_tab.p; a.dm_mask = R.dm_mask.p; a.rm_mask = R.rm_mask.p;
   a.dm_excl = R.dm_excl.p; a.rm_excl = R.rm_excl.p; a.tot = R.tot.p;
+  a.fo_rng = R.fo_rng.p;
+  a.bnd0 = R.bnd0.p;
+  a.bnd1 = R.bnd1.p;
+  a.max_tiles = max_tiles;
   a.out = dev_out; a.err = err_.p;
   const bool tree = approach == APPROACH_TREE;
 
@@ -784,6 +840,14 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     MTC_CUDA_R(grid_scan(MainShiftLen{R.sh_prev.p, M, tree ? 1 : 0}, StoreExcl{R.sh_excl.p}, nullptr, di[0].S,
                          R.scan.p, R.tot.p + 3, s));
   }
+  if (di[0].F) {
+    expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.fo_excl.p, di[0].F, R.tot.p + 2, R.bnd0.p, a.max_tiles);
+    note_launch();
+  }
+  if (di[0].S) {
+    expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.sh_excl.p, di[0].S, R.tot.p + 3, R.bnd1.p, a.max_tiles);
+    note_launch();
+  }
   main_cover_kernel<<<num_sms() * 4, 256, 0, s>>>(a, 0);
   main_cover_kernel<<<num_sms() * 4, 256, 0, s>>>(a, 1);
   main_resolve_kernel<<<gsz(N), 256, 0, s>>>(a);
@@ -793,12 +857,27 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     MTC_CUDA_R(cudaMemsetAsync(R.dm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
     MTC_CUDA_R(cudaMemsetAsync(R.rm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
     const uint32_t nfo_chain = nfo - di[1].fo_begin, nsh_chain = nsh - di[1].sh_begin;
+    if (nfo_chain) {
+      chain_ranges_kernel<<<gsz(nfo_chain), 256, 0, s>>>(a, nfo_chain);
+      note_launch();
+    }
     if (nfo_chain)
       MTC_CUDA_R(grid_scan(ChainDmCount{a}, StoreExcl{R.dm_excl.p}, nullptr, nfo_chain, R.scan.p, R.tot.p + 0, s));
     if (nsh_chain && !basic)
       MTC_CUDA_R(grid_scan(ChainRmCount{a}, StoreExcl{R.rm_excl.p}, nullptr, nsh_chain, R.scan.p, R.tot.p + 1, s));
-    for (int pass = 0; pass < 2; pass++)
-      for (int which = 0; which < 2; which++)
+    if (nfo_chain) {
+      expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.dm_excl.p, nfo_chain, R.tot.p + 0, R.bnd0.p,
+                                                         a.max_tiles);
+      note_launch();
+    }
+    if (nsh_chain && !basic) {
+      expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.rm_excl.p, nsh_chain, R.tot.p + 1, R.bnd1.p,
+                                                         a.max_tiles);
+      note_launch();
+    }
+    // per table: every cell initialised (pass 0) before the lowest rank wins (pass 1)
+    for (int which = 0; which < 2; which++)
+      for (int pass = 0; pass < 2; pass++)
         chain_tables_kernel<<<num_sms() * 4, 256, 0, s>>>(a, pass, which);
     walk_kernel<<<gsz(N), 256, 0, s>>>(a);
     note_launch(5);

@@ -31,3 +31,14 @@ def test_cpp_api_on_gpu(mtc, tmp_path):
     r = subprocess.run([exe], input=stdin, text=True, capture_output=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 failures" in r.stdout
+
+
+def test_leaf_range_closed_form_equals_reference_loop(tmp_path):
+    # host-only program over the kernels' own header: no GPU needed
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = os.path.join(ROOT, "tests", "cpp", "leaf_range_test.cu")
+    exe = str(tmp_path / "leaf_range_test")
+    subprocess.check_call([nvcc, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                           "-I", os.path.join(ROOT, "mtcheck_gb300", "csrc"), src, "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0 and out.stdout.startswith("ok"), out.stdout
