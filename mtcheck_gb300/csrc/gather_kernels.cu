@@ -45,6 +45,79 @@ __device__ __forceinline__ uint8_t child_flag(uint8_t lab) {
 // baseline variant that tests the not-yet-hashed digest and then hashes and
 // inserts every interior node (:155-227).
 constexpr uint32_t kSpanLevels = 9;  // 256 nodes on the bottom level of a span
+
+// One interior node n of a forest pass, given its children's labels: the
+// hashing, map insert or lookup and children's root flags of the reference's
+// level loops (first-occurrence forest src/tree_approach.cpp:378-404,
+// duplicate forest :413-477, baseline :124-227).  Writes and returns n's label.
+// Writes n's label only when `store` is set (a span's top level, read by the
+// next launch, or the baseline); only flags other than ROOT_NONE are written,
+// the flag array being cleared before the duplicate pass.
+__device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, int baseline, uint64_t n, uint8_t ll,
+                                               uint8_t lr, uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all,
+                                               bool store) {
+  const uint32_t l = 2 * (uint32_t)n + 1, rr = l + 1;
+  uint8_t lab_n;
+  if (pass == 0) {
+    if (ll == FIRST_OCUR && lr == FIRST_OCUR) {
+      lab_n = FIRST_OCUR;
+      Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
+      st_digest(a.tree + n, dg);
+      map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_fo, a.err);
+    } else {
+      lab_n = DONE;
+    }
+  } else {
+    uint8_t fl = ROOT_NONE, fr = ROOT_NONE;
+    if (ll != lr) {
+      lab_n = DONE;
+      fl = child_flag(ll);
+      fr = child_flag(lr);
+    } else if (ll == FIXED_DUPL) {
+      lab_n = FIXED_DUPL;
+    } else if (ll == SHIFT_DUPL) {
+      Digest dg;
+      if (baseline) {
+        dg = ld_digest(a.tree + n);
+      } else {
+        dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
+        st_digest(a.tree + n, dg);
+      }
+      if (map_find(a.map, dg, a.err) >= 0) {
+        lab_n = SHIFT_DUPL;
+      } else {
+        lab_n = DONE;
+        fl = ROOT_SHIFT;
+        fr = ROOT_SHIFT;
+      }
+    } else {
+      lab_n = ll == FIRST_OCUR ? FIRST_OCUR : DONE;  // both first occurrences, or both done
+    }
+    if (fl != ROOT_NONE) a.rflag[canon_pos(a, l)] = fl;
+    if (fr != ROOT_NONE) a.rflag[canon_pos(a, rr)] = fr;
+    if (baseline) {
+      Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
+      st_digest(a.tree + n, dg);
+      map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_all, a.err);
+    }
+  }
+  if (store) a.labels[n] = lab_n;
+  return lab_n;
+}
+
+// Label of node n at a level of a span: final for a leaf (or DONE past the
+// end), otherwise computed from the children's labels.
+__device__ __forceinline__ uint8_t forest_label(const ForestArgs& a, int pass, int baseline, uint64_t n,
+                                                uint64_t last_interior, uint64_t M, uint8_t ll, uint8_t lr,
+                                                uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all, bool store) {
+  if (n > last_interior) return n < M ? a.labels[n] : DONE;
+  return forest_node(a, pass, baseline, n, ll, lr, cur_id, epoch_fo, epoch_all, store);
+}
+
+// Levels d_bot .. d_top of the subtree rooted at depth d_top, node labels in
+// shared memory, one barrier per level.  Serves every span shape, and the
+// baseline's duplicate pass, whose shift test must see every insert of the
+// levels below it.
 __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass, int baseline, uint32_t N,
                                                           uint32_t d_top, uint32_t d_bot) {
   __shared__ uint8_t lab[2][2 << (kSpanLevels - 1)];
@@ -66,65 +139,71 @@ __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass
   for (int d = (int)d_bot; d >= (int)d_top; d--) {
     const uint32_t width = 1u << (d - d_top);
     const uint64_t first = (r + 1) * width - 1;
-    for (uint32_t i = threadIdx.x; i < width; i += blockDim.x) {
-      const uint64_t n = first + i;
-      if (n > last_interior) {  // a leaf (or past the end): its label is final
-        cur[i] = n < M ? a.labels[n] : DONE;
-        continue;
-      }
-      const uint32_t l = 2 * (uint32_t)n + 1, rr = l + 1;
-      const uint8_t ll = child[2 * i], lr = child[2 * i + 1];
-      uint8_t lab_n;
-      if (pass == 0) {
-        if (ll == FIRST_OCUR && lr == FIRST_OCUR) {
-          lab_n = FIRST_OCUR;
-          Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
-          st_digest(a.tree + n, dg);
-          map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_fo, a.err);
-        } else {
-          lab_n = DONE;
-        }
-      } else {
-        uint8_t fl = ROOT_NONE, fr = ROOT_NONE;
-        if (ll != lr) {
-          lab_n = DONE;
-          fl = child_flag(ll);
-          fr = child_flag(lr);
-        } else if (ll == FIXED_DUPL) {
-          lab_n = FIXED_DUPL;
-        } else if (ll == SHIFT_DUPL) {
-          Digest dg;
-          if (baseline) {
-            dg = ld_digest(a.tree + n);
-          } else {
-            dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
-            st_digest(a.tree + n, dg);
-          }
-          if (map_find(a.map, dg, a.err) >= 0) {
-            lab_n = SHIFT_DUPL;
-          } else {
-            lab_n = DONE;
-            fl = ROOT_SHIFT;
-            fr = ROOT_SHIFT;
-          }
-        } else {
-          lab_n = ll == FIRST_OCUR ? FIRST_OCUR : DONE;  // both first occurrences, or both done
-        }
-        a.rflag[canon_pos(a, l)] = fl;
-        a.rflag[canon_pos(a, rr)] = fr;
-        if (baseline) {
-          Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
-          st_digest(a.tree + n, dg);
-          map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_all, a.err);
-        }
-      }
-      cur[i] = lab_n;
-      a.labels[n] = lab_n;
-    }
+    for (uint32_t i = threadIdx.x; i < width; i += blockDim.x)
+      cur[i] = forest_label(a, pass, baseline, first + i, last_interior, M, child[2 * i], child[2 * i + 1], cur_id,
+                            epoch_fo, epoch_all, baseline || d == (int)d_top);
     __syncthreads();
     uint8_t* t = child;
     child = cur;
     cur = t;
+  }
+}
+
+// A full span of 9 levels (256 nodes on its bottom level) for the incremental
+// passes: each warp carries 32 nodes up 6 levels in registers (children's
+// labels by shuffle), then warp 0 finishes the last 3 levels from the 8
+// warps' labels -- one block barrier instead of nine.  The incremental passes
+// never look up a digest inserted by the same launch (the first-occurrence
+// pass only inserts, the duplicate pass only looks up), so the order of the
+// warps does not matter; the digests of children computed by other lanes are
+// ordered by __syncwarp / __syncthreads.
+__global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
+  __shared__ uint8_t top8[8];
+  const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1, epoch_all = a.sp->epoch + 2;
+  const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
+  const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
+  if (r > last_interior) return;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr unsigned kFull = 0xffffffffu;
+  // bottom level: 256 nodes, children read from memory
+  uint8_t lab;
+  {
+    const uint64_t n = (r + 1) * 256 - 1 + warp * 32 + lane;
+    uint8_t ll = DONE, lr = DONE;
+    if (n <= last_interior) {
+      const uint64_t c = 2 * n + 1;
+      ll = c < M ? a.labels[c] : DONE;
+      lr = c + 1 < M ? a.labels[c + 1] : DONE;
+    }
+    lab = forest_label(a, pass, 0, n, last_interior, M, ll, lr, cur_id, epoch_fo, epoch_all, false);
+  }
+  // five levels inside the warp: 16, 8, 4, 2, 1 nodes
+#pragma unroll
+  for (uint32_t step = 1; step <= 5; step++) {
+    __syncwarp();
+    const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, (2 * lane) & 31);
+    const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, (2 * lane + 1) & 31);
+    const uint32_t width = 32u >> step;
+    if (lane < width) {
+      const uint64_t n = (r + 1) * (256u >> step) - 1 + warp * width + lane;
+      lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, false);
+    }
+  }
+  if (lane == 0) top8[warp] = lab;
+  __syncthreads();
+  if (warp != 0) return;
+  lab = lane < 8 ? top8[lane] : DONE;
+  // three levels in warp 0: 4, 2, 1 nodes
+#pragma unroll
+  for (uint32_t step = 6; step <= 8; step++) {
+    __syncwarp();
+    const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, (2 * lane) & 31);
+    const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, (2 * lane + 1) & 31);
+    const uint32_t width = 256u >> step;
+    if (lane < width) {
+      const uint64_t n = (r + 1) * width - 1 + lane;
+      lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, step == 8);
+    }
   }
 }
 
@@ -586,6 +665,12 @@ cudaError_t launch_map_rehash(const DigestMap& from, uint64_t from_cap, const Di
 // ---------------------------------------------------------------------------
 cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, cudaStream_t s) {
   if (N < 2) return cudaSuccess;
+  // the duplicate pass writes only the flags of roots; every other position
+  // (node 1 .. M-1 in canonical order) reads ROOT_NONE
+  if (pass == 1) {
+    cudaError_t e = cudaMemsetAsync(a.rflag, ROOT_NONE, 2ull * N - 2, s);
+    if (e != cudaSuccess) return e;
+  }
   // deepest interior depth: that of node N-2
   uint32_t dmax = 0;
   while (((2ull << dmax) - 1) <= (uint64_t)(N - 2)) dmax++;
@@ -593,7 +678,10 @@ cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t 
     const uint32_t top = bot >= (int)kSpanLevels - 1 ? (uint32_t)bot - (kSpanLevels - 1) : 0;
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
-    forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot);
+    if (!baseline && (uint32_t)bot - top == kSpanLevels - 1)
+      forest_span9_warp_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+    else
+      forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot);
     note_launch();
     if (top == 0) break;
   }
