@@ -50,12 +50,21 @@ constexpr uint32_t kSpanLevels = 9;  // 256 nodes on the bottom level of a span
 // hashing, map insert or lookup and children's root flags of the reference's
 // level loops (first-occurrence forest src/tree_approach.cpp:378-404,
 // duplicate forest :413-477, baseline :124-227).  Writes and returns n's label.
+// First-occurrence inserts collected by a span block and issued after its
+// last level (the first-occurrence pass never looks an entry up, and the
+// serial-order rule of map_insert_serial does not depend on arrival order).
+struct InsertSink {
+  Digest dg[511];
+  uint32_t node[511];
+  uint32_t n;
+};
+
 // Writes n's label only when `store` is set (a span's top level, read by the
 // next launch, or the baseline); only flags other than ROOT_NONE are written,
 // the flag array being cleared before the duplicate pass.
 __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, int baseline, uint64_t n, uint8_t ll,
                                                uint8_t lr, uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all,
-                                               bool store) {
+                                               bool store, InsertSink* sink = nullptr) {
   const uint32_t l = 2 * (uint32_t)n + 1, rr = l + 1;
   uint8_t lab_n;
   if (pass == 0) {
@@ -63,7 +72,13 @@ __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, in
       lab_n = FIRST_OCUR;
       Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
       st_digest(a.tree + n, dg);
-      map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_fo, a.err);
+      if (sink) {
+        const uint32_t k = atomicAdd(&sink->n, 1u);
+        sink->dg[k] = dg;
+        sink->node[k] = (uint32_t)n;
+      } else {
+        map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_fo, a.err);
+      }
     } else {
       lab_n = DONE;
     }
@@ -109,9 +124,10 @@ __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, in
 // end), otherwise computed from the children's labels.
 __device__ __forceinline__ uint8_t forest_label(const ForestArgs& a, int pass, int baseline, uint64_t n,
                                                 uint64_t last_interior, uint64_t M, uint8_t ll, uint8_t lr,
-                                                uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all, bool store) {
+                                                uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all, bool store,
+                                                InsertSink* sink = nullptr) {
   if (n > last_interior) return n < M ? a.labels[n] : DONE;
-  return forest_node(a, pass, baseline, n, ll, lr, cur_id, epoch_fo, epoch_all, store);
+  return forest_node(a, pass, baseline, n, ll, lr, cur_id, epoch_fo, epoch_all, store, sink);
 }
 
 // Levels d_bot .. d_top of the subtree rooted at depth d_top, node labels in
@@ -159,10 +175,14 @@ __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass
 // ordered by __syncwarp / __syncthreads.
 __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
   __shared__ uint8_t top8[8];
+  __shared__ InsertSink sink_mem;
   const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1, epoch_all = a.sp->epoch + 2;
   const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
   const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
   if (r > last_interior) return;
+  InsertSink* sink = pass == 0 ? &sink_mem : nullptr;
+  if (threadIdx.x == 0) sink_mem.n = 0;
+  __syncthreads();
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr unsigned kFull = 0xffffffffu;
   // bottom level: 256 nodes, children read from memory
@@ -175,7 +195,7 @@ __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, in
       ll = c < M ? a.labels[c] : DONE;
       lr = c + 1 < M ? a.labels[c + 1] : DONE;
     }
-    lab = forest_label(a, pass, 0, n, last_interior, M, ll, lr, cur_id, epoch_fo, epoch_all, false);
+    lab = forest_label(a, pass, 0, n, last_interior, M, ll, lr, cur_id, epoch_fo, epoch_all, false, sink);
   }
   // five levels inside the warp: 16, 8, 4, 2, 1 nodes
 #pragma unroll
@@ -186,25 +206,32 @@ __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, in
     const uint32_t width = 32u >> step;
     if (lane < width) {
       const uint64_t n = (r + 1) * (256u >> step) - 1 + warp * width + lane;
-      lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, false);
+      lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, false, sink);
     }
   }
   if (lane == 0) top8[warp] = lab;
   __syncthreads();
-  if (warp != 0) return;
-  lab = lane < 8 ? top8[lane] : DONE;
-  // three levels in warp 0: 4, 2, 1 nodes
+  if (warp == 0) {
+    lab = lane < 8 ? top8[lane] : DONE;
+    // three levels in warp 0: 4, 2, 1 nodes
 #pragma unroll
-  for (uint32_t step = 6; step <= 8; step++) {
-    __syncwarp();
-    const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, (2 * lane) & 31);
-    const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, (2 * lane + 1) & 31);
-    const uint32_t width = 256u >> step;
-    if (lane < width) {
-      const uint64_t n = (r + 1) * width - 1 + lane;
-      lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, step == 8);
+    for (uint32_t step = 6; step <= 8; step++) {
+      __syncwarp();
+      const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, (2 * lane) & 31);
+      const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, (2 * lane + 1) & 31);
+      const uint32_t width = 256u >> step;
+      if (lane < width) {
+        const uint64_t n = (r + 1) * width - 1 + lane;
+        lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, step == 8, sink);
+      }
     }
   }
+  if (pass != 0) return;
+  // the collected first-occurrence inserts, all threads at once
+  __syncthreads();
+  const uint32_t cnt = sink_mem.n;
+  for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x)
+    map_insert_serial(a.map, sink_mem.dg[k], sink_mem.node[k], cur_id, epoch_fo, a.err);
 }
 
 // ---------------------------------------------------------------------------
