@@ -121,7 +121,7 @@ int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
     MTC_CUDA(rflag_.ensure(tree ? M : 1, stream_));
     MTC_CUDA(chunk_slot_.ensure(N, stream_));
     MTC_CUDA(changed_list_.ensure(N, stream_));
-    MTC_CUDA(changed_count_.ensure(1, stream_));
+    MTC_CUDA(changed_count_.ensure(3, stream_));  // [changed chunks, leaves demoted, forest inserts]
     MTC_CUDA(map_size_.ensure(1, stream_));
     MTC_CUDA(err_.ensure(1, stream_));
     MTC_CUDA(fo_list_.ensure(N + 1, stream_));
@@ -206,7 +206,8 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.epi = EPI_TREE;
   la.changed_list = changed_list_.p;
   la.changed_count = changed_count_.p;
-  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, sizeof(uint32_t), stream_));
+  la.demoted = changed_count_.p + 1;
+  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 2 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   MTC_CUDA(launch_leaf_inserts(la, stream_));
@@ -223,6 +224,13 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   fa.D = 0;
   while (((2ull << fa.D) - 1) <= (uint64_t)(M - 1)) fa.D++;  // depth of node M-1
   fa.sizeD = (uint64_t)M - ((1ull << fa.D) - 1);
+  // an incremental checkpoint without demoted leaves runs both passes in one
+  // traversal (the launches of the duplicate pass then return at once)
+  fa.fuse_gate = baseline_path ? nullptr : la.demoted;
+  // the changed-chunk list is free once the leaf inserts are done: it queues
+  // the forest's first-occurrence inserts
+  fa.ins_queue = changed_list_.p;
+  fa.ins_count = changed_count_.p + 2;
   MTC_CUDA(launch_forest(fa, 0, 0, N, stream_));                         // first-occurrence forest
   MTC_CUDA(launch_forest(fa, 1, baseline_path ? 1 : 0, N, stream_));  // duplicate forest
   MTC_CUDA(launch_root_compaction(fa, N, M, fo_list_.p, sh_list_.p, lay_.p, scan_.p, scan_total_.p, stream_));

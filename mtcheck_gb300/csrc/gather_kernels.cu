@@ -38,47 +38,54 @@ __device__ __forceinline__ uint8_t child_flag(uint8_t lab) {
 
 // Several levels per launch: CTA b owns the subtree of interior node
 // r = 2^d_top - 1 + b and computes its interior nodes from depth d_bot up to
-// d_top.  The labels of one level stay in shared memory for the next; only
-// the bottom children, leaves met on the way, digests and the results touch
-// global memory.  pass 0: first-occurrence forest (src/tree_approach.cpp
-// :378-404); pass 1: duplicate forest (:413-477), with baseline != 0 the
-// baseline variant that tests the not-yet-hashed digest and then hashes and
-// inserts every interior node (:155-227).
-constexpr uint32_t kSpanLevels = 9;  // 256 nodes on the bottom level of a span
+// d_top.  Only the bottom children, leaves met on the way, digests and the
+// results touch global memory.  pass 0: first-occurrence forest
+// (src/tree_approach.cpp:378-404); pass 1: duplicate forest (:413-477), with
+// baseline != 0 the baseline variant that tests the not-yet-hashed digest and
+// then hashes and inserts every interior node (:155-227); pass 2: both
+// incremental passes in one traversal (ForestArgs::fuse_gate).
+constexpr uint32_t kSpanLevels = 9;     // 256 nodes on the bottom level of a span
+constexpr uint32_t kBottomLevels = 12;  // bottom span: 16 leaves per thread, 4096 per block
+constexpr uint32_t kFixed4 = 0x01010101u * FIXED_DUPL;
+
+// First-occurrence inserts are queued (node ids in ForestArgs::ins_queue) and
+// issued by forest_insert_kernel after the pass's last launch: the
+// first-occurrence pass never looks an entry up, the fused pass looks up only
+// digests that no queued insert can equal, and the serial-order rule of
+// map_insert_serial does not depend on arrival order.  A span block collects
+// its ids in shared memory and appends them with one atomic.
+struct IdSink {
+  uint32_t* ids;  // shared memory
+  uint32_t* n;    // shared counter
+};
+__device__ __forceinline__ void queue_insert(const ForestArgs& a, IdSink* sink, uint32_t n) {
+  if (sink) sink->ids[atomicAdd(sink->n, 1u)] = n;
+  else a.ins_queue[atomicAdd(a.ins_count, 1u)] = n;
+}
+__device__ __forceinline__ void flush_sink(const ForestArgs& a, const IdSink& sink, uint32_t* base) {
+  __syncthreads();
+  const uint32_t cnt = *sink.n;
+  if (cnt == 0) return;
+  if (threadIdx.x == 0) *base = atomicAdd(a.ins_count, cnt);
+  __syncthreads();
+  const uint32_t b = *base;
+  for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) a.ins_queue[b + k] = sink.ids[k];
+}
 
 // One interior node n of a forest pass, given its children's labels: the
 // hashing, map insert or lookup and children's root flags of the reference's
-// level loops (first-occurrence forest src/tree_approach.cpp:378-404,
-// duplicate forest :413-477, baseline :124-227).  Writes and returns n's label.
-// First-occurrence inserts collected by a span block and issued after its
-// last level (the first-occurrence pass never looks an entry up, and the
-// serial-order rule of map_insert_serial does not depend on arrival order).
-struct InsertSink {
-  Digest dg[511];
-  uint32_t node[511];
-  uint32_t n;
-};
-
-// Writes n's label only when `store` is set (a span's top level, read by the
-// next launch, or the baseline); only flags other than ROOT_NONE are written,
-// the flag array being cleared before the duplicate pass.
+// level loops.  Writes n's label only when `store` is set (a span's top
+// level, read by the next launch, or the baseline); only flags other than
+// ROOT_NONE are written, the flag array being cleared before the first pass.
 __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, int baseline, uint64_t n, uint8_t ll,
-                                               uint8_t lr, uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all,
-                                               bool store, InsertSink* sink = nullptr) {
+                                               uint8_t lr, uint32_t cur_id, uint32_t epoch_all, bool store) {
   const uint32_t l = 2 * (uint32_t)n + 1, rr = l + 1;
   uint8_t lab_n;
   if (pass == 0) {
     if (ll == FIRST_OCUR && lr == FIRST_OCUR) {
       lab_n = FIRST_OCUR;
-      Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
-      st_digest(a.tree + n, dg);
-      if (sink) {
-        const uint32_t k = atomicAdd(&sink->n, 1u);
-        sink->dg[k] = dg;
-        sink->node[k] = (uint32_t)n;
-      } else {
-        map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_fo, a.err);
-      }
+      st_digest(a.tree + n, hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr)));
+      queue_insert(a, nullptr, (uint32_t)n);
     } else {
       lab_n = DONE;
     }
@@ -105,8 +112,14 @@ __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, in
         fl = ROOT_SHIFT;
         fr = ROOT_SHIFT;
       }
+    } else if (ll == FIRST_OCUR) {
+      lab_n = FIRST_OCUR;
+      if (pass == 2) {
+        st_digest(a.tree + n, hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr)));
+        queue_insert(a, nullptr, (uint32_t)n);
+      }
     } else {
-      lab_n = ll == FIRST_OCUR ? FIRST_OCUR : DONE;  // both first occurrences, or both done
+      lab_n = DONE;  // both first duplicates, or both done
     }
     if (fl != ROOT_NONE) a.rflag[canon_pos(a, l)] = fl;
     if (fr != ROOT_NONE) a.rflag[canon_pos(a, rr)] = fr;
@@ -124,10 +137,17 @@ __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, in
 // end), otherwise computed from the children's labels.
 __device__ __forceinline__ uint8_t forest_label(const ForestArgs& a, int pass, int baseline, uint64_t n,
                                                 uint64_t last_interior, uint64_t M, uint8_t ll, uint8_t lr,
-                                                uint32_t cur_id, uint32_t epoch_fo, uint32_t epoch_all, bool store,
-                                                InsertSink* sink = nullptr) {
+                                                uint32_t cur_id, uint32_t epoch_all, bool store) {
   if (n > last_interior) return n < M ? a.labels[n] : DONE;
-  return forest_node(a, pass, baseline, n, ll, lr, cur_id, epoch_fo, epoch_all, store, sink);
+  return forest_node(a, pass, baseline, n, ll, lr, cur_id, epoch_all, store);
+}
+
+// Resolves the pass of an incremental launch: with the fuse gate open the
+// first-occurrence launch runs both passes (2) and the duplicate launch has
+// nothing left to do (-1).
+__device__ __forceinline__ int resolve_pass(const ForestArgs& a, int pass) {
+  if (a.fuse_gate && *a.fuse_gate == 0) return pass == 1 ? -1 : 2;
+  return pass;
 }
 
 // Levels d_bot .. d_top of the subtree rooted at depth d_top, node labels in
@@ -137,7 +157,9 @@ __device__ __forceinline__ uint8_t forest_label(const ForestArgs& a, int pass, i
 __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass, int baseline, uint32_t N,
                                                           uint32_t d_top, uint32_t d_bot) {
   __shared__ uint8_t lab[2][2 << (kSpanLevels - 1)];
-  const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1, epoch_all = a.sp->epoch + 2;
+  pass = resolve_pass(a, pass);
+  if (pass < 0) return;
+  const uint32_t cur_id = a.sp->cur, epoch_all = a.sp->epoch + 2;
   const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
   const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
   if (r > last_interior) return;
@@ -157,7 +179,7 @@ __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass
     const uint64_t first = (r + 1) * width - 1;
     for (uint32_t i = threadIdx.x; i < width; i += blockDim.x)
       cur[i] = forest_label(a, pass, baseline, first + i, last_interior, M, child[2 * i], child[2 * i + 1], cur_id,
-                            epoch_fo, epoch_all, baseline || d == (int)d_top);
+                            epoch_all, baseline || d == (int)d_top);
     __syncthreads();
     uint8_t* t = child;
     child = cur;
@@ -165,73 +187,267 @@ __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass
   }
 }
 
+// Whether a node's digest is read by its parent in a pass: first-occurrence
+// pairs are hashed in the first pass, shifted-duplicate pairs in the second,
+// both in the fused pass 2.
+__device__ __forceinline__ bool digest_wanted(int pass, uint8_t lab) {
+  return pass == 0 ? lab == FIRST_OCUR : pass == 1 ? lab == SHIFT_DUPL : (lab == FIRST_OCUR || lab == SHIFT_DUPL);
+}
+
+// One interior node n of an incremental pass (first-occurrence forest
+// src/tree_approach.cpp:378-404, duplicate forest :413-477, or both: pass 2)
+// given its children's labels and digests; `dg` receives n's digest when n is
+// hashed.  First-occurrence inserts go to the block's sink.
+__device__ __forceinline__ uint8_t span_node(const ForestArgs& a, int pass, uint32_t n, uint8_t ll, uint8_t lr,
+                                             const Digest& dl, const Digest& dr, Digest& dg, bool store,
+                                             IdSink* sink) {
+  const uint32_t l = 2 * n + 1, rr = l + 1;
+  uint8_t lab_n;
+  if (pass == 0) {
+    if (ll == FIRST_OCUR && lr == FIRST_OCUR) {
+      lab_n = FIRST_OCUR;
+      dg = hash_pair(a.hash_kind, dl, dr);
+      st_digest(a.tree + n, dg);
+      queue_insert(a, sink, n);
+    } else {
+      lab_n = DONE;
+    }
+  } else {
+    uint8_t fl = ROOT_NONE, fr = ROOT_NONE;
+    if (ll != lr) {
+      lab_n = DONE;
+      fl = child_flag(ll);
+      fr = child_flag(lr);
+    } else if (ll == FIXED_DUPL) {
+      lab_n = FIXED_DUPL;
+    } else if (ll == SHIFT_DUPL) {
+      dg = hash_pair(a.hash_kind, dl, dr);
+      st_digest(a.tree + n, dg);
+      if (map_find(a.map, dg, a.err) >= 0) {
+        lab_n = SHIFT_DUPL;
+      } else {
+        lab_n = DONE;
+        fl = ROOT_SHIFT;
+        fr = ROOT_SHIFT;
+      }
+    } else if (ll == FIRST_OCUR) {
+      lab_n = FIRST_OCUR;
+      if (pass == 2) {
+        dg = hash_pair(a.hash_kind, dl, dr);
+        st_digest(a.tree + n, dg);
+        queue_insert(a, sink, n);
+      }
+    } else {
+      lab_n = DONE;  // both first duplicates, or both done
+    }
+    if (fl != ROOT_NONE) a.rflag[canon_pos(a, l)] = fl;
+    if (fr != ROOT_NONE) a.rflag[canon_pos(a, rr)] = fr;
+  }
+  if (store) a.labels[n] = lab_n;
+  return lab_n;
+}
+
+// Node n on the deepest interior level: a leaf there (a ragged last level)
+// keeps its label and stored digest; an interior node is computed.
+__device__ __forceinline__ uint8_t span_label(const ForestArgs& a, int pass, uint64_t n, uint64_t last_interior,
+                                              uint64_t M, uint8_t ll, uint8_t lr, const Digest& dl,
+                                              const Digest& dr, Digest& dg, IdSink* sink) {
+  if (n > last_interior) {
+    const uint8_t lab = n < M ? a.labels[n] : DONE;
+    if (digest_wanted(pass, lab)) dg = ld_digest(a.tree + n);
+    return lab;
+  }
+  return span_node(a, pass, (uint32_t)n, ll, lr, dl, dr, dg, false, sink);
+}
+
+__device__ __forceinline__ Digest shfl_digest(const Digest& d, int src) {
+  constexpr unsigned kFull = 0xffffffffu;
+  return Digest{{__shfl_sync(kFull, d.w[0], src), __shfl_sync(kFull, d.w[1], src), __shfl_sync(kFull, d.w[2], src),
+                 __shfl_sync(kFull, d.w[3], src)}};
+}
+
+// The eight upper levels of a span below node r, from one node per thread
+// (relative depth 8, node (r+1)*256-1+threadIdx.x, label `lab`, digest `dg`):
+// five inside each warp (children's labels and digests by shuffle), then
+// three in warp 0 from the eight warps' results.  Stores r's label.  Every
+// node here is interior.
+__device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint64_t r, uint8_t lab, Digest dg,
+                                             IdSink* sink, uint8_t* top8, Digest* topdg) {
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr unsigned kFull = 0xffffffffu;
+#pragma unroll
+  for (uint32_t step = 1; step <= 5; step++) {
+    const int sl = (2 * lane) & 31, sr = (2 * lane + 1) & 31;
+    const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, sl);
+    const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, sr);
+    Digest dl{{0, 0, 0, 0}}, dr{{0, 0, 0, 0}};
+    if (__any_sync(kFull, digest_wanted(pass, lab))) {
+      dl = shfl_digest(dg, sl);
+      dr = shfl_digest(dg, sr);
+    }
+    const uint32_t width = 32u >> step;
+    if (lane < width) {
+      const uint64_t n = (r + 1) * (256u >> step) - 1 + warp * width + lane;
+      lab = span_node(a, pass, (uint32_t)n, cl, cr, dl, dr, dg, false, sink);
+    }
+  }
+  if (lane == 0) {
+    top8[warp] = lab;
+    topdg[warp] = dg;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    lab = lane < 8 ? top8[lane] : DONE;
+    if (lane < 8) dg = topdg[lane];
+#pragma unroll
+    for (uint32_t step = 6; step <= 8; step++) {
+      const int sl = (2 * lane) & 31, sr = (2 * lane + 1) & 31;
+      const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, sl);
+      const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, sr);
+      const Digest dl = shfl_digest(dg, sl), dr = shfl_digest(dg, sr);
+      const uint32_t width = 256u >> step;
+      if (lane < width) {
+        const uint64_t n = (r + 1) * width - 1 + lane;
+        lab = span_node(a, pass, (uint32_t)n, cl, cr, dl, dr, dg, step == 8, sink);
+      }
+    }
+  }
+}
+
 // A full span of 9 levels (256 nodes on its bottom level) for the incremental
-// passes: each warp carries 32 nodes up 6 levels in registers (children's
-// labels by shuffle), then warp 0 finishes the last 3 levels from the 8
-// warps' labels -- one block barrier instead of nine.  The incremental passes
-// never look up a digest inserted by the same launch (the first-occurrence
-// pass only inserts, the duplicate pass only looks up), so the order of the
-// warps does not matter; the digests of children computed by other lanes are
-// ordered by __syncwarp / __syncthreads.
+// passes and the baseline's first-occurrence pass: the bottom nodes' children
+// come from memory, the rest by upper_levels -- one block barrier instead of
+// nine, and no digest goes through memory between levels (they are still
+// stored: the tree keeps every digest for the next checkpoint).
 __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
   __shared__ uint8_t top8[8];
-  __shared__ InsertSink sink_mem;
-  const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1, epoch_all = a.sp->epoch + 2;
+  __shared__ Digest topdg[8];
+  __shared__ uint32_t ids[(1u << kSpanLevels) - 1];
+  __shared__ uint32_t ids_n, ids_base;
   const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
   const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
   if (r > last_interior) return;
-  InsertSink* sink = pass == 0 ? &sink_mem : nullptr;
-  if (threadIdx.x == 0) sink_mem.n = 0;
+  pass = resolve_pass(a, pass);
+  if (pass < 0) return;
+  if (threadIdx.x == 0) ids_n = 0;
   __syncthreads();
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr unsigned kFull = 0xffffffffu;
-  // bottom level: 256 nodes, children read from memory
+  IdSink sink{ids, &ids_n};
   uint8_t lab;
+  Digest dg{{0, 0, 0, 0}};
   {
-    const uint64_t n = (r + 1) * 256 - 1 + warp * 32 + lane;
+    const uint64_t n = (r + 1) * 256 - 1 + threadIdx.x;
     uint8_t ll = DONE, lr = DONE;
+    Digest dl{{0, 0, 0, 0}}, dr{{0, 0, 0, 0}};
     if (n <= last_interior) {
       const uint64_t c = 2 * n + 1;
       ll = c < M ? a.labels[c] : DONE;
       lr = c + 1 < M ? a.labels[c + 1] : DONE;
-    }
-    lab = forest_label(a, pass, 0, n, last_interior, M, ll, lr, cur_id, epoch_fo, epoch_all, false, sink);
-  }
-  // five levels inside the warp: 16, 8, 4, 2, 1 nodes
-#pragma unroll
-  for (uint32_t step = 1; step <= 5; step++) {
-    __syncwarp();
-    const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, (2 * lane) & 31);
-    const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, (2 * lane + 1) & 31);
-    const uint32_t width = 32u >> step;
-    if (lane < width) {
-      const uint64_t n = (r + 1) * (256u >> step) - 1 + warp * width + lane;
-      lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, false, sink);
-    }
-  }
-  if (lane == 0) top8[warp] = lab;
-  __syncthreads();
-  if (warp == 0) {
-    lab = lane < 8 ? top8[lane] : DONE;
-    // three levels in warp 0: 4, 2, 1 nodes
-#pragma unroll
-    for (uint32_t step = 6; step <= 8; step++) {
-      __syncwarp();
-      const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, (2 * lane) & 31);
-      const uint8_t cr = (uint8_t)__shfl_sync(kFull, lab, (2 * lane + 1) & 31);
-      const uint32_t width = 256u >> step;
-      if (lane < width) {
-        const uint64_t n = (r + 1) * width - 1 + lane;
-        lab = forest_label(a, pass, 0, n, last_interior, M, cl, cr, cur_id, epoch_fo, epoch_all, step == 8, sink);
+      if (ll == lr && digest_wanted(pass, ll)) {
+        dl = ld_digest(a.tree + c);
+        dr = ld_digest(a.tree + c + 1);
       }
     }
+    lab = span_label(a, pass, n, last_interior, M, ll, lr, dl, dr, dg, &sink);
   }
-  if (pass != 0) return;
-  // the collected first-occurrence inserts, all threads at once
+  upper_levels(a, pass, r, lab, dg, &sink, top8, topdg);
+  if (pass != 1) flush_sink(a, sink, &ids_base);
+}
+
+__device__ __forceinline__ uint8_t label_byte(const uint32_t cw[4], int j) {
+  return (uint8_t)(cw[j >> 2] >> (8 * (j & 3)));
+}
+
+// The bottom span of an incremental pass (and of the baseline's
+// first-occurrence pass): 12 levels, 4096 leaves per block.  Each thread
+// reads the labels of its 16 children with one aligned 16-byte load (the
+// first byte comes from the lane before) and carries its 8, 4, 2 and 1 nodes
+// in registers, depth first; a thread whose 16 children are all unchanged
+// (fixed duplicates) has nothing to hash, flag or insert.  upper_levels does
+// the rest.
+__global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
+  __shared__ uint8_t top8[8];
+  __shared__ Digest topdg[8];
+  __shared__ uint32_t ids[(1u << kBottomLevels) - 1];
+  __shared__ uint32_t ids_n, ids_base;
+  const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
+  const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
+  if (r > last_interior) return;
+  pass = resolve_pass(a, pass);
+  if (pass < 0) return;
+  if (threadIdx.x == 0) ids_n = 0;
   __syncthreads();
-  const uint32_t cnt = sink_mem.n;
-  for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x)
-    map_insert_serial(a.map, sink_mem.dg[k], sink_mem.node[k], cur_id, epoch_fo, a.err);
+  IdSink sink{ids, &ids_n};
+  const uint32_t t = threadIdx.x, lane = t & 31;
+  constexpr unsigned kFull = 0xffffffffu;
+  // children (relative depth 12) cb .. cb+15; cb + 1 is a multiple of 16
+  const uint64_t cb = (r + 1) * 4096 - 1 + 16ull * t;
+  uint4 v;
+  if (cb + 17 <= M) {
+    v = *reinterpret_cast<const uint4*>(a.labels + cb + 1);
+  } else {
+    uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const uint64_t c = cb + 1 + j;
+      w[j >> 2] |= (uint32_t)(c < M ? a.labels[c] : DONE) << (8 * (j & 3));
+    }
+    v = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  uint32_t first = __shfl_up_sync(kFull, v.w, 1) >> 24;  // byte 15 of the lane before = child cb
+  if (lane == 0) first = cb < M ? a.labels[cb] : DONE;
+  const uint32_t cw[4] = {(v.x << 8) | first, (v.y << 8) | (v.x >> 24), (v.z << 8) | (v.y >> 24),
+                          (v.w << 8) | (v.z >> 24)};
+  const uint64_t nb1 = (r + 1) * 2048 - 1 + 8ull * t;  // relative depth 11: the deepest interior level
+  uint8_t lab;
+  Digest dg{{0, 0, 0, 0}};
+  if (cw[0] == kFixed4 && cw[1] == kFixed4 && cw[2] == kFixed4 && cw[3] == kFixed4 && nb1 + 7 <= last_interior) {
+    lab = pass == 0 ? DONE : FIXED_DUPL;
+  } else {
+    uint8_t l3[2];
+    Digest d3[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      uint8_t l2[2];
+      Digest d2[2];
+#pragma unroll
+      for (int p = 0; p < 2; p++) {
+        uint8_t l1[2];
+        Digest d1[2];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+          const int k = 4 * q + 2 * p + i;
+          const uint64_t n = nb1 + k;
+          const uint8_t ll = label_byte(cw, 2 * k), lr = label_byte(cw, 2 * k + 1);
+          Digest dl{{0, 0, 0, 0}}, dr{{0, 0, 0, 0}};
+          d1[i] = Digest{{0, 0, 0, 0}};
+          if (n <= last_interior && ll == lr && digest_wanted(pass, ll)) {
+            dl = ld_digest(a.tree + 2 * n + 1);
+            dr = ld_digest(a.tree + 2 * n + 2);
+          }
+          l1[i] = span_label(a, pass, n, last_interior, M, ll, lr, dl, dr, d1[i], &sink);
+        }
+        d2[p] = Digest{{0, 0, 0, 0}};
+        l2[p] = span_node(a, pass, (uint32_t)((r + 1) * 1024 - 1 + 4 * t + 2 * q + p), l1[0], l1[1], d1[0], d1[1],
+                          d2[p], false, &sink);
+      }
+      d3[q] = Digest{{0, 0, 0, 0}};
+      l3[q] = span_node(a, pass, (uint32_t)((r + 1) * 512 - 1 + 2 * t + q), l2[0], l2[1], d2[0], d2[1], d3[q],
+                        false, &sink);
+    }
+    lab = span_node(a, pass, (uint32_t)((r + 1) * 256 - 1 + t), l3[0], l3[1], d3[0], d3[1], dg, false, &sink);
+  }
+  upper_levels(a, pass, r, lab, dg, &sink, top8, topdg);
+  if (pass != 1) flush_sink(a, sink, &ids_base);
+}
+
+// The queued first-occurrence inserts of a pass, one thread per node.
+__global__ void forest_insert_kernel(ForestArgs a) {
+  const uint32_t n = *a.ins_count;
+  const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t node = a.ins_queue[k];
+    map_insert_serial(a.map, ld_digest(a.tree + node), node, cur_id, epoch_fo, a.err);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -247,29 +463,45 @@ __device__ __forceinline__ uint32_t node_at(const ForestArgs& a, uint64_t p) {
   return (uint32_t)(((1ull << d) - 1) + q);
 }
 
-// 8 flags per thread, 4096 per tile; counts packed as (shift << 32) | fo
-__device__ __forceinline__ uint64_t flags8(const uint8_t* f, uint64_t p, uint64_t n, uint8_t out[8]) {
+// 128 contiguous flags per thread (eight 16-byte loads), 64 Ki flags per
+// tile; counts packed as (shift << 32) | fo.  Flag bytes are 0, 1 (first
+// occurrence) or 2 (shifted duplicate), so bit 0 and bit 1 of each byte
+// count the two kinds.
+constexpr int kRootVec = 8;
+constexpr uint64_t kRootPerThread = 16 * kRootVec;
+constexpr uint64_t kRootTile = kRootPerThread * kScanThreads;
+static_assert(ROOT_FO == 1 && ROOT_SHIFT == 2, "flag bytes counted by bit");
+
+__device__ __forceinline__ uint64_t count_word(uint32_t w) {
+  return (uint64_t)__popc(w & 0x01010101u) | ((uint64_t)__popc(w & 0x02020202u) << 32);
+}
+
+// The thread's 128 flags starting at p (p a multiple of 128); bytes at or past
+// n read as ROOT_NONE.
+__device__ __forceinline__ uint64_t load_flags128(const uint8_t* f, uint64_t p, uint64_t n, uint4 v[kRootVec]) {
   uint64_t c = 0;
 #pragma unroll
-  for (int k = 0; k < 8; k++) {
-    uint8_t v = (p + k < n) ? f[p + k] : 0;
-    out[k] = v;
-    c += (v == ROOT_FO) ? 1ull : (v == ROOT_SHIFT ? (1ull << 32) : 0ull);
+  for (int k = 0; k < kRootVec; k++) {
+    const uint64_t q = p + 16 * (uint64_t)k;
+    if (q + 16 <= n) {
+      v[k] = *reinterpret_cast<const uint4*>(f + q);
+    } else {
+      uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        if (q + j < n) w[j >> 2] |= (uint32_t)f[q + j] << (8 * (j & 3));
+      v[k] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    c += count_word(v[k].x) + count_word(v[k].y) + count_word(v[k].z) + count_word(v[k].w);
   }
   return c;
 }
 
 __global__ void __launch_bounds__(kScanThreads) root_count_kernel(const uint8_t* rflag, uint64_t n, uint64_t* tile_sums) {
   __shared__ uint64_t sh[33];
-  const uint64_t p = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanPerThread;
-  uint8_t v[8];
-  uint64_t c = 0;
-  if (p + 8 <= n && ((p & 7) == 0)) {
-    uint64_t w = *reinterpret_cast<const uint64_t*>(rflag + p);
-    if (w) c = flags8(rflag, p, n, v);
-  } else if (p < n) {
-    c = flags8(rflag, p, n, v);
-  }
+  const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
+  uint4 v[kRootVec];
+  const uint64_t c = p < n ? load_flags128(rflag, p, n, v) : 0;
   uint64_t total;
   block_excl_scan(c, sh, &total);
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
@@ -278,22 +510,28 @@ __global__ void __launch_bounds__(kScanThreads) root_count_kernel(const uint8_t*
 __global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, uint64_t n, const uint64_t* tile_off,
                                                                  uint32_t* fo_list, uint32_t* sh_list, const Layout* lay) {
   __shared__ uint64_t sh[33];
-  const uint64_t p = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanPerThread;
-  uint8_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  uint64_t c = 0;
-  if (p < n) {
-    if (p + 8 <= n && ((p & 7) == 0)) {
-      if (*reinterpret_cast<const uint64_t*>(a.rflag + p)) c = flags8(a.rflag, p, n, v);
-    } else {
-      c = flags8(a.rflag, p, n, v);
-    }
-  }
+  const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
+  uint4 v[kRootVec];
+  const uint64_t c = p < n ? load_flags128(a.rflag, p, n, v) : 0;
   uint64_t ex = block_excl_scan(c, sh, nullptr) + tile_off[blockIdx.x];
   if (!c) return;
   const uint32_t root = lay->root_fo;
-  for (int k = 0; k < 8; k++) {
-    if (v[k] == ROOT_FO) { fo_list[root + (uint32_t)ex] = node_at(a, p + k); ex += 1; }
-    else if (v[k] == ROOT_SHIFT) { sh_list[(uint32_t)(ex >> 32)] = node_at(a, p + k); ex += 1ull << 32; }
+#pragma unroll
+  for (int k = 0; k < kRootVec; k++) {
+    const uint32_t w4[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      uint32_t w = w4[j];
+      while (w) {
+        const int bit = __ffs(w) - 1;  // lowest set flag bit: byte order = serial order
+        const int byte = bit >> 3;
+        const uint8_t f = (uint8_t)(w >> (8 * byte));
+        const uint64_t pos = p + 16 * (uint64_t)k + 4 * j + byte;
+        if (f == ROOT_FO) { fo_list[root + (uint32_t)ex] = node_at(a, pos); ex += 1; }
+        else { sh_list[(uint32_t)(ex >> 32)] = node_at(a, pos); ex += 1ull << 32; }
+        w &= ~(0xffu << (8 * byte));
+      }
+    }
   }
 }
 
@@ -692,25 +930,41 @@ cudaError_t launch_map_rehash(const DigestMap& from, uint64_t from_cap, const Di
 // ---------------------------------------------------------------------------
 cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t N, cudaStream_t s) {
   if (N < 2) return cudaSuccess;
-  // the duplicate pass writes only the flags of roots; every other position
-  // (node 1 .. M-1 in canonical order) reads ROOT_NONE
-  if (pass == 1) {
+  if (pass == 0) {
+    // the duplicate pass (alone or fused into the first) writes only the
+    // flags of roots; every other position (node 1 .. M-1 in canonical
+    // order) reads ROOT_NONE
     cudaError_t e = cudaMemsetAsync(a.rflag, ROOT_NONE, 2ull * N - 2, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.ins_count, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
   }
   // deepest interior depth: that of node N-2
   uint32_t dmax = 0;
   while (((2ull << dmax) - 1) <= (uint64_t)(N - 2)) dmax++;
-  for (int bot = (int)dmax; bot >= 0; bot -= kSpanLevels) {
+  const bool dup_baseline = pass == 1 && baseline;
+  int bot = (int)dmax;
+  if (!dup_baseline && dmax + 1 >= kBottomLevels) {
+    const uint32_t top = dmax - (kBottomLevels - 1);
+    const uint64_t first = (1ull << top) - 1;
+    const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
+    forest_bottom12_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+    note_launch();
+    bot = (int)top - 1;
+  }
+  for (; bot >= 0; bot -= kSpanLevels) {
     const uint32_t top = bot >= (int)kSpanLevels - 1 ? (uint32_t)bot - (kSpanLevels - 1) : 0;
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
-    if (!baseline && (uint32_t)bot - top == kSpanLevels - 1)
+    if (!dup_baseline && (uint32_t)bot - top == kSpanLevels - 1)
       forest_span9_warp_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
     else
       forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot);
     note_launch();
     if (top == 0) break;
+  }
+  if (pass == 0) {
+    forest_insert_kernel<<<grid_for(N, 256), 256, 0, s>>>(a);
+    note_launch();
   }
   return cudaGetLastError();
 }
@@ -719,7 +973,7 @@ cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M,
                                    uint32_t* sh_list, Layout* lay, uint64_t* scan_scratch, uint64_t* scan_total,
                                    cudaStream_t s) {
   const uint64_t n = (uint64_t)M - 1;  // every node but the root
-  uint32_t ntiles = (uint32_t)((n + kScanTile - 1) / kScanTile);
+  uint32_t ntiles = (uint32_t)((n + kRootTile - 1) / kRootTile);
   if (ntiles == 0) ntiles = 1;
   root_prologue_kernel<<<1, 1, 0, s>>>(fa.labels, N, fa.ascending, fo_list, lay);
   root_count_kernel<<<ntiles, kScanThreads, 0, s>>>(fa.rflag, n, scan_scratch);

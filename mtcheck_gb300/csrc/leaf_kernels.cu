@@ -126,7 +126,10 @@ __global__ void leaf_demote_kernel(LeafArgs a) {
     if (a.labels[c] != FIRST_OCUR) continue;
     const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
     const uint32_t node = a.leaf_base + c;
-    if (a.epi == EPI_TREE ? (s->tree == cur && s->node != node) : (s->node != node)) a.labels[c] = SHIFT_DUPL;
+    if (a.epi == EPI_TREE ? (s->tree == cur && s->node != node) : (s->node != node)) {
+      a.labels[c] = SHIFT_DUPL;
+      if (a.demoted) atomicOr(a.demoted, 1u);
+    }
   }
 }
 

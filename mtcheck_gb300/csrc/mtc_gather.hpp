@@ -36,6 +36,14 @@ struct ForestArgs {
   int ascending;   // canonical order: 0 = deeper levels first (serial push order), 1 = ascending node id
   uint32_t D;      // depth of node M-1
   uint64_t sizeD;  // nodes on depth D
+  // Incremental checkpoints: word that is 0 when no leaf was demoted to a
+  // shifted duplicate of a digest first seen in this checkpoint.  Then no
+  // shifted pair can hash to a digest inserted by the first-occurrence pass
+  // (its leaves would share a digest with a first occurrence, whose digest is
+  // new), so both passes run in one traversal.  Null: two passes.
+  const uint32_t* fuse_gate;
+  uint32_t* ins_queue;  // first-occurrence nodes awaiting their map insert (N entries)
+  uint32_t* ins_count;
 };
 
 // Position of node x (>= 1) in the canonical root order.

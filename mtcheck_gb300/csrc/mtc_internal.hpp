@@ -46,6 +46,7 @@ struct LeafArgs {
   uint32_t* err = nullptr;        // device error word
   uint32_t* changed_list = nullptr;  // chunks whose digest changed (tree, list)
   uint32_t* changed_count = nullptr;
+  uint32_t* demoted = nullptr;    // set to 1 when a first occurrence is demoted (tree; may be null)
   int hash_kind = HASH_MURMUR3;
   int epi = EPI_HASH;
   int basic_first = 0;            // basic approach with current_id == 0: every chunk changed

@@ -82,6 +82,30 @@ def test_heavy_duplication_and_zero_region(cuda, mtc, oracle):
         run_both(cuda, mtc, oracle, approach, 0, seq, 128)
 
 
+@pytest.mark.parametrize("kind", [0, 1], ids=["murmur3", "md5"])
+@pytest.mark.parametrize("nbytes,cs", [(1 << 20, 128), ((1 << 20) + 300, 256)])
+def test_new_content_repeated_in_one_checkpoint(cuda, mtc, oracle, kind, nbytes, cs):
+    # Fresh bytes written at several places in one incremental checkpoint: the
+    # later copies' leaves are demoted to shifted duplicates, and the aligned
+    # copy's interior pairs hash to first-occurrence digests inserted by the
+    # same checkpoint, so the duplicate pass has to follow the first-occurrence
+    # pass.  The next checkpoint repeats no new content (one traversal), with
+    # shifted duplicates of old content.
+    rng = np.random.default_rng(nbytes + kind)
+    s0 = rng.integers(0, 256, nbytes, dtype=np.uint8)
+    s1 = s0.copy()
+    run = 64 * cs
+    fresh = rng.integers(0, 256, run, dtype=np.uint8)
+    for at in (128 * cs, 1024 * cs, 2048 * cs + 5 * cs):
+        s1[at:at + run] = fresh
+    s2 = s1.copy()
+    s2[512 * cs:512 * cs + run] = rng.integers(0, 256, run, dtype=np.uint8)
+    s2[3000 * cs:3007 * cs] = s1[100 * cs:107 * cs]
+    s2[3100 * cs:3164 * cs] = s1[1024 * cs:1088 * cs]
+    for approach in (4, 5):
+        run_both(cuda, mtc, oracle, approach, kind, [s0, s1, s2], cs)
+
+
 def test_same_id_header_overload(cuda, mtc, oracle):
     # checkpoint(header_t&, ...) does not advance current_id
     seq = series(1, 1 << 18, 128, 3, seed=2)
