@@ -5,6 +5,7 @@
 // src/list_approach.cpp:843-931, src/basic_approach.cpp:468-549,
 // src/full_approach.cpp:14-77).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "engine.hpp"
@@ -27,6 +28,8 @@ Engine::Engine(int mode, int hash_kind, uint32_t chunk_size) : mode_(mode), hash
   cudaMallocHost(&sp_host_, sizeof(StepParams));
   std::memset(lay_host_, 0, sizeof(Layout));
   std::memset(sp_host_, 0, sizeof(StepParams));
+  // test hook: start the launch epochs near their limit to exercise the rebase
+  if (const char* e = std::getenv("MTCHECK_EPOCH_START")) epoch_ = (uint32_t)std::strtoul(e, nullptr, 10);
 }
 
 Engine::~Engine() {
@@ -61,7 +64,7 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
       MTC_CUDA(slots_.ensure(need, stream_));
     }
     map_cap_ = slots_.n;
-    MTC_CUDA(cudaMemsetAsync(slots_.p, 0, sizeof(MapSlot) * map_cap_, stream_));
+    MTC_CUDA(cudaMemsetAsync(slots_.p, kMapFill, sizeof(MapSlot) * map_cap_, stream_));
     MTC_CUDA(cudaMemsetAsync(map_size_.p, 0, sizeof(uint32_t), stream_));
     map_size_host_ = 0;
     return ST_OK;
@@ -69,7 +72,7 @@ int Engine::ensure_map(uint64_t want_entries, bool reset) {
   if (map_cap_ >= need) return ST_OK;
   DevBuf<MapSlot> fresh;
   MTC_CUDA(fresh.ensure(need, stream_));
-  MTC_CUDA(cudaMemsetAsync(fresh.p, 0, sizeof(MapSlot) * need, stream_));
+  MTC_CUDA(cudaMemsetAsync(fresh.p, kMapFill, sizeof(MapSlot) * need, stream_));
   MTC_CUDA(cudaMemsetAsync(map_size_.p, 0, sizeof(uint32_t), stream_));
   DigestMap from{slots_.p, map_cap_ - 1, map_size_.p};
   DigestMap to{fresh.p, need - 1, map_size_.p};
@@ -148,6 +151,12 @@ int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
   if (mode_ != MODE_BASIC) {
     int rc = ensure_map((uint64_t)map_size_host_ + (tree ? M_ : N_), false);
     if (rc) return rc;
+    // map entries keep their epoch in 26 bits: before the counter gets
+    // there, every entry goes back to epoch 0 (older than any launch to come)
+    if (epoch_ + kEpochsPerCheckpoint >= kEpochLimit) {
+      if (map_cap_) MTC_CUDA(launch_map_rebase(DigestMap{slots_.p, map_cap_ - 1, map_size_.p}, map_cap_, stream_));
+      epoch_ = 0;
+    }
   }
   return ensure_sort(current_id + 1 + id_headroom);
 }

@@ -126,7 +126,7 @@ __device__ __forceinline__ uint8_t forest_node(const ForestArgs& a, int pass, in
     if (baseline) {
       Digest dg = hash_pair(a.hash_kind, ld_digest(a.tree + l), ld_digest(a.tree + rr));
       st_digest(a.tree + n, dg);
-      map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_all, a.err);
+      if (map_insert_serial(a.map, dg, (uint32_t)n, cur_id, epoch_all, a.err)) atomicAdd(a.map.size, 1u);
     }
   }
   if (store) a.labels[n] = lab_n;
@@ -444,10 +444,12 @@ __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int 
 __global__ void forest_insert_kernel(ForestArgs a) {
   const uint32_t n = *a.ins_count;
   const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1;
+  uint32_t created = 0;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t node = a.ins_queue[k];
-    map_insert_serial(a.map, ld_digest(a.tree + node), node, cur_id, epoch_fo, a.err);
+    created += map_insert_serial(a.map, ld_digest(a.tree + node), node, cur_id, epoch_fo, a.err);
   }
+  count_new_entries(a.map, created);
 }
 
 // ---------------------------------------------------------------------------
@@ -906,13 +908,28 @@ __global__ void chunk_totals_kernel(const uint64_t* total, Layout* lay) {
   lay->S = (uint32_t)(*total >> 32);
 }
 
+// Entries of a table moved into a larger one (keys are stored already
+// mapped, and unique, so every claim is new).
 __global__ void map_rehash_kernel(DigestMap from, uint64_t from_cap, DigestMap to, uint32_t* err) {
+  uint32_t created = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < from_cap; i += (uint64_t)gridDim.x * blockDim.x) {
     const MapSlot& s = from.slots[i];
-    if (s.state != 2) continue;
-    Digest k{{s.key[0], s.key[1], s.key[2], s.key[3]}};
+    const uint4 v = *reinterpret_cast<const uint4*>(s.key);
+    if (key_empty(v)) continue;
     uint64_t slot;
-    map_insert(to, k, s.node, s.tree, s.epoch, &slot, err);
+    if (map_claim(to, Digest{{v.x, v.y, v.z, v.w}}, &slot, err) != INS_NEW) continue;
+    to.slots[slot].win = s.win;
+    to.slots[slot].tree = s.tree;
+    created++;
+  }
+  count_new_entries(to, created);
+}
+
+// Epochs of every entry set to 0, before the engine's epoch counter restarts.
+__global__ void map_rebase_kernel(DigestMap m, uint64_t cap) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+    MapSlot& s = m.slots[i];
+    if (s.win != kWinEmpty) s.win &= (1ull << kPrioBits) - 1;
   }
 }
 
@@ -921,6 +938,12 @@ __global__ void map_rehash_kernel(DigestMap from, uint64_t from_cap, DigestMap t
 cudaError_t launch_map_rehash(const DigestMap& from, uint64_t from_cap, const DigestMap& to, uint32_t* err,
                               cudaStream_t s) {
   map_rehash_kernel<<<grid_for(from_cap, 256), 256, 0, s>>>(from, from_cap, to, err);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_map_rebase(const DigestMap& m, uint64_t cap, cudaStream_t s) {
+  map_rebase_kernel<<<grid_for(cap, 256), 256, 0, s>>>(m, cap);
   note_launch();
   return cudaGetLastError();
 }

@@ -79,41 +79,47 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uin
   append_changed(changed, c, a.changed_list, a.changed_count);
 }
 
-// Map insert of one changed chunk.
+// Map insert of one changed chunk (src/tree_approach.cpp:325-349,
+// src/list_approach.cpp:50-59): new digest -> first occurrence; a digest
+// already inserted by this launch -> first occurrence for now, the lowest
+// chunk keeping the entry; an older digest -> shifted duplicate, except (tree)
+// one whose entry carries this checkpoint's id, which an id that was not
+// advanced (the header overload) leaves in place: the reference lowers its
+// node and keeps the chunk a first occurrence there too.
 template <int EPI>
 __global__ void leaf_insert_kernel(LeafArgs a) {
   const uint32_t n = *a.changed_count;
   const uint32_t cur = a.sp->cur, epoch = a.sp->epoch;
+  uint32_t created = 0;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = a.changed_list[k];
     const Digest dg = ld_digest(a.prev + c);
+    const uint32_t node = EPI == EPI_TREE ? a.leaf_base + c : c;
     uint64_t slot = 0;
+    unsigned long long old = kWinEmpty;
     uint8_t label = SHIFT_DUPL;
-    if (EPI == EPI_TREE) {
-      const uint32_t node = a.leaf_base + c;
-      int r = map_insert(a.map, dg, node, cur, epoch, &slot, a.err);
-      if (r == INS_NEW) {
-        label = FIRST_OCUR;
-      } else if (r == INS_EXISTING) {
-        MapSlot* s = &a.map.slots[slot];
-        if (__ldcg(&s->tree) == cur) {
-          atomicMin(&s->node, node);  // lowest offset wins
-          label = FIRST_OCUR;
+    const int r = map_insert_win(a.map, dg, win_of(epoch, node), cur, &slot, &old, a.err);
+    if (r == INS_NEW) {
+      label = FIRST_OCUR;
+      created++;
+    } else if (r == INS_EXISTING) {
+      if (old == kWinEmpty || win_epoch(old) == epoch) {
+        label = FIRST_OCUR;  // first seen by this launch
+      } else if (EPI == EPI_TREE && __ldcg(&a.map.slots[slot].tree) == cur) {
+        // lowest node within the older entry, its epoch kept
+        unsigned long long w = old;
+        for (int i = 0; i < 64 && win_node(w) > node; i++) {
+          const unsigned long long seen = atomicCAS(&a.map.slots[slot].win, w, (w & ~0xffffffffull) | node);
+          if (seen == w) break;
+          w = seen;
         }
-      }
-    } else {
-      int r = map_insert(a.map, dg, c, cur, epoch, &slot, a.err);
-      if (r == INS_NEW) {
         label = FIRST_OCUR;
-      } else if (r == INS_EXISTING) {
-        MapSlot* s = &a.map.slots[slot];
-        // a serial backend gives the digest to the lowest changed chunk of this pass
-        if (__ldcg(&s->epoch) == epoch) { atomicMin(&s->node, c); label = FIRST_OCUR; }
       }
     }
     a.chunk_slot[c] = (uint32_t)slot;
     a.labels[c] = label;
   }
+  count_new_entries(a.map, created);
 }
 
 // Second pass (src/tree_approach.cpp:356-369): a first occurrence that does
@@ -126,7 +132,8 @@ __global__ void leaf_demote_kernel(LeafArgs a) {
     if (a.labels[c] != FIRST_OCUR) continue;
     const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
     const uint32_t node = a.leaf_base + c;
-    if (a.epi == EPI_TREE ? (s->tree == cur && s->node != node) : (s->node != node)) {
+    const uint32_t owner = win_node(s->win);
+    if (a.epi == EPI_TREE ? (s->tree == cur && owner != node) : (owner != node)) {
       a.labels[c] = SHIFT_DUPL;
       if (a.demoted) atomicOr(a.demoted, 1u);
     }

@@ -16,7 +16,7 @@ enum : int { HASH_MURMUR3 = 0, HASH_MD5 = 1 };
 // Bits of the per-handle device error word.
 enum : uint32_t {
   DERR_MAP_FULL = 1u << 0,      // probe sequence wrapped: table full
-  DERR_SPIN = 1u << 1,          // bounded wait on a slot being published ran out
+  DERR_SPIN = 1u << 1,          // a bounded device wait ran out
   DERR_FO_MISMATCH = 1u << 2,   // a first-occurrence root is not its digest's owner
   DERR_CAPACITY = 1u << 3,      // diff larger than the device staging buffer
   DERR_MISSING = 1u << 4,       // a root digest is absent from the map
@@ -256,107 +256,126 @@ __host__ __device__ __forceinline__ uint32_t leftmost_leaf(uint32_t node, uint32
 // Digest -> NodeID map (the reference's DigestNodeIDDeviceMap,
 // include/map_helpers.hpp:105-110, with Kokkos::UnorderedMap's
 // insert-if-absent semantics).  Open addressing, linear probing, 32-byte
-// slots.  A slot is claimed by CAS on `state` (0 empty, 1 being written,
-// 2 published); waits on state 1 are bounded and raise DERR_SPIN.
-// `epoch` identifies the launch that inserted the entry, which gives the
-// serial "first insert wins" order between launches and "lowest node wins"
-// among the inserts of one launch.
+// slots.  A slot is claimed by one 128-bit compare-and-swap of its key
+// (all-ones = empty; a digest equal to that pattern is stored with its lowest
+// bit cleared).  `win` packs (epoch << 38) | priority and starts all-ones;
+// every insert of a key, its creator's included, applies atomicMin to it, so
+//   * an entry created by an earlier launch (smaller epoch) is kept,
+//   * among the inserts of one launch the lowest priority wins: the lowest
+//     chunk or node (the reference's atomic_min), or the serial order of a
+//     forest pass,
+// and the old value an insert gets back tells whether the entry is older
+// than its launch.  The node is win's low 32 bits.  `tree` (the checkpoint id
+// of the first occurrence) is written by the creator and read by later
+// launches.  No insert waits on another thread.
 // ---------------------------------------------------------------------------
 struct __align__(32) MapSlot {
   uint32_t key[4];
-  uint32_t node, tree, epoch, state;
+  unsigned long long win;
+  uint32_t tree;
+  uint32_t reserved;
 };
 struct DigestMap {
   MapSlot* slots;
   uint64_t mask;       // capacity - 1 (capacity a power of two)
-  uint32_t* size;      // number of published entries
+  uint32_t* size;      // number of entries
 };
+constexpr unsigned long long kWinEmpty = ~0ull;
+constexpr int kPrioBits = 38;
+constexpr uint32_t kEpochLimit = 1u << (64 - kPrioBits);  // epochs are rebased to 0 before reaching it
+constexpr int kMapFill = 0xff;                             // byte pattern of an empty table
+
+__host__ __device__ __forceinline__ unsigned long long win_of(uint32_t epoch, uint64_t prio) {
+  return ((unsigned long long)epoch << kPrioBits) | prio;
+}
+__host__ __device__ __forceinline__ uint32_t win_epoch(unsigned long long w) { return (uint32_t)(w >> kPrioBits); }
+__host__ __device__ __forceinline__ uint32_t win_node(unsigned long long w) { return (uint32_t)w; }
 
 enum : int { INS_FAILED = 0, INS_NEW = 1, INS_EXISTING = 2 };
-constexpr int kSpinLimit = 1 << 20;
 
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
+__device__ __forceinline__ Digest map_key(const Digest& k) {
+  Digest m = k;
+  if ((k.w[0] & k.w[1] & k.w[2] & k.w[3]) == 0xffffffffu) m.w[0] = 0xfffffffeu;
+  return m;
 }
-__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+__device__ __forceinline__ bool key_empty(const uint4& v) { return (v.x & v.y & v.z & v.w) == 0xffffffffu; }
+__device__ __forceinline__ bool key_eq(const uint4& v, const Digest& k) {
+  return ((v.x ^ k.w[0]) | (v.y ^ k.w[1]) | (v.z ^ k.w[2]) | (v.w ^ k.w[3])) == 0;
 }
 __device__ __forceinline__ uint64_t slot_of(const Digest& k, uint64_t mask) {
   uint64_t a = ((uint64_t)k.w[1] << 32) | k.w[0];
   a ^= a >> 29; a *= 0xbf58476d1ce4e5b9ull; a ^= a >> 32;
   return a & mask;
 }
-__device__ __forceinline__ bool slot_key_eq(const MapSlot* s, const Digest& k) {
-  uint4 v = __ldcg(reinterpret_cast<const uint4*>(s->key));
-  return ((v.x ^ k.w[0]) | (v.y ^ k.w[1]) | (v.z ^ k.w[2]) | (v.w ^ k.w[3])) == 0;
-}
-// Wait until slot state leaves 1; returns the state or 0xffffffff on timeout.
-__device__ __forceinline__ uint32_t wait_published(MapSlot* s, uint32_t st, uint32_t* err) {
-  int spins = 0;
-  while (st == 1) {
-    if (++spins > kSpinLimit) { atomicOr(err, DERR_SPIN); return 0xffffffffu; }
-    __nanosleep(32);
-    st = ld_acquire_u32(&s->state);
-  }
-  return st;
+
+// 128-bit compare-and-swap of a slot's key from empty to k; returns the key
+// that was there (empty: the caller now owns the slot).
+__device__ __forceinline__ uint4 claim_key(MapSlot* s, const Digest& k) {
+  const unsigned long long e = ~0ull;
+  const unsigned long long vlo = ((unsigned long long)k.w[1] << 32) | k.w[0];
+  const unsigned long long vhi = ((unsigned long long)k.w[3] << 32) | k.w[2];
+  unsigned long long olo, ohi;
+  asm volatile(
+      "{\n\t.reg .b128 c, v, o;\n\t"
+      "mov.b128 c, {%2, %3};\n\t"
+      "mov.b128 v, {%4, %5};\n\t"
+      "atom.relaxed.gpu.global.cas.b128 o, [%6], c, v;\n\t"
+      "mov.b128 {%0, %1}, o;\n\t}"
+      : "=l"(olo), "=l"(ohi)
+      : "l"(e), "l"(e), "l"(vlo), "l"(vhi), "l"(s->key)
+      : "memory");
+  return make_uint4((uint32_t)olo, (uint32_t)(olo >> 32), (uint32_t)ohi, (uint32_t)(ohi >> 32));
 }
 
-// Insert (key -> node, tree, epoch) if absent.  Returns INS_NEW / INS_EXISTING
-// with *slot set, or INS_FAILED (error word set).
-__device__ inline int map_insert(const DigestMap& m, const Digest& k, uint32_t node, uint32_t tree, uint32_t epoch,
-                                 uint64_t* slot, uint32_t* err) {
+// The slot of k, claimed if absent: INS_NEW (this thread created the entry),
+// INS_EXISTING, or INS_FAILED (table full, error word set).
+__device__ inline int map_claim(const DigestMap& m, const Digest& k, uint64_t* slot, uint32_t* err) {
   uint64_t i = slot_of(k, m.mask);
   for (uint64_t probe = 0; probe <= m.mask; probe++) {
-    MapSlot* s = &m.slots[i];
-    uint32_t st = ld_acquire_u32(&s->state);
-    if (st == 0) {
-      uint32_t old = atomicCAS(&s->state, 0u, 1u);
-      if (old == 0) {
-        *reinterpret_cast<uint4*>(s->key) = make_uint4(k.w[0], k.w[1], k.w[2], k.w[3]);
-        s->node = node; s->tree = tree; s->epoch = epoch;
-        st_release_u32(&s->state, 2u);
-        atomicAdd(m.size, 1u);
-        *slot = i;
-        return INS_NEW;
-      }
-      st = old;
-    }
-    st = wait_published(s, st, err);
-    if (st == 0xffffffffu) return INS_FAILED;
-    if (slot_key_eq(s, k)) { *slot = i; return INS_EXISTING; }
+    const uint4 old = claim_key(&m.slots[i], k);
+    if (key_empty(old)) { *slot = i; return INS_NEW; }
+    if (key_eq(old, k)) { *slot = i; return INS_EXISTING; }
     i = (i + 1) & m.mask;
   }
   atomicOr(err, DERR_MAP_FULL);
   return INS_FAILED;
 }
 
-// Slot index of key, or -1.
-__device__ inline int64_t map_find(const DigestMap& m, const Digest& k, uint32_t* err) {
+// Insert (k -> win, tree) with the priority rule above.  *old_win receives the
+// entry's previous win: kWinEmpty for an entry created by this launch whose
+// creator has not applied its own yet.  A new entry is not counted in
+// m.size: the caller adds it (count_new_entries).
+__device__ __forceinline__ int map_insert_win(const DigestMap& m, const Digest& k0, unsigned long long win,
+                                              uint32_t tree, uint64_t* slot, unsigned long long* old_win,
+                                              uint32_t* err) {
+  const Digest k = map_key(k0);
+  const int r = map_claim(m, k, slot, err);
+  if (r == INS_FAILED) return r;
+  MapSlot* s = &m.slots[*slot];
+  if (r == INS_NEW) s->tree = tree;
+  *old_win = atomicMin(&s->win, win);
+  return r;
+}
+
+// Warp total of new entries added to m.size (every lane of the warp calls it).
+__device__ __forceinline__ void count_new_entries(const DigestMap& m, uint32_t n) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(m.size, n);
+}
+
+// Slot index of key, or -1.  Plain loads: a key inserted by an earlier launch
+// is found through slots that were all full when this launch started.
+__device__ inline int64_t map_find(const DigestMap& m, const Digest& k0, uint32_t* err) {
+  const Digest k = map_key(k0);
   uint64_t i = slot_of(k, m.mask);
   for (uint64_t probe = 0; probe <= m.mask; probe++) {
-    MapSlot* s = &m.slots[i];
-    uint32_t st = ld_acquire_u32(&s->state);
-    if (st == 0) return -1;
-    st = wait_published(s, st, err);
-    if (st == 0xffffffffu) return -1;
-    if (slot_key_eq(s, k)) return (int64_t)i;
+    const uint4 v = __ldcg(reinterpret_cast<const uint4*>(m.slots[i].key));
+    if (key_empty(v)) return -1;
+    if (key_eq(v, k)) return (int64_t)i;
     i = (i + 1) & m.mask;
   }
   return -1;
-}
-
-// Insert with the serial order of one reference launch: an entry created by an
-// earlier launch is kept; among inserts of this launch the lowest node wins.
-__device__ inline void map_insert_first(const DigestMap& m, const Digest& k, uint32_t node, uint32_t tree,
-                                        uint32_t epoch, uint32_t* err) {
-  uint64_t slot;
-  int r = map_insert(m, k, node, tree, epoch, &slot, err);
-  if (r == INS_EXISTING) {
-    MapSlot* s = &m.slots[slot];
-    if (__ldcg(&s->epoch) == epoch) atomicMin(&s->node, node);
-  }
 }
 
 // Serial insertion order inside one forest pass: deeper levels first, then
@@ -367,19 +386,12 @@ __device__ __forceinline__ uint64_t serial_prio(uint32_t node) {
 }
 // Insert for a pass that spans several levels in one launch: an entry from an
 // earlier launch is kept; among inserts of this pass the serially first wins.
-__device__ inline void map_insert_serial(const DigestMap& m, const Digest& k, uint32_t node, uint32_t tree,
-                                         uint32_t epoch, uint32_t* err) {
+// Returns 1 when the entry is new.
+__device__ __forceinline__ uint32_t map_insert_serial(const DigestMap& m, const Digest& k, uint32_t node,
+                                                      uint32_t tree, uint32_t epoch, uint32_t* err) {
   uint64_t slot;
-  int r = map_insert(m, k, node, tree, epoch, &slot, err);
-  if (r != INS_EXISTING) return;
-  MapSlot* s = &m.slots[slot];
-  if (__ldcg(&s->epoch) != epoch) return;
-  uint32_t cur = __ldcg(&s->node);
-  for (int i = 0; i < 64 && serial_prio(node) < serial_prio(cur); i++) {
-    uint32_t old = atomicCAS(&s->node, cur, node);
-    if (old == cur) return;
-    cur = old;
-  }
+  unsigned long long old;
+  return map_insert_win(m, k, win_of(epoch, serial_prio(node)), tree, &slot, &old, err) == INS_NEW ? 1u : 0u;
 }
 
 // Plain read of a slot's value after the launch that wrote it has finished.
@@ -387,7 +399,7 @@ struct NodeIdDev { uint32_t node, tree; };
 __device__ __forceinline__ NodeIdDev slot_value(const DigestMap& m, int64_t slot) {
   if (slot < 0) return NodeIdDev{0xffffffffu, 0xffffffffu};
   const MapSlot* s = &m.slots[slot];
-  return NodeIdDev{s->node, s->tree};
+  return NodeIdDev{win_node(s->win), s->tree};
 }
 
 }  // namespace mtc

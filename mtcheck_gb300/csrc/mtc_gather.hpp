@@ -96,5 +96,7 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
 // Rebuild `from` into the empty table `to` (capacity change), preserving values.
 cudaError_t launch_map_rehash(const DigestMap& from, uint64_t from_cap, const DigestMap& to, uint32_t* err,
                               cudaStream_t s);
+// Every entry's epoch set to 0 (before the epoch counter restarts).
+cudaError_t launch_map_rebase(const DigestMap& m, uint64_t cap, cudaStream_t s);
 
 }  // namespace mtc

@@ -106,6 +106,16 @@ def test_new_content_repeated_in_one_checkpoint(cuda, mtc, oracle, kind, nbytes,
         run_both(cuda, mtc, oracle, approach, kind, [s0, s1, s2], cs)
 
 
+def test_epochs_rebased_near_their_limit(cuda, mtc, oracle, monkeypatch):
+    # launch epochs start just below the 26-bit epoch field of a map entry:
+    # the map's entries go back to epoch 0 at the third checkpoint and every
+    # diff stays equal to the oracle's
+    monkeypatch.setenv("MTCHECK_EPOCH_START", str((1 << 26) - 8))
+    seq = series(2, 1 << 20, 128, 6, seed=5)
+    for approach in (3, 4):
+        run_both(cuda, mtc, oracle, approach, 0, seq, 128)
+
+
 def test_same_id_header_overload(cuda, mtc, oracle):
     # checkpoint(header_t&, ...) does not advance current_id
     seq = series(1, 1 << 18, 128, 3, seed=2)
