@@ -667,7 +667,7 @@ def main():
     dd.checkpoint_device(states[0], True)
     for s in states[1:1 + W]:
         dd.checkpoint_device(s, False)
-    leaf_t, ckpt_t, sizes, sdata, smeta = [], [], [], [], []
+    leaf_t, tree_t, asm_t, ckpt_t, sizes, sdata, smeta = [], [], [], [], [], [], []
     l0 = mc.launch_count()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -677,6 +677,8 @@ def main():
             n = dd.checkpoint_device(s, False)
             info = dd.info()
             leaf_t.append(info.phase_times[0])
+            tree_t.append(info.phase_times[1])
+            asm_t.append(info.timers[2])
             ckpt_t.append(sum(info.timers[:3]))
             sizes.append(n)
             sdata.append(info.data_size)
@@ -772,6 +774,8 @@ def main():
                        "diff_bytes_mean": int(sum(sizes) / K),
                        "checkpoint_roofline_frac": round(ckpt_frac, 4),
                        "phase_ms_mean": {"leaf_hash": round(leaf_avg * 1e3, 4),
+                                         "labels_forest_roots": round(sum(tree_t) / K * 1e3, 4),
+                                         "diff_assembly": round(sum(asm_t) / K * 1e3, 4),
                                          "checkpoint_device": round(sum(ckpt_t) / K * 1e3, 4)}},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,

@@ -46,6 +46,7 @@ __device__ __forceinline__ uint8_t child_flag(uint8_t lab) {
 // incremental passes in one traversal (ForestArgs::fuse_gate).
 constexpr uint32_t kSpanLevels = 9;     // 256 nodes on the bottom level of a span
 constexpr uint32_t kBottomLevels = 12;  // bottom span: 16 leaves per thread, 4096 per block
+constexpr uint32_t kBottomSink = 2048;  // queued inserts a bottom block holds in shared memory
 constexpr uint32_t kFixed4 = 0x01010101u * FIXED_DUPL;
 
 // First-occurrence inserts are queued (node ids in ForestArgs::ins_queue) and
@@ -57,14 +58,21 @@ constexpr uint32_t kFixed4 = 0x01010101u * FIXED_DUPL;
 struct IdSink {
   uint32_t* ids;  // shared memory
   uint32_t* n;    // shared counter
+  uint32_t cap;   // ids beyond it go to the global queue directly
 };
 __device__ __forceinline__ void queue_insert(const ForestArgs& a, IdSink* sink, uint32_t n) {
-  if (sink) sink->ids[atomicAdd(sink->n, 1u)] = n;
-  else a.ins_queue[atomicAdd(a.ins_count, 1u)] = n;
+  if (sink) {
+    const uint32_t k = atomicAdd(sink->n, 1u);
+    if (k < sink->cap) {
+      sink->ids[k] = n;
+      return;
+    }
+  }
+  a.ins_queue[atomicAdd(a.ins_count, 1u)] = n;
 }
 __device__ __forceinline__ void flush_sink(const ForestArgs& a, const IdSink& sink, uint32_t* base) {
   __syncthreads();
-  const uint32_t cnt = *sink.n;
+  const uint32_t cnt = min(*sink.n, sink.cap);
   if (cnt == 0) return;
   if (threadIdx.x == 0) *base = atomicAdd(a.ins_count, cnt);
   __syncthreads();
@@ -198,6 +206,7 @@ __device__ __forceinline__ bool digest_wanted(int pass, uint8_t lab) {
 // src/tree_approach.cpp:378-404, duplicate forest :413-477, or both: pass 2)
 // given its children's labels and digests; `dg` receives n's digest when n is
 // hashed.  First-occurrence inserts go to the block's sink.
+template <int HK>
 __device__ __forceinline__ uint8_t span_node(const ForestArgs& a, int pass, uint32_t n, uint8_t ll, uint8_t lr,
                                              const Digest& dl, const Digest& dr, Digest& dg, bool store,
                                              IdSink* sink) {
@@ -206,7 +215,7 @@ __device__ __forceinline__ uint8_t span_node(const ForestArgs& a, int pass, uint
   if (pass == 0) {
     if (ll == FIRST_OCUR && lr == FIRST_OCUR) {
       lab_n = FIRST_OCUR;
-      dg = hash_pair(a.hash_kind, dl, dr);
+      dg = hash_pair(HK, dl, dr);
       st_digest(a.tree + n, dg);
       queue_insert(a, sink, n);
     } else {
@@ -221,7 +230,7 @@ __device__ __forceinline__ uint8_t span_node(const ForestArgs& a, int pass, uint
     } else if (ll == FIXED_DUPL) {
       lab_n = FIXED_DUPL;
     } else if (ll == SHIFT_DUPL) {
-      dg = hash_pair(a.hash_kind, dl, dr);
+      dg = hash_pair(HK, dl, dr);
       st_digest(a.tree + n, dg);
       if (map_find(a.map, dg, a.err) >= 0) {
         lab_n = SHIFT_DUPL;
@@ -233,7 +242,7 @@ __device__ __forceinline__ uint8_t span_node(const ForestArgs& a, int pass, uint
     } else if (ll == FIRST_OCUR) {
       lab_n = FIRST_OCUR;
       if (pass == 2) {
-        dg = hash_pair(a.hash_kind, dl, dr);
+        dg = hash_pair(HK, dl, dr);
         st_digest(a.tree + n, dg);
         queue_insert(a, sink, n);
       }
@@ -249,6 +258,7 @@ __device__ __forceinline__ uint8_t span_node(const ForestArgs& a, int pass, uint
 
 // Node n on the deepest interior level: a leaf there (a ragged last level)
 // keeps its label and stored digest; an interior node is computed.
+template <int HK>
 __device__ __forceinline__ uint8_t span_label(const ForestArgs& a, int pass, uint64_t n, uint64_t last_interior,
                                               uint64_t M, uint8_t ll, uint8_t lr, const Digest& dl,
                                               const Digest& dr, Digest& dg, IdSink* sink) {
@@ -257,7 +267,7 @@ __device__ __forceinline__ uint8_t span_label(const ForestArgs& a, int pass, uin
     if (digest_wanted(pass, lab)) dg = ld_digest(a.tree + n);
     return lab;
   }
-  return span_node(a, pass, (uint32_t)n, ll, lr, dl, dr, dg, false, sink);
+  return span_node<HK>(a, pass, (uint32_t)n, ll, lr, dl, dr, dg, false, sink);
 }
 
 __device__ __forceinline__ Digest shfl_digest(const Digest& d, int src) {
@@ -271,11 +281,12 @@ __device__ __forceinline__ Digest shfl_digest(const Digest& d, int src) {
 // five inside each warp (children's labels and digests by shuffle), then
 // three in warp 0 from the eight warps' results.  Stores r's label.  Every
 // node here is interior.
+template <int HK>
 __device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint64_t r, uint8_t lab, Digest dg,
                                              IdSink* sink, uint8_t* top8, Digest* topdg) {
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr unsigned kFull = 0xffffffffu;
-#pragma unroll
+#pragma unroll 1
   for (uint32_t step = 1; step <= 5; step++) {
     const int sl = (2 * lane) & 31, sr = (2 * lane + 1) & 31;
     const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, sl);
@@ -288,7 +299,7 @@ __device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint
     const uint32_t width = 32u >> step;
     if (lane < width) {
       const uint64_t n = (r + 1) * (256u >> step) - 1 + warp * width + lane;
-      lab = span_node(a, pass, (uint32_t)n, cl, cr, dl, dr, dg, false, sink);
+      lab = span_node<HK>(a, pass, (uint32_t)n, cl, cr, dl, dr, dg, false, sink);
     }
   }
   if (lane == 0) {
@@ -299,7 +310,7 @@ __device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint
   if (warp == 0) {
     lab = lane < 8 ? top8[lane] : DONE;
     if (lane < 8) dg = topdg[lane];
-#pragma unroll
+#pragma unroll 1
     for (uint32_t step = 6; step <= 8; step++) {
       const int sl = (2 * lane) & 31, sr = (2 * lane + 1) & 31;
       const uint8_t cl = (uint8_t)__shfl_sync(kFull, lab, sl);
@@ -308,7 +319,7 @@ __device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint
       const uint32_t width = 256u >> step;
       if (lane < width) {
         const uint64_t n = (r + 1) * width - 1 + lane;
-        lab = span_node(a, pass, (uint32_t)n, cl, cr, dl, dr, dg, step == 8, sink);
+        lab = span_node<HK>(a, pass, (uint32_t)n, cl, cr, dl, dr, dg, step == 8, sink);
       }
     }
   }
@@ -319,10 +330,11 @@ __device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint
 // come from memory, the rest by upper_levels -- one block barrier instead of
 // nine, and no digest goes through memory between levels (they are still
 // stored: the tree keeps every digest for the next checkpoint).
+template <int HK>
 __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
   __shared__ uint8_t top8[8];
   __shared__ Digest topdg[8];
-  __shared__ uint32_t ids[(1u << kSpanLevels) - 1];
+  __shared__ uint32_t ids[(1u << kSpanLevels) - 1];  // one per interior node: never overflows
   __shared__ uint32_t ids_n, ids_base;
   const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
   const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
@@ -331,7 +343,7 @@ __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, in
   if (pass < 0) return;
   if (threadIdx.x == 0) ids_n = 0;
   __syncthreads();
-  IdSink sink{ids, &ids_n};
+  IdSink sink{ids, &ids_n, (1u << kSpanLevels) - 1};
   uint8_t lab;
   Digest dg{{0, 0, 0, 0}};
   {
@@ -347,28 +359,27 @@ __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, in
         dr = ld_digest(a.tree + c + 1);
       }
     }
-    lab = span_label(a, pass, n, last_interior, M, ll, lr, dl, dr, dg, &sink);
+    lab = span_label<HK>(a, pass, n, last_interior, M, ll, lr, dl, dr, dg, &sink);
   }
-  upper_levels(a, pass, r, lab, dg, &sink, top8, topdg);
+  upper_levels<HK>(a, pass, r, lab, dg, &sink, top8, topdg);
   if (pass != 1) flush_sink(a, sink, &ids_base);
-}
-
-__device__ __forceinline__ uint8_t label_byte(const uint32_t cw[4], int j) {
-  return (uint8_t)(cw[j >> 2] >> (8 * (j & 3)));
 }
 
 // The bottom span of an incremental pass (and of the baseline's
 // first-occurrence pass): 12 levels, 4096 leaves per block.  Each thread
 // reads the labels of its 16 children with one aligned 16-byte load (the
-// first byte comes from the lane before) and carries its 8, 4, 2 and 1 nodes
-// in registers, depth first; a thread whose 16 children are all unchanged
-// (fixed duplicates) has nothing to hash, flag or insert.  upper_levels does
-// the rest.
+// first byte comes from the lane before) and computes its 8, 4, 2 and 1 nodes
+// in a loop, labels packed in a 64-bit word, digests in shared memory; a
+// thread whose 16 children are all unchanged (fixed duplicates) has nothing
+// to hash, flag or insert.  upper_levels does the rest.  Loops rather than
+// unrolled levels keep the kernel small enough for the instruction cache.
+template <int HK>
 __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
   __shared__ uint8_t top8[8];
   __shared__ Digest topdg[8];
-  __shared__ uint32_t ids[(1u << kBottomLevels) - 1];
+  __shared__ uint32_t ids[kBottomSink];
   __shared__ uint32_t ids_n, ids_base;
+  __shared__ Digest work[8][256];  // [node of the thread's level][thread]: 16-byte lanes, no bank conflicts
   const uint64_t r = ((1ull << d_top) - 1) + blockIdx.x;
   const uint64_t last_interior = (uint64_t)N - 2, M = 2ull * N - 1;
   if (r > last_interior) return;
@@ -376,7 +387,7 @@ __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int 
   if (pass < 0) return;
   if (threadIdx.x == 0) ids_n = 0;
   __syncthreads();
-  IdSink sink{ids, &ids_n};
+  IdSink sink{ids, &ids_n, kBottomSink};
   const uint32_t t = threadIdx.x, lane = t & 31;
   constexpr unsigned kFull = 0xffffffffu;
   // children (relative depth 12) cb .. cb+15; cb + 1 is a multiple of 16
@@ -395,48 +406,53 @@ __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int 
   }
   uint32_t first = __shfl_up_sync(kFull, v.w, 1) >> 24;  // byte 15 of the lane before = child cb
   if (lane == 0) first = cb < M ? a.labels[cb] : DONE;
-  const uint32_t cw[4] = {(v.x << 8) | first, (v.y << 8) | (v.x >> 24), (v.z << 8) | (v.y >> 24),
-                          (v.w << 8) | (v.z >> 24)};
+  // child j's label is byte j of (lo, hi)
+  uint64_t lo = ((uint64_t)((v.y << 8) | (v.x >> 24)) << 32) | ((v.x << 8) | first);
+  uint64_t hi = ((uint64_t)((v.w << 8) | (v.z >> 24)) << 32) | ((v.y >> 24) | (v.z << 8));
   const uint64_t nb1 = (r + 1) * 2048 - 1 + 8ull * t;  // relative depth 11: the deepest interior level
   uint8_t lab;
   Digest dg{{0, 0, 0, 0}};
-  if (cw[0] == kFixed4 && cw[1] == kFixed4 && cw[2] == kFixed4 && cw[3] == kFixed4 && nb1 + 7 <= last_interior) {
+  constexpr uint64_t kFixed8 = 0x0101010101010101ull * FIXED_DUPL;
+  if (lo == kFixed8 && hi == kFixed8 && nb1 + 7 <= last_interior) {
     lab = pass == 0 ? DONE : FIXED_DUPL;
   } else {
-    uint8_t l3[2];
-    Digest d3[2];
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-      uint8_t l2[2];
-      Digest d2[2];
-#pragma unroll
-      for (int p = 0; p < 2; p++) {
-        uint8_t l1[2];
-        Digest d1[2];
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-          const int k = 4 * q + 2 * p + i;
-          const uint64_t n = nb1 + k;
-          const uint8_t ll = label_byte(cw, 2 * k), lr = label_byte(cw, 2 * k + 1);
-          Digest dl{{0, 0, 0, 0}}, dr{{0, 0, 0, 0}};
-          d1[i] = Digest{{0, 0, 0, 0}};
-          if (n <= last_interior && ll == lr && digest_wanted(pass, ll)) {
-            dl = ld_digest(a.tree + 2 * n + 1);
-            dr = ld_digest(a.tree + 2 * n + 2);
+    uint64_t nb = nb1;
+    uint32_t width = 8;
+#pragma unroll 1
+    for (int lvl = 0; lvl < 4; lvl++) {
+      uint64_t out = 0;
+#pragma unroll 1
+      for (uint32_t i = 0; i < width; i++) {
+        const uint32_t j = 2 * i;
+        const uint8_t ll = (uint8_t)((j < 8 ? lo >> (8 * j) : hi >> (8 * (j - 8))) & 0xff);
+        const uint8_t lr = (uint8_t)((j + 1 < 8 ? lo >> (8 * (j + 1)) : hi >> (8 * (j - 7))) & 0xff);
+        const uint64_t n = nb + i;
+        Digest dl{{0, 0, 0, 0}}, dr{{0, 0, 0, 0}}, d{{0, 0, 0, 0}};
+        if (ll == lr && digest_wanted(pass, ll)) {
+          if (lvl == 0) {
+            if (n <= last_interior) {
+              dl = ld_digest(a.tree + 2 * n + 1);
+              dr = ld_digest(a.tree + 2 * n + 2);
+            }
+          } else {
+            dl = work[j][t];
+            dr = work[j + 1][t];
           }
-          l1[i] = span_label(a, pass, n, last_interior, M, ll, lr, dl, dr, d1[i], &sink);
         }
-        d2[p] = Digest{{0, 0, 0, 0}};
-        l2[p] = span_node(a, pass, (uint32_t)((r + 1) * 1024 - 1 + 4 * t + 2 * q + p), l1[0], l1[1], d1[0], d1[1],
-                          d2[p], false, &sink);
+        const uint8_t l = lvl == 0 ? span_label<HK>(a, pass, n, last_interior, M, ll, lr, dl, dr, d, &sink)
+                                   : span_node<HK>(a, pass, (uint32_t)n, ll, lr, dl, dr, d, false, &sink);
+        if (digest_wanted(pass, l)) work[i][t] = d;  // read back only at the next level, from a higher index
+        out |= (uint64_t)l << (8 * i);
+        if (lvl == 3) dg = d;
       }
-      d3[q] = Digest{{0, 0, 0, 0}};
-      l3[q] = span_node(a, pass, (uint32_t)((r + 1) * 512 - 1 + 2 * t + q), l2[0], l2[1], d2[0], d2[1], d3[q],
-                        false, &sink);
+      lo = out;
+      hi = 0;
+      nb = (nb - 1) / 2;  // parent of the level's first node
+      width >>= 1;
     }
-    lab = span_node(a, pass, (uint32_t)((r + 1) * 256 - 1 + t), l3[0], l3[1], d3[0], d3[1], dg, false, &sink);
+    lab = (uint8_t)lo;
   }
-  upper_levels(a, pass, r, lab, dg, &sink, top8, topdg);
+  upper_levels<HK>(a, pass, r, lab, dg, &sink, top8, topdg);
   if (pass != 1) flush_sink(a, sink, &ids_base);
 }
 
@@ -459,17 +475,18 @@ __global__ void forest_insert_kernel(ForestArgs a) {
 __device__ __forceinline__ uint32_t node_at(const ForestArgs& a, uint64_t p) {
   if (a.ascending) return (uint32_t)p + 1;
   if (p < a.sizeD) return (uint32_t)(((1ull << a.D) - 1) + p);
-  uint64_t q = p - a.sizeD;  // within levels D-1, D-2, ... of sizes 2^(D-1), 2^(D-2), ...
-  int d = (int)a.D - 1;
-  while (d > 0 && q >= (1ull << d)) { q -= 1ull << d; d--; }
-  return (uint32_t)(((1ull << d) - 1) + q);
+  // levels D-1, D-2, ... follow with sizes 2^(D-1), 2^(D-2), ...: position q
+  // past level D lies on level d with x = 2^D - q in (2^d, 2^(d+1)]
+  const uint64_t x = (1ull << a.D) - (p - a.sizeD);
+  const int d = 63 - __clzll((long long)(x - 1));
+  return (uint32_t)(((1ull << d) - 1) + ((2ull << d) - x));
 }
 
-// 128 contiguous flags per thread (eight 16-byte loads), 64 Ki flags per
+// 64 contiguous flags per thread (four 16-byte loads), 32 Ki flags per
 // tile; counts packed as (shift << 32) | fo.  Flag bytes are 0, 1 (first
 // occurrence) or 2 (shifted duplicate), so bit 0 and bit 1 of each byte
 // count the two kinds.
-constexpr int kRootVec = 8;
+constexpr int kRootVec = 4;
 constexpr uint64_t kRootPerThread = 16 * kRootVec;
 constexpr uint64_t kRootTile = kRootPerThread * kScanThreads;
 static_assert(ROOT_FO == 1 && ROOT_SHIFT == 2, "flag bytes counted by bit");
@@ -478,9 +495,9 @@ __device__ __forceinline__ uint64_t count_word(uint32_t w) {
   return (uint64_t)__popc(w & 0x01010101u) | ((uint64_t)__popc(w & 0x02020202u) << 32);
 }
 
-// The thread's 128 flags starting at p (p a multiple of 128); bytes at or past
-// n read as ROOT_NONE.
-__device__ __forceinline__ uint64_t load_flags128(const uint8_t* f, uint64_t p, uint64_t n, uint4 v[kRootVec]) {
+// The thread's flags starting at p (p a multiple of 16); bytes at or past n
+// read as ROOT_NONE.
+__device__ __forceinline__ uint64_t load_flags(const uint8_t* f, uint64_t p, uint64_t n, uint4 v[kRootVec]) {
   uint64_t c = 0;
 #pragma unroll
   for (int k = 0; k < kRootVec; k++) {
@@ -503,7 +520,7 @@ __global__ void __launch_bounds__(kScanThreads) root_count_kernel(const uint8_t*
   __shared__ uint64_t sh[33];
   const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
   uint4 v[kRootVec];
-  const uint64_t c = p < n ? load_flags128(rflag, p, n, v) : 0;
+  const uint64_t c = p < n ? load_flags(rflag, p, n, v) : 0;
   uint64_t total;
   block_excl_scan(c, sh, &total);
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
@@ -514,7 +531,7 @@ __global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, u
   __shared__ uint64_t sh[33];
   const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
   uint4 v[kRootVec];
-  const uint64_t c = p < n ? load_flags128(a.rflag, p, n, v) : 0;
+  const uint64_t c = p < n ? load_flags(a.rflag, p, n, v) : 0;
   uint64_t ex = block_excl_scan(c, sh, nullptr) + tile_off[blockIdx.x];
   if (!c) return;
   const uint32_t root = lay->root_fo;
@@ -561,8 +578,14 @@ __global__ void fo_prep_kernel(GatherArgs g) {
     uint32_t node = g.fo_list[i];
     uint64_t v = 0;
     if (g.approach == APPROACH_TREE) {
-      NodeIdDev prev = slot_value(g.map, map_find(g.map, ld_digest(g.digests + node), g.err));
-      if (prev.node == node && prev.tree == cur) v = (1ull << 32) | num_leaf_descendents(node, g.M);
+      // a first-occurrence leaf owns its digest: the leaf pass demotes every
+      // other one (same checkpoint id, another owner)
+      bool owner = node >= g.N - 1;
+      if (!owner) {
+        NodeIdDev prev = slot_value(g.map, map_find(g.map, ld_digest(g.digests + node), g.err));
+        owner = prev.node == node && prev.tree == cur;
+      }
+      if (owner) v = (1ull << 32) | num_leaf_descendents(node, g.M);
     } else {
       v = (1ull << 32) | 1ull;  // list / basic: one chunk per entry
     }
@@ -592,17 +615,26 @@ __global__ void fo_totals_kernel(const uint64_t* total, Layout* lay) {
 }
 
 // Shifted duplicates: (source checkpoint, source node) of each root.
+// The histogram of source checkpoints is warp-aggregated: most entries share
+// a few keys.
 __global__ void shift_prep_kernel(GatherArgs g) {
   const uint32_t S = g.lay->S;
   const uint32_t cur = g.sp->cur;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t node = g.sh_list[i];
-    int64_t slot = map_find(g.map, ld_digest(g.digests + node), g.err);
-    NodeIdDev prev = slot_value(g.map, slot);
-    if (slot < 0 || prev.tree > cur) { atomicOr(g.err, DERR_MISSING); prev.tree = 0; prev.node = 0; }
-    g.sh_key[i] = prev.tree;
-    g.sh_prev[i] = prev.node;
-    atomicAdd(&g.hist[prev.tree], 1u);
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x; b < S; b += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = b + threadIdx.x;
+    uint32_t key = 0xffffffffu;
+    if (i < S) {
+      uint32_t node = g.sh_list[i];
+      int64_t slot = map_find(g.map, ld_digest(g.digests + node), g.err);
+      NodeIdDev prev = slot_value(g.map, slot);
+      if (slot < 0 || prev.tree > cur) { atomicOr(g.err, DERR_MISSING); prev.tree = 0; prev.node = 0; }
+      g.sh_key[i] = prev.tree;
+      g.sh_prev[i] = prev.node;
+      key = prev.tree;
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&g.hist[key], (uint32_t)__popc(peers));
   }
 }
 
@@ -620,6 +652,7 @@ __global__ void layout_kernel(GatherArgs g) {
     smax = 0;
     lay->nkeys = 0;  // set below once the keys are known
     lay->sort_n = 0;
+    lay->sort_tiles = 0;
   }
   __syncthreads();
   uint32_t P = 0;
@@ -731,7 +764,8 @@ __global__ void layout_kernel(GatherArgs g) {
     if (g.hist[k] > 0) g.rep[k] = g.rank[g.rep[k]];
   if (threadIdx.x == 0) {
     lay->nkeys = run;
-    const uint32_t T = (uint32_t)((g.N + 1 + kSortTile - 1) / kSortTile) + 1;
+    const uint32_t T = (S + kSortTile - 1) / kSortTile;
+    lay->sort_tiles = T;
     lay->sort_n = run * T;
     if (run > kSortFastKeys) atomicOr(g.err, DERR_SORTKEYS);
   }
@@ -739,15 +773,27 @@ __global__ void layout_kernel(GatherArgs g) {
 
 // Stable counting sort of the shift entries by representative key.
 // Tile t counts its keys; matrix[key * T + t] (key-major).
-__global__ void sort_count_kernel(GatherArgs g, uint32_t T) {
+__global__ void sort_count_kernel(GatherArgs g) {
   extern __shared__ uint32_t cnt[];
-  const uint32_t K = g.lay->nkeys, S = g.lay->S;
+  const uint32_t K = g.lay->nkeys, S = g.lay->S, T = g.lay->sort_tiles;
   if (K > kSortFastKeys) return;
   for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
     const uint64_t b = (uint64_t)t * kSortTile;
-    for (uint64_t i = b + threadIdx.x; i < b + kSortTile && i < S; i += blockDim.x) atomicAdd(&cnt[g.rep[g.sh_key[i]]], 1u);
+    // every load of the tile issued before the first count
+    constexpr int kPer = kSortTile / 256;
+    uint32_t key[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+      const uint64_t i = b + threadIdx.x + 256ull * j;
+      key[j] = i < S ? g.sh_key[i] : 0xffffffffu;
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; j++) key[j] = key[j] != 0xffffffffu ? g.rep[key[j]] : 0xffffffffu;
+#pragma unroll
+    for (int j = 0; j < kPer; j++)
+      if (key[j] != 0xffffffffu) atomicAdd(&cnt[key[j]], 1u);
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) g.sort_mat[(uint64_t)k * T + t] = cnt[k];
     __syncthreads();
@@ -766,11 +812,11 @@ struct MatEmit {
 // memory), then the per-key counts of earlier warps and the tile's global
 // base (key-major scan of sort_mat) give each entry its position.
 constexpr int kSortWarps = 8;
-__global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g, uint32_t T) {
+__global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g) {
   __shared__ uint32_t keys[kSortTile];
   __shared__ uint32_t lrank[kSortTile];
   extern __shared__ uint32_t cnt[];  // [kSortWarps][K]
-  const uint32_t K = g.lay->nkeys, S = g.lay->S;
+  const uint32_t K = g.lay->nkeys, S = g.lay->S, T = g.lay->sort_tiles;
   if (!g.lay->ok || K > kSortFastKeys) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr uint32_t kSlice = kSortTile / kSortWarps;
@@ -779,7 +825,20 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g, uint32_
     const uint64_t b = (uint64_t)t * kSortTile;
     if (b >= S) break;
     const uint32_t n = (uint32_t)(S - b < kSortTile ? S - b : kSortTile);
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) keys[i] = g.rep[g.sh_key[b + i]];
+    constexpr int kPer = kSortTile / 256;
+    {
+      uint32_t kk[kPer];
+#pragma unroll
+      for (int j = 0; j < kPer; j++) {
+        const uint32_t i = threadIdx.x + 256u * j;
+        kk[j] = i < n ? g.sh_key[b + i] : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < kPer; j++) {
+        const uint32_t i = threadIdx.x + 256u * j;
+        if (i < n) keys[i] = g.rep[kk[j]];
+      }
+    }
     for (uint32_t k = threadIdx.x; k < kSortWarps * K; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
     uint32_t* wc = cnt + warp * K;
@@ -807,11 +866,23 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g, uint32_
       }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const uint32_t pos = cnt[(i / kSlice) * K + keys[i]] + lrank[i];
-      uint32_t* e = reinterpret_cast<uint32_t*>(pairs + 8ull * pos);
-      e[0] = g.sh_list[b + i];
-      e[1] = g.sh_prev[b + i];
+    {
+      uint32_t nd[kPer], pv[kPer];
+#pragma unroll
+      for (int j = 0; j < kPer; j++) {
+        const uint32_t i = threadIdx.x + 256u * j;
+        nd[j] = i < n ? g.sh_list[b + i] : 0;
+        pv[j] = i < n ? g.sh_prev[b + i] : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < kPer; j++) {
+        const uint32_t i = threadIdx.x + 256u * j;
+        if (i >= n) continue;
+        const uint32_t pos = cnt[(i / kSlice) * K + keys[i]] + lrank[i];
+        uint32_t* e = reinterpret_cast<uint32_t*>(pairs + 8ull * pos);  // 4-byte aligned only
+        e[0] = nd[j];
+        e[1] = pv[j];
+      }
     }
     __syncthreads();
   }
@@ -842,11 +913,13 @@ __global__ void copy_kernel(GatherArgs g) {
     if (g.reg_slot[mid] <= slot) lo = mid; else hi = mid - 1;
   }
   uint32_t r = lo;
-  for (; u < u1; u += blockDim.x) {
-    slot = u * 16 / cs;
-    while (r + 1 < R && g.reg_slot[r + 1] <= slot) r++;
-    const uint64_t within = u * 16 - slot * cs;
-    const uint64_t chunk = (uint64_t)g.reg_chunk[r] + (slot - g.reg_slot[r]);
+  // one 16-byte unit of the data section; chunks past the end of the buffer
+  // stay zero (the reference reads out of bounds there)
+  auto load = [&](uint64_t uu) {
+    const uint64_t sl = uu * 16 / cs;
+    while (r + 1 < R && g.reg_slot[r + 1] <= sl) r++;
+    const uint64_t within = uu * 16 - sl * cs;
+    const uint64_t chunk = (uint64_t)g.reg_chunk[r] + (sl - g.reg_slot[r]);
     uint4 v = make_uint4(0, 0, 0, 0);
     if (chunk < last || (chunk == last && within + 16 <= tail_len)) {
       v = __ldcs(reinterpret_cast<const uint4*>(g.data + chunk * cs + within));
@@ -855,8 +928,15 @@ __global__ void copy_kernel(GatherArgs g) {
       for (uint32_t b = 0; b < 16 && within + b < tail_len; b++) w[b >> 2] |= (uint32_t)g.data[chunk * cs + within + b] << (8 * (b & 3));
       v = make_uint4(w[0], w[1], w[2], w[3]);
     }
-    // chunks past the end of the buffer stay zero (the reference reads out of bounds there)
-    __stcs(reinterpret_cast<uint4*>(dst + u * 16), v);
+    return v;
+  };
+  // two units in flight per thread: both loads issue before either store
+  for (; u < u1; u += 2 * (uint64_t)blockDim.x) {
+    const uint64_t ub = u + blockDim.x;
+    const uint4 va = load(u);
+    const uint4 vb = ub < u1 ? load(ub) : make_uint4(0, 0, 0, 0);
+    __stcs(reinterpret_cast<uint4*>(dst + u * 16), va);
+    if (ub < u1) __stcs(reinterpret_cast<uint4*>(dst + ub * 16), vb);
   }
 }
 
@@ -970,7 +1050,8 @@ cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t 
     const uint32_t top = dmax - (kBottomLevels - 1);
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
-    forest_bottom12_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+    if (a.hash_kind == HASH_MD5) forest_bottom12_kernel<HASH_MD5><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+    else forest_bottom12_kernel<HASH_MURMUR3><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
     note_launch();
     bot = (int)top - 1;
   }
@@ -979,7 +1060,8 @@ cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t 
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
     if (!dup_baseline && (uint32_t)bot - top == kSpanLevels - 1)
-      forest_span9_warp_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+      if (a.hash_kind == HASH_MD5) forest_span9_warp_kernel<HASH_MD5><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+      else forest_span9_warp_kernel<HASH_MURMUR3><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
     else
       forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot);
     note_launch();
@@ -1050,11 +1132,13 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
       cudaFuncSetAttribute(sort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sc);
       attr_sc = smem_sc;
     }
-    sort_count_kernel<<<grid_for(T, 1, 16), 256, smem_cnt, s>>>(g, T);
+    // tiles of the actual shift entries, read on the device: small grids
+    const uint32_t gsort = std::min<uint32_t>(T, 2 * num_sms());
+    sort_count_kernel<<<gsort, 256, smem_cnt, s>>>(g);
     e = grid_scan(MatVal{g.sort_mat}, MatEmit{g.sort_mat}, &g.lay->sort_n, (uint64_t)K * T, g.scan_scratch2,
                   g.scan_total2, s);
     if (e != cudaSuccess) return e;
-    sort_scatter_kernel<<<grid_for(T, 1, 16), 256, smem_sc, s>>>(g, T);
+    sort_scatter_kernel<<<gsort, 256, smem_sc, s>>>(g);
     note_launch(2);
   }
   const bool vec = (g.cs % 16 == 0) && ((reinterpret_cast<uintptr_t>(g.data) & 15) == 0);

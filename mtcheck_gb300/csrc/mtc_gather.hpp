@@ -22,7 +22,7 @@ struct Layout {
   uint64_t pad, data_off, table_off, pairs_off, diff_len;
   uint64_t size_data, size_meta;   // the reference's datasizes pair
   uint32_t root_fo, max_key, ok, nkeys;  // nkeys: distinct sort keys of the shift entries
-  uint32_t sort_n, reserved2;             // nkeys * sort tiles
+  uint32_t sort_n, sort_tiles;            // nkeys * sort tiles; tiles of kSortTile shift entries
 };
 
 struct ForestArgs {
