@@ -47,7 +47,6 @@ __device__ __forceinline__ uint8_t child_flag(uint8_t lab) {
 constexpr uint32_t kSpanLevels = 9;     // 256 nodes on the bottom level of a span
 constexpr uint32_t kBottomLevels = 12;  // bottom span: 16 leaves per thread, 4096 per block
 constexpr uint32_t kBottomSink = 2048;  // queued inserts a bottom block holds in shared memory
-constexpr uint32_t kFixed4 = 0x01010101u * FIXED_DUPL;
 
 // First-occurrence inserts are queued (node ids in ForestArgs::ins_queue) and
 // issued by forest_insert_kernel after the pass's last launch: the
@@ -516,25 +515,55 @@ __device__ __forceinline__ uint64_t load_flags(const uint8_t* f, uint64_t p, uin
   return c;
 }
 
-__global__ void __launch_bounds__(kScanThreads) root_count_kernel(const uint8_t* rflag, uint64_t n, uint64_t* tile_sums) {
+// The root itself is pushed only for N >= 2 in the incremental and baseline
+// passes (src/tree_approach.cpp:384-393); the serial reference inserts it
+// whenever it is a first occurrence (include/reference_impl.hpp:105-106).
+__device__ __forceinline__ void root_prologue(const uint8_t* labels, uint32_t N, int ascending, uint32_t* fo_list,
+                                              Layout* lay) {
+  const uint32_t root = (labels[0] == FIRST_OCUR && (ascending || N >= 2)) ? 1u : 0u;
+  lay->root_fo = root;
+  if (root) fo_list[0] = 0;
+}
+
+__global__ void __launch_bounds__(kScanThreads) root_count_kernel(ForestArgs a, uint32_t N, uint64_t n,
+                                                                  uint64_t* tile_sums, uint32_t* fo_list,
+                                                                  Layout* lay) {
   __shared__ uint64_t sh[33];
+  if (blockIdx.x == 0 && threadIdx.x == 0) root_prologue(a.labels, N, a.ascending, fo_list, lay);
   const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
   uint4 v[kRootVec];
-  const uint64_t c = p < n ? load_flags(rflag, p, n, v) : 0;
+  const uint64_t c = p < n ? load_flags(a.rflag, p, n, v) : 0;
   uint64_t total;
   block_excl_scan(c, sh, &total);
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
+// Emits the roots in serial push order.  kReduce: the tile offset is the sum of
+// the earlier tiles' counts (few tiles), and the last tile sets F and S;
+// otherwise tile_off holds scanned offsets and root_epilogue_kernel follows.
+template <bool kReduce>
 __global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, uint64_t n, const uint64_t* tile_off,
-                                                                 uint32_t* fo_list, uint32_t* sh_list, const Layout* lay) {
+                                                                 uint32_t* fo_list, uint32_t* sh_list, Layout* lay) {
   __shared__ uint64_t sh[33];
+  uint64_t off = 0;
+  if (kReduce) {
+    uint64_t part = 0;
+    for (uint32_t k = threadIdx.x; k < blockIdx.x; k += blockDim.x) part += tile_off[k];
+    block_excl_scan(part, sh, &off);
+  } else {
+    off = tile_off[blockIdx.x];
+  }
   const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
   uint4 v[kRootVec];
   const uint64_t c = p < n ? load_flags(a.rflag, p, n, v) : 0;
-  uint64_t ex = block_excl_scan(c, sh, nullptr) + tile_off[blockIdx.x];
-  if (!c) return;
+  uint64_t tile_total;
+  uint64_t ex = block_excl_scan(c, sh, &tile_total) + off;
   const uint32_t root = lay->root_fo;
+  if (kReduce && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    lay->F = root + (uint32_t)(off + tile_total);
+    lay->S = (uint32_t)((off + tile_total) >> 32);
+  }
+  if (!c) return;
 #pragma unroll
   for (int k = 0; k < kRootVec; k++) {
     const uint32_t w4[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
@@ -554,14 +583,6 @@ __global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, u
   }
 }
 
-__global__ void root_prologue_kernel(const uint8_t* labels, uint32_t N, int ascending, uint32_t* fo_list, Layout* lay) {
-  // the incremental/baseline passes push the root only for N >= 2
-  // (src/tree_approach.cpp:384-393); the serial reference inserts it whenever
-  // it is a first occurrence (include/reference_impl.hpp:105-106)
-  uint32_t root = (labels[0] == FIRST_OCUR && (ascending || N >= 2)) ? 1u : 0u;
-  lay->root_fo = root;
-  if (root) fo_list[0] = 0;
-}
 __global__ void root_epilogue_kernel(const uint64_t* total, Layout* lay) {
   lay->F = lay->root_fo + (uint32_t)(*total);
   lay->S = (uint32_t)(*total >> 32);
@@ -609,10 +630,6 @@ struct FoEmit {
     if (g.lay->ok) *reinterpret_cast<uint32_t*>(g.stage + g.lay->pad + 32 + 4ull * r) = node;
   }
 };
-__global__ void fo_totals_kernel(const uint64_t* total, Layout* lay) {
-  lay->num_distinct = (uint32_t)(*total >> 32);
-  lay->chunk_counter = (uint32_t)(*total);
-}
 
 // Shifted duplicates: (source checkpoint, source node) of each root.
 // The histogram of source checkpoints is warp-aggregated: most entries share
@@ -640,9 +657,27 @@ __global__ void shift_prep_kernel(GatherArgs g) {
 
 // One block: repeat-count table, layout, header; bin representatives for the
 // list approach's BinOp1D.
-__global__ void layout_kernel(GatherArgs g) {
+// First, the tile sums of the region-size scan become tile offsets in place,
+// and their total gives the region count and the data chunk count.
+__global__ void layout_kernel(GatherArgs g, uint32_t ntiles) {
   __shared__ uint64_t sh[33];
   Layout* lay = g.lay;
+  {
+    uint64_t carry = 0;
+    for (uint32_t b = 0; b < ntiles; b += blockDim.x) {
+      const uint32_t i = b + threadIdx.x;
+      const uint64_t v = i < ntiles ? g.scan_scratch[i] : 0;
+      uint64_t t;
+      const uint64_t ex = block_excl_scan(v, sh, &t);
+      if (i < ntiles) g.scan_scratch[i] = carry + ex;
+      carry += t;
+    }
+    if (threadIdx.x == 0) {
+      lay->num_distinct = (uint32_t)(carry >> 32);
+      lay->chunk_counter = (uint32_t)carry;
+    }
+    __syncthreads();
+  }
   const uint32_t cur = g.sp->cur;
   const uint32_t K = cur + 1;
   const uint32_t F = lay->F, S = lay->S, nd = lay->num_distinct;
@@ -1080,12 +1115,16 @@ cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M,
   const uint64_t n = (uint64_t)M - 1;  // every node but the root
   uint32_t ntiles = (uint32_t)((n + kRootTile - 1) / kRootTile);
   if (ntiles == 0) ntiles = 1;
-  root_prologue_kernel<<<1, 1, 0, s>>>(fa.labels, N, fa.ascending, fo_list, lay);
-  root_count_kernel<<<ntiles, kScanThreads, 0, s>>>(fa.rflag, n, scan_scratch);
+  root_count_kernel<<<ntiles, kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay);
+  if (ntiles <= kReduceTiles) {
+    root_emit_kernel<true><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
+    note_launch(2);
+    return cudaGetLastError();
+  }
   scan_tile_offsets_kernel<<<1, 1024, 0, s>>>(scan_scratch, ntiles, scan_total);
-  root_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
+  root_emit_kernel<false><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
   root_epilogue_kernel<<<1, 1, 0, s>>>(scan_total, lay);
-  note_launch(5);
+  note_launch(4);
   return cudaGetLastError();
 }
 
@@ -1114,11 +1153,9 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   uint32_t ntiles = (uint32_t)((max_entries + kScanTile - 1) / kScanTile);
   if (ntiles == 0) ntiles = 1;
   scan_tile_sums_kernel<<<ntiles, kScanThreads, 0, s>>>(FoVal{g.fo_val}, &g.lay->F, 0, g.scan_scratch);
-  scan_tile_offsets_kernel<<<1, 1024, 0, s>>>(g.scan_scratch, ntiles, g.scan_total);
-  fo_totals_kernel<<<1, 1, 0, s>>>(g.scan_total, g.lay);
-  layout_kernel<<<1, 1024, 0, s>>>(g);
+  layout_kernel<<<1, 1024, 0, s>>>(g, ntiles);
   scan_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(FoVal{g.fo_val}, FoEmit{g}, &g.lay->F, 0, g.scan_scratch);
-  note_launch(7);
+  note_launch(5);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (g.approach != APPROACH_BASIC) {
     // bound on the distinct keys (source checkpoints): at most k_cap, which

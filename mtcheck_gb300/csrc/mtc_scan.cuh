@@ -107,7 +107,42 @@ __global__ void scan_emit_kernel(Val val, Emit emit, const uint32_t* n_ptr, uint
   }
 }
 
-// Host helper: run the three phases.  `scratch` holds >= ceil(max_n/kScanTile)+1
+// Phases 2 and 3 in one launch, for grids of at most kReduceTiles tiles: each
+// block sums the sums of the tiles before it; the block holding element n-1
+// (block 0 when n is 0) writes the grand total.
+constexpr uint32_t kReduceTiles = 2048;
+template <class Val, class Emit>
+__global__ void scan_emit_reduce_kernel(Val val, Emit emit, const uint32_t* n_ptr, uint64_t n_const,
+                                        const uint64_t* tile_sums, uint64_t* total) {
+  __shared__ uint64_t sh[33];
+  const uint64_t n = n_ptr ? *n_ptr : n_const;
+  const uint64_t last_tile = n ? (n - 1) / kScanTile : 0;
+  if (blockIdx.x > last_tile) return;
+  uint64_t part = 0;
+  for (uint32_t k = threadIdx.x; k < blockIdx.x; k += blockDim.x) part += tile_sums[k];
+  uint64_t off;
+  block_excl_scan(part, sh, &off);
+  const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+  uint64_t v[kScanPerThread];
+  uint64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; k++) {
+    uint64_t i = base + (uint64_t)threadIdx.x * kScanPerThread + k;
+    v[k] = i < n ? val(i) : 0;
+    s += v[k];
+  }
+  uint64_t tile_total;
+  uint64_t ex = block_excl_scan(s, sh, &tile_total) + off;
+  if (total && blockIdx.x == last_tile && threadIdx.x == 0) *total = off + tile_total;
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; k++) {
+    uint64_t i = base + (uint64_t)threadIdx.x * kScanPerThread + k;
+    if (i < n) emit(i, ex, v[k]);
+    ex += v[k];
+  }
+}
+
+// Host helper: run the three phases (two launches up to kReduceTiles tiles).  `scratch` holds >= ceil(max_n/kScanTile)+1
 // u64; `total` (device) receives the grand total.
 template <class Val, class Emit>
 inline cudaError_t grid_scan(Val val, Emit emit, const uint32_t* n_dev, uint64_t max_n, uint64_t* scratch,
@@ -115,6 +150,11 @@ inline cudaError_t grid_scan(Val val, Emit emit, const uint32_t* n_dev, uint64_t
   uint32_t ntiles = (uint32_t)((max_n + kScanTile - 1) / kScanTile);
   if (ntiles == 0) ntiles = 1;
   scan_tile_sums_kernel<<<ntiles, kScanThreads, 0, s>>>(val, n_dev, max_n, scratch);
+  if (ntiles <= kReduceTiles) {
+    scan_emit_reduce_kernel<<<ntiles, kScanThreads, 0, s>>>(val, emit, n_dev, max_n, scratch, total);
+    note_launch(2);
+    return cudaGetLastError();
+  }
   scan_tile_offsets_kernel<<<1, 1024, 0, s>>>(scratch, ntiles, total);
   scan_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(val, emit, n_dev, max_n, scratch);
   note_launch(3);
