@@ -455,16 +455,26 @@ __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int 
   if (pass != 1) flush_sink(a, sink, &ids_base);
 }
 
-// The queued first-occurrence inserts of a pass, one thread per node.
-__global__ void forest_insert_kernel(ForestArgs a) {
+// The queued first-occurrence inserts of a pass, one thread per node, over
+// blocks b0 .. b0+nb-1 of the launch.
+__device__ __forceinline__ void drain_inserts(const ForestArgs& a, uint32_t b0, uint32_t nb) {
   const uint32_t n = *a.ins_count;
   const uint32_t cur_id = a.sp->cur, epoch_fo = a.sp->epoch + 1;
   uint32_t created = 0;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+  for (uint32_t k = (blockIdx.x - b0) * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
     const uint32_t node = a.ins_queue[k];
     created += map_insert_serial(a.map, ld_digest(a.tree + node), node, cur_id, epoch_fo, a.err);
   }
   count_new_entries(a.map, created);
+}
+__device__ __forceinline__ bool forest_fused(const ForestArgs& a) { return a.fuse_gate && *a.fuse_gate == 0; }
+
+// After the first-occurrence pass: the duplicate pass that follows looks its
+// digests up.  A fused pass looks nothing up that these inserts could add,
+// so its inserts wait for the root count (root_count_kernel's extra blocks).
+__global__ void forest_insert_kernel(ForestArgs a) {
+  if (forest_fused(a)) return;
+  drain_inserts(a, 0, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -525,10 +535,16 @@ __device__ __forceinline__ void root_prologue(const uint8_t* labels, uint32_t N,
   if (root) fo_list[0] = 0;
 }
 
+// Blocks past the tiles issue a fused forest pass's queued inserts, which only
+// the assembly's ownership test and later checkpoints read.
 __global__ void __launch_bounds__(kScanThreads) root_count_kernel(ForestArgs a, uint32_t N, uint64_t n,
                                                                   uint64_t* tile_sums, uint32_t* fo_list,
-                                                                  Layout* lay) {
+                                                                  Layout* lay, uint32_t ntiles) {
   __shared__ uint64_t sh[33];
+  if (blockIdx.x >= ntiles) {
+    if (forest_fused(a)) drain_inserts(a, ntiles, gridDim.x - ntiles);
+    return;
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) root_prologue(a.labels, N, a.ascending, fo_list, lay);
   const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
   uint4 v[kRootVec];
@@ -592,7 +608,7 @@ __global__ void root_epilogue_kernel(const uint64_t* total, Layout* lay) {
 // Diff assembly
 // ---------------------------------------------------------------------------
 // First-occurrence roots: region size if the root owns its digest.
-__global__ void fo_prep_kernel(GatherArgs g) {
+__device__ __forceinline__ void fo_prep(const GatherArgs& g) {
   const uint32_t F = g.lay->F;
   const uint32_t cur = g.sp->cur;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -634,7 +650,7 @@ struct FoEmit {
 // Shifted duplicates: (source checkpoint, source node) of each root.
 // The histogram of source checkpoints is warp-aggregated: most entries share
 // a few keys.
-__global__ void shift_prep_kernel(GatherArgs g) {
+__device__ __forceinline__ void shift_prep(const GatherArgs& g) {
   const uint32_t S = g.lay->S;
   const uint32_t cur = g.sp->cur;
   const uint32_t lane = threadIdx.x & 31;
@@ -653,6 +669,12 @@ __global__ void shift_prep_kernel(GatherArgs g) {
     const uint32_t peers = __match_any_sync(0xffffffffu, key);
     if (key != 0xffffffffu && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&g.hist[key], (uint32_t)__popc(peers));
   }
+}
+
+// Both root lists' lookups in one launch.
+__global__ void roots_prep_kernel(GatherArgs g) {
+  shift_prep(g);
+  fo_prep(g);
 }
 
 // One block: repeat-count table, layout, header; bin representatives for the
@@ -941,7 +963,11 @@ __global__ void copy_kernel(GatherArgs g) {
   const uint64_t u0 = (uint64_t)blockIdx.x * per_block, u1 = min(u0 + per_block, nunits);
   uint64_t u = u0 + threadIdx.x;
   if (u >= u1) return;
-  uint64_t slot = u * 16 / cs;
+  // 16-byte units per chunk; a power of two (every usual chunk size) is a shift
+  const uint64_t upc = cs / 16;
+  const int lg = (upc & (upc - 1)) == 0 ? __ffsll((long long)upc) - 1 : -1;
+  auto slot_of_unit = [&](uint64_t uu) { return lg >= 0 ? uu >> lg : uu / upc; };
+  uint64_t slot = slot_of_unit(u);
   uint32_t lo = 0, hi = R - 1;
   while (lo < hi) {
     uint32_t mid = (lo + hi + 1) >> 1;
@@ -951,9 +977,9 @@ __global__ void copy_kernel(GatherArgs g) {
   // one 16-byte unit of the data section; chunks past the end of the buffer
   // stay zero (the reference reads out of bounds there)
   auto load = [&](uint64_t uu) {
-    const uint64_t sl = uu * 16 / cs;
+    const uint64_t sl = slot_of_unit(uu);
     while (r + 1 < R && g.reg_slot[r + 1] <= sl) r++;
-    const uint64_t within = uu * 16 - sl * cs;
+    const uint64_t within = (uu - sl * upc) * 16;
     const uint64_t chunk = (uint64_t)g.reg_chunk[r] + (sl - g.reg_slot[r]);
     uint4 v = make_uint4(0, 0, 0, 0);
     if (chunk < last || (chunk == last && within + 16 <= tail_len)) {
@@ -1115,7 +1141,7 @@ cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M,
   const uint64_t n = (uint64_t)M - 1;  // every node but the root
   uint32_t ntiles = (uint32_t)((n + kRootTile - 1) / kRootTile);
   if (ntiles == 0) ntiles = 1;
-  root_count_kernel<<<ntiles, kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay);
+  root_count_kernel<<<ntiles + 2 * num_sms(), kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay, ntiles);
   if (ntiles <= kReduceTiles) {
     root_emit_kernel<true><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
     note_launch(2);
@@ -1147,15 +1173,14 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   // FO emit (metadata + regions), sort, copy.
   cudaMemsetAsync(g.hist, 0, sizeof(uint32_t) * (size_t)g.k_cap, s);
   const uint32_t gs = grid_for(max_entries, 256);
-  shift_prep_kernel<<<gs, 256, 0, s>>>(g);
-  fo_prep_kernel<<<gs, 256, 0, s>>>(g);
+  roots_prep_kernel<<<gs, 256, 0, s>>>(g);
   // region totals first (phase 1+2 of the scan), then layout, then emit
   uint32_t ntiles = (uint32_t)((max_entries + kScanTile - 1) / kScanTile);
   if (ntiles == 0) ntiles = 1;
   scan_tile_sums_kernel<<<ntiles, kScanThreads, 0, s>>>(FoVal{g.fo_val}, &g.lay->F, 0, g.scan_scratch);
   layout_kernel<<<1, 1024, 0, s>>>(g, ntiles);
   scan_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(FoVal{g.fo_val}, FoEmit{g}, &g.lay->F, 0, g.scan_scratch);
-  note_launch(5);
+  note_launch(4);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (g.approach != APPROACH_BASIC) {
     // bound on the distinct keys (source checkpoints): at most k_cap, which
