@@ -364,6 +364,113 @@ __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, in
   if (pass != 1) flush_sink(a, sink, &ids_base);
 }
 
+// Byte-parallel labelling of four (left, right) pairs per 32-bit word, the
+// rules of span_node: P receives the parents' labels, FL / FR the children's
+// root flags (duplicate passes), XF the pairs to hash and insert
+// (first-occurrence passes), XS the pairs to hash and look up (duplicate
+// passes; their parents read SHIFT_DUPL until resolved).  Bytes are 0xff in
+// the X masks.
+constexpr uint32_t kB1 = 0x01010101u;
+__device__ __forceinline__ uint32_t child_flags4(uint32_t x) {
+  const uint32_t sh = __vcmpeq4(x, SHIFT_DUPL * kB1);
+  const uint32_t none = __vcmpeq4(x, FIXED_DUPL * kB1) | __vcmpeq4(x, DONE * kB1);
+  return (sh & (ROOT_SHIFT * kB1)) | (~sh & ~none & (ROOT_FO * kB1));
+}
+__device__ __forceinline__ void label_pairs4(int pass, uint32_t L, uint32_t R, uint32_t& P, uint32_t& FL,
+                                             uint32_t& FR, uint32_t& XF, uint32_t& XS) {
+  const uint32_t eq = __vcmpeq4(L, R);
+  const uint32_t fo = eq & __vcmpeq4(L, FIRST_OCUR * kB1);
+  P = (DONE * kB1) & ~fo;  // FIRST_OCUR is 0
+  FL = FR = XS = 0;
+  XF = pass != 1 ? fo : 0;
+  if (pass != 0) {
+    const uint32_t fix = eq & __vcmpeq4(L, FIXED_DUPL * kB1);
+    const uint32_t sh = eq & __vcmpeq4(L, SHIFT_DUPL * kB1);
+    P = (P & ~(fix | sh)) | (fix & (FIXED_DUPL * kB1)) | (sh & (SHIFT_DUPL * kB1));
+    FL = ~eq & child_flags4(L);
+    FR = ~eq & child_flags4(R);
+    XS = sh;
+  }
+}
+__device__ __forceinline__ void set_byte(uint32_t& w, int b, uint32_t v) {
+  w = (w & ~(0xffu << (8 * b))) | (v << (8 * b));
+}
+
+// A thread's four levels below node (r+1)*256-1+t when its 8 nodes on the
+// deepest interior level are all interior: the 16 children's labels in c[4]
+// (byte j = child j).  Returns the label of the thread's top node and its
+// digest in dg when a parent reads it.
+template <int HK>
+__device__ __forceinline__ uint8_t thread_levels_bytewise(const ForestArgs& a, int pass, uint64_t r, uint32_t t,
+                                                          uint32_t c[4], IdSink* sink, Digest (*work)[256],
+                                                          Digest& dg) {
+  uint64_t nb = (r + 1) * 2048 - 1 + 8ull * t;  // first parent of the level
+#pragma unroll 1
+  for (int lvl = 0; lvl < 4; lvl++) {
+    uint32_t P[2], FL[2], FR[2], XF[2], XS[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+      label_pairs4(pass, __byte_perm(c[2 * q], c[2 * q + 1], 0x6420), __byte_perm(c[2 * q], c[2 * q + 1], 0x7531),
+                   P[q], FL[q], FR[q], XF[q], XS[q]);
+    // pairs that hash: ascending, so work[i] is written after its children
+    // work[2i], work[2i+1] of the level below were read
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      uint32_t X = XF[q] | XS[q];
+      while (X) {
+        const int b = (__ffs(X) - 1) >> 3;
+        X &= ~(0xffu << (8 * b));
+        const uint32_t i = 4 * q + b;
+        const uint64_t n = nb + i;
+        Digest dl, dr;
+        if (lvl == 0) {
+          dl = ld_digest(a.tree + 2 * n + 1);
+          dr = ld_digest(a.tree + 2 * n + 2);
+        } else {
+          dl = work[2 * i][t];
+          dr = work[2 * i + 1][t];
+        }
+        const Digest d = hash_pair(HK, dl, dr);
+        st_digest(a.tree + n, d);
+        if ((XF[q] >> (8 * b)) & 1) {
+          queue_insert(a, sink, (uint32_t)n);
+          work[i][t] = d;
+        } else if (map_find(a.map, d, a.err) >= 0) {
+          work[i][t] = d;  // parent stays SHIFT_DUPL
+        } else {
+          set_byte(P[q], b, DONE);
+          set_byte(FL[q], b, ROOT_SHIFT);
+          set_byte(FR[q], b, ROOT_SHIFT);
+        }
+      }
+    }
+    // children's root flags, children in order at consecutive canonical positions
+    if ((FL[0] | FR[0] | FL[1] | FR[1]) != 0) {
+      const uint64_t cp0 = canon_pos(a, (uint32_t)(2 * nb + 1));
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const uint32_t f4[2] = {__byte_perm(FL[q], FR[q], 0x5140), __byte_perm(FL[q], FR[q], 0x7362)};
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          uint32_t f = f4[k];
+          while (f) {
+            const int b = (__ffs(f) - 1) >> 3;
+            a.rflag[cp0 + 8 * q + 4 * k + b] = (uint8_t)(f >> (8 * b));
+            f &= ~(0xffu << (8 * b));
+          }
+        }
+      }
+    }
+    c[0] = P[0];
+    c[1] = P[1];
+    c[2] = c[3] = DONE * kB1;  // pairs past the level's width: DONE, no flags
+    nb = (nb - 1) / 2;
+  }
+  const uint8_t lab = (uint8_t)c[0];
+  if (digest_wanted(pass, lab)) dg = work[0][t];
+  return lab;
+}
+
 // The bottom span of an incremental pass (and of the baseline's
 // first-occurrence pass): 12 levels, 4096 leaves per block.  Each thread
 // reads the labels of its 16 children with one aligned 16-byte load (the
@@ -414,6 +521,9 @@ __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int 
   constexpr uint64_t kFixed8 = 0x0101010101010101ull * FIXED_DUPL;
   if (lo == kFixed8 && hi == kFixed8 && nb1 + 7 <= last_interior) {
     lab = pass == 0 ? DONE : FIXED_DUPL;
+  } else if (nb1 + 7 <= last_interior) {
+    uint32_t c[4] = {(uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32)};
+    lab = thread_levels_bytewise<HK>(a, pass, r, t, c, &sink, work, dg);
   } else {
     uint64_t nb = nb1;
     uint32_t width = 8;
