@@ -124,7 +124,7 @@ int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
     MTC_CUDA(rflag_.ensure(tree ? M : 1, stream_));
     MTC_CUDA(chunk_slot_.ensure(N, stream_));
     MTC_CUDA(changed_list_.ensure(N, stream_));
-    MTC_CUDA(changed_count_.ensure(3, stream_));  // [changed chunks, leaves demoted, forest inserts]
+    MTC_CUDA(changed_count_.ensure(4, stream_));  // [changed chunks, leaves demoted, forest inserts, duplicate notes]
     MTC_CUDA(map_size_.ensure(1, stream_));
     MTC_CUDA(err_.ensure(1, stream_));
     MTC_CUDA(fo_list_.ensure(N + 1, stream_));
@@ -135,7 +135,9 @@ int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
     MTC_CUDA(reg_len_.ensure(N + 1, stream_));
     MTC_CUDA(sh_key_.ensure(N + 1, stream_));
     MTC_CUDA(sh_prev_.ensure(N + 1, stream_));
-    MTC_CUDA(scan_.ensure((size_t)(std::max(M, N + 1) + kScanTile - 1) / kScanTile + 2, stream_));
+    // tile sums: scans of 4096 entries over max(M, N+1), or of 512 regions over N+1
+    MTC_CUDA(scan_.ensure(std::max<size_t>((size_t)(std::max(M, N + 1) + kScanTile - 1) / kScanTile,
+                                           ((size_t)N + 1 + 511) / 512) + 2, stream_));
     MTC_CUDA(scan_total_.ensure(1, stream_));
     MTC_CUDA(scan_total2_.ensure(1, stream_));
     MTC_CUDA(lay_.ensure(1, stream_));
@@ -216,7 +218,11 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.changed_list = changed_list_.p;
   la.changed_count = changed_count_.p;
   la.demoted = changed_count_.p + 1;
-  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 2 * sizeof(uint32_t), stream_));
+  // the first-occurrence root list is free until the root compaction
+  la.dup_list = fo_list_.p;
+  la.dup_count = changed_count_.p + 3;
+  la.dup_cap = (uint32_t)fo_list_.n;
+  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   MTC_CUDA(launch_leaf_inserts(la, stream_));
@@ -264,7 +270,10 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.basic_first = current_id == 0 ? 1 : 0;  // never true in a captured sequence
   la.changed_list = changed_list_.p;
   la.changed_count = changed_count_.p;
-  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, sizeof(uint32_t), stream_));
+  la.dup_list = fo_list_.p;  // free until the chunk compaction
+  la.dup_count = changed_count_.p + 3;
+  la.dup_cap = (uint32_t)fo_list_.n;
+  MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
   if (mode_ == MODE_LIST) MTC_CUDA(launch_leaf_inserts(la, stream_));

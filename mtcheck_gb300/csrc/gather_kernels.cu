@@ -645,23 +645,25 @@ __device__ __forceinline__ void root_prologue(const uint8_t* labels, uint32_t N,
   if (root) fo_list[0] = 0;
 }
 
-// Blocks past the tiles issue a fused forest pass's queued inserts, which only
-// the assembly's ownership test and later checkpoints read.
+// The first `nd` blocks issue a fused forest pass's queued inserts (only the
+// assembly's ownership test and later checkpoints read them), the others
+// count one tile each.
 __global__ void __launch_bounds__(kScanThreads) root_count_kernel(ForestArgs a, uint32_t N, uint64_t n,
                                                                   uint64_t* tile_sums, uint32_t* fo_list,
-                                                                  Layout* lay, uint32_t ntiles) {
+                                                                  Layout* lay, uint32_t nd) {
   __shared__ uint64_t sh[33];
-  if (blockIdx.x >= ntiles) {
-    if (forest_fused(a)) drain_inserts(a, ntiles, gridDim.x - ntiles);
+  if (blockIdx.x < nd) {
+    if (forest_fused(a)) drain_inserts(a, 0, nd);
     return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) root_prologue(a.labels, N, a.ascending, fo_list, lay);
-  const uint64_t p = (uint64_t)blockIdx.x * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
+  const uint32_t tile = blockIdx.x - nd;
+  if (tile == 0 && threadIdx.x == 0) root_prologue(a.labels, N, a.ascending, fo_list, lay);
+  const uint64_t p = (uint64_t)tile * kRootTile + (uint64_t)threadIdx.x * kRootPerThread;
   uint4 v[kRootVec];
   const uint64_t c = p < n ? load_flags(a.rflag, p, n, v) : 0;
   uint64_t total;
   block_excl_scan(c, sh, &total);
-  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+  if (threadIdx.x == 0) tile_sums[tile] = total;
 }
 
 // Emits the roots in serial push order.  kReduce: the tile offset is the sum of
@@ -739,10 +741,6 @@ __device__ __forceinline__ void fo_prep(const GatherArgs& g) {
     g.fo_val[i] = v;
   }
 }
-struct FoVal {
-  const uint64_t* fo_val;
-  __device__ __forceinline__ uint64_t operator()(uint64_t i) const { return fo_val[i]; }
-};
 struct FoEmit {
   GatherArgs g;
   __device__ __forceinline__ void operator()(uint64_t i, uint64_t ex, uint64_t v) const {
@@ -756,6 +754,33 @@ struct FoEmit {
     if (g.lay->ok) *reinterpret_cast<uint32_t*>(g.stage + g.lay->pad + 32 + 4ull * r) = node;
   }
 };
+
+// Region sizes scanned with one first-occurrence root per thread (tiles of
+// kFoTile) over a persistent grid: the tile count follows F on the device.
+constexpr uint32_t kFoTile = kScanThreads;
+__global__ void __launch_bounds__(kScanThreads) fo_tile_sums_kernel(GatherArgs g) {
+  __shared__ uint64_t sh[33];
+  const uint32_t F = g.lay->F;
+  const uint32_t nt = (F + kFoTile - 1) / kFoTile;
+  for (uint32_t t = blockIdx.x; t < nt; t += gridDim.x) {
+    const uint32_t i = t * kFoTile + threadIdx.x;
+    uint64_t total;
+    block_excl_scan(i < F ? g.fo_val[i] : 0, sh, &total);
+    if (threadIdx.x == 0) g.scan_scratch[t] = total;
+  }
+}
+__global__ void __launch_bounds__(kScanThreads) fo_emit_kernel(GatherArgs g) {
+  __shared__ uint64_t sh[33];
+  const uint32_t F = g.lay->F;
+  const uint32_t nt = (F + kFoTile - 1) / kFoTile;
+  const FoEmit emit{g};
+  for (uint32_t t = blockIdx.x; t < nt; t += gridDim.x) {
+    const uint32_t i = t * kFoTile + threadIdx.x;
+    const uint64_t v = i < F ? g.fo_val[i] : 0;
+    const uint64_t ex = block_excl_scan(v, sh, nullptr) + g.scan_scratch[t];
+    if (i < F) emit(i, ex, v);
+  }
+}
 
 // Shifted duplicates: (source checkpoint, source node) of each root.
 // The histogram of source checkpoints is warp-aggregated: most entries share
@@ -791,10 +816,11 @@ __global__ void roots_prep_kernel(GatherArgs g) {
 // list approach's BinOp1D.
 // First, the tile sums of the region-size scan become tile offsets in place,
 // and their total gives the region count and the data chunk count.
-__global__ void layout_kernel(GatherArgs g, uint32_t ntiles) {
+__global__ void layout_kernel(GatherArgs g) {
   __shared__ uint64_t sh[33];
   Layout* lay = g.lay;
   {
+    const uint32_t ntiles = (lay->F + kFoTile - 1) / kFoTile;
     uint64_t carry = 0;
     for (uint32_t b = 0; b < ntiles; b += blockDim.x) {
       const uint32_t i = b + threadIdx.x;
@@ -1251,7 +1277,8 @@ cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M,
   const uint64_t n = (uint64_t)M - 1;  // every node but the root
   uint32_t ntiles = (uint32_t)((n + kRootTile - 1) / kRootTile);
   if (ntiles == 0) ntiles = 1;
-  root_count_kernel<<<ntiles + 2 * num_sms(), kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay, ntiles);
+  const uint32_t nd = 2 * num_sms();
+  root_count_kernel<<<ntiles + nd, kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay, nd);
   if (ntiles <= kReduceTiles) {
     root_emit_kernel<true><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
     note_launch(2);
@@ -1285,11 +1312,10 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   const uint32_t gs = grid_for(max_entries, 256);
   roots_prep_kernel<<<gs, 256, 0, s>>>(g);
   // region totals first (phase 1+2 of the scan), then layout, then emit
-  uint32_t ntiles = (uint32_t)((max_entries + kScanTile - 1) / kScanTile);
-  if (ntiles == 0) ntiles = 1;
-  scan_tile_sums_kernel<<<ntiles, kScanThreads, 0, s>>>(FoVal{g.fo_val}, &g.lay->F, 0, g.scan_scratch);
-  layout_kernel<<<1, 1024, 0, s>>>(g, ntiles);
-  scan_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(FoVal{g.fo_val}, FoEmit{g}, &g.lay->F, 0, g.scan_scratch);
+  const uint32_t gfo = (uint32_t)std::min<uint64_t>((max_entries + kFoTile - 1) / kFoTile + 1, 4ull * num_sms());
+  fo_tile_sums_kernel<<<gfo, kScanThreads, 0, s>>>(g);
+  layout_kernel<<<1, 1024, 0, s>>>(g);
+  fo_emit_kernel<<<gfo, kScanThreads, 0, s>>>(g);
   note_launch(4);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (g.approach != APPROACH_BASIC) {

@@ -79,6 +79,11 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uin
   append_changed(changed, c, a.changed_list, a.changed_count);
 }
 
+__device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t chunk) {
+  const uint32_t k = atomicAdd(a.dup_count, 1u);
+  if (k < a.dup_cap) a.dup_list[k] = chunk;
+}
+
 // Map insert of one changed chunk (src/tree_approach.cpp:325-349,
 // src/list_approach.cpp:50-59): new digest -> first occurrence; a digest
 // already inserted by this launch -> first occurrence for now, the lowest
@@ -99,12 +104,18 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
     unsigned long long old = kWinEmpty;
     uint8_t label = SHIFT_DUPL;
     const int r = map_insert_win(a.map, dg, win_of(epoch, node), cur, &slot, &old, a.err);
+    // every chunk that may lose its entry to another of this launch is noted
+    // for the demote pass: the creator once another thread's priority was
+    // there first, the others with the owner they displaced
     if (r == INS_NEW) {
       label = FIRST_OCUR;
       created++;
+      if (old != kWinEmpty) note_dup(a, c);
     } else if (r == INS_EXISTING) {
       if (old == kWinEmpty || win_epoch(old) == epoch) {
         label = FIRST_OCUR;  // first seen by this launch
+        note_dup(a, c);
+        if (old != kWinEmpty) note_dup(a, win_node(old) - (EPI == EPI_TREE ? a.leaf_base : 0u));
       } else if (EPI == EPI_TREE && __ldcg(&a.map.slots[slot].tree) == cur) {
         // lowest node within the older entry, its epoch kept
         unsigned long long w = old;
@@ -114,6 +125,7 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
           w = seen;
         }
         label = FIRST_OCUR;
+        note_dup(a, c);
       }
     }
     a.chunk_slot[c] = (uint32_t)slot;
@@ -123,12 +135,16 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
 }
 
 // Second pass (src/tree_approach.cpp:356-369): a first occurrence that does
-// not own its digest becomes a shifted duplicate.
+// not own its digest becomes a shifted duplicate.  Only the noted chunks can
+// be such (every changed chunk when the note list overflowed).
 __global__ void leaf_demote_kernel(LeafArgs a) {
-  const uint32_t n = *a.changed_count;
+  const uint32_t nd = *a.dup_count;
+  const bool all = nd > a.dup_cap;
+  const uint32_t n = all ? *a.changed_count : nd;
+  const uint32_t* list = all ? a.changed_list : a.dup_list;
   const uint32_t cur = a.sp->cur;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = a.changed_list[k];
+    const uint32_t c = list[k];
     if (a.labels[c] != FIRST_OCUR) continue;
     const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
     const uint32_t node = a.leaf_base + c;

@@ -47,6 +47,9 @@ struct LeafArgs {
   uint32_t* changed_list = nullptr;  // chunks whose digest changed (tree, list)
   uint32_t* changed_count = nullptr;
   uint32_t* demoted = nullptr;    // set to 1 when a first occurrence is demoted (tree; may be null)
+  uint32_t* dup_list = nullptr;   // chunks that met a duplicate of their digest inserted by the same launch
+  uint32_t* dup_count = nullptr;  // appends; above dup_cap the demote pass visits every changed chunk
+  uint32_t dup_cap = 0;
   int hash_kind = HASH_MURMUR3;
   int epi = EPI_HASH;
   int basic_first = 0;            // basic approach with current_id == 0: every chunk changed
