@@ -625,6 +625,27 @@ def serve_bench(torch, mc, dev, a):
     }
 
 
+def bind_local_cpus(torch, local):
+    """Pin this process to the CPUs next to the GPU (sysfs local_cpulist of
+    its PCI function), so that pinned host buffers are allocated on the GPU's
+    own memory node.  Returns the CPU list, or None when sysfs does not say."""
+    try:
+        p = torch.cuda.get_device_properties(local)
+        path = "/sys/bus/pci/devices/%04x:%02x:%02x.0/local_cpulist" % (p.pci_domain_id, p.pci_bus_id,
+                                                                          p.pci_device_id)
+        spec = open(path).read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        if not cpus or not hasattr(os, "sched_setaffinity"):
+            return None
+        os.sched_setaffinity(0, cpus & os.sched_getaffinity(0) or cpus)
+        return spec
+    except (OSError, ValueError, AttributeError):
+        return None
+
+
 def main():
     a = parse()
     ws, rank, local = dist_setup()
@@ -635,6 +656,7 @@ def main():
     import mtcheck_gb300 as mc
 
     torch.cuda.set_device(local)
+    host_cpus = bind_local_cpus(torch, local)
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -771,6 +793,7 @@ def main():
                        "approach": "tree", "hash": a.hash, "buffer_bytes": nbytes, "chunk_size": cs,
                        "chunks": N, "l2": "inputs (%d MiB) larger than L2" % (nbytes >> 20),
                        "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "host_cpus": host_cpus,
                        "diff_bytes_mean": int(sum(sizes) / K),
                        "checkpoint_roofline_frac": round(ckpt_frac, 4),
                        "phase_ms_mean": {"leaf_hash": round(leaf_avg * 1e3, 4),

@@ -42,10 +42,18 @@ int Batch::fail(int code, const std::string& msg) {
   return code;
 }
 
+void Batch::drop_parent() {
+  if (parent_exec_) cudaGraphExecDestroy(parent_exec_);
+  if (parent_) cudaGraphDestroy(parent_);
+  parent_exec_ = nullptr;
+  parent_ = nullptr;
+}
+
 void Batch::drop_graph() {
-  for (auto& x : execs_)
-    if (x) cudaGraphExecDestroy(x);
-  execs_.assign(engs_.size(), nullptr);
+  drop_parent();
+  for (auto& g : graphs_)
+    if (g) cudaGraphDestroy(g);
+  graphs_.assign(engs_.size(), nullptr);
   sigs_.assign(engs_.size(), 0);
   nodes_.assign(engs_.size(), 0);
   kernels_.assign(engs_.size(), 0);
@@ -77,8 +85,9 @@ int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
   } while (0)
 
 int Batch::capture_member(size_t i, const uint8_t* data, uint64_t len) {
-  if (execs_[i]) cudaGraphExecDestroy(execs_[i]);
-  execs_[i] = nullptr;
+  drop_parent();
+  if (graphs_[i]) cudaGraphDestroy(graphs_[i]);
+  graphs_[i] = nullptr;
   const uint64_t l0 = launch_count();
   MTC_BCUDA(cudaStreamBeginCapture(streams_[i], cudaStreamCaptureModeRelaxed));
   int rc = engs_[i]->enqueue(data, len, false);
@@ -90,18 +99,28 @@ int Batch::capture_member(size_t i, const uint8_t* data, uint64_t len) {
     if (rc != ST_OK) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
     return fail(ST_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
   }
-  cudaError_t ie = cudaGraphInstantiate(&execs_[i], g, 0);
   size_t n = 0;
   cudaGraphGetNodes(g, nullptr, &n);
-  cudaGraphDestroy(g);
-  if (ie != cudaSuccess) {
-    execs_[i] = nullptr;
-    return fail(ST_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
-  }
+  graphs_[i] = g;
   nodes_[i] = n;
   kernels_[i] = launch_count() - l0;
   sigs_[i] = engs_[i]->signature(data, len);
   stats_.captures++;
+  return ST_OK;
+}
+
+int Batch::build_parent() {
+  MTC_BCUDA(cudaGraphCreate(&parent_, 0));
+  for (size_t i = 0; i < engs_.size(); i++) {
+    cudaGraphNode_t node;
+    MTC_BCUDA(cudaGraphAddChildGraphNode(&node, parent_, nullptr, 0, graphs_[i]));
+  }
+  cudaError_t ie = cudaGraphInstantiate(&parent_exec_, parent_, 0);
+  if (ie != cudaSuccess) {
+    parent_exec_ = nullptr;
+    drop_parent();
+    return fail(ST_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+  }
   return ST_OK;
 }
 
@@ -120,37 +139,56 @@ int Batch::checkpoint(const uint8_t* const* data, const uint64_t* lens, bool mak
   // each member's stream; nothing waits for it here
   const double t_prep = now_ms();
   const bool graph = use_graph_ && !any_fresh;
-  // 2. (re)capture the members whose device buffers moved
+  // 2. (re)capture the members whose device buffers moved; their streams
+  // (allocations, rehash) and those of members whose prepare issued other
+  // work are joined into the origin stream before the step
+  std::vector<char> join(engs_.size(), 0);
   if (graph) {
-    for (size_t i = 0; i < engs_.size(); i++)
-      if (!execs_[i] || sigs_[i] != engs_[i]->signature(data[i], lens[i])) {
+    for (size_t i = 0; i < engs_.size(); i++) {
+      if (engs_[i]->take_stream_work()) join[i] = 1;
+      if (!graphs_[i] || sigs_[i] != engs_[i]->signature(data[i], lens[i])) {
         int rc = capture_member(i, data[i], lens[i]);
         if (rc) return rc;
+        join[i] = 1;
       }
+    }
+    if (!parent_exec_) {
+      int rc = build_parent();
+      if (rc) return rc;
+    }
   }
   // 3. issue: the step starts after the work already on the legacy default
-  // stream (where the inputs are usually written), every member on its own
-  // stream between a fork and a join on the origin stream
+  // stream (where the inputs are usually written): one launch of the parent
+  // graph on the origin stream, or every member on its own stream between a
+  // fork and a join on the origin stream
   const double t_cap = now_ms();
   const uint64_t l0 = launch_count();
   MTC_BCUDA(cudaEventRecord(in_, cudaStreamLegacy));
   MTC_BCUDA(cudaStreamWaitEvent(origin_, in_, 0));
-  MTC_BCUDA(cudaEventRecord(t0_, origin_));
-  MTC_BCUDA(cudaEventRecord(fork_, origin_));
   uint64_t nodes = 0, kernels = 0;
-  for (size_t i = 0; i < engs_.size(); i++) {
-    MTC_BCUDA(cudaStreamWaitEvent(streams_[i], fork_, 0));
-    engs_[i]->stage_params();
-    if (graph) {
-      MTC_BCUDA(cudaGraphLaunch(execs_[i], streams_[i]));
+  if (graph) {
+    for (size_t i = 0; i < engs_.size(); i++) {
+      if (join[i]) {
+        MTC_BCUDA(cudaEventRecord(joins_[i], streams_[i]));
+        MTC_BCUDA(cudaStreamWaitEvent(origin_, joins_[i], 0));
+      }
+      engs_[i]->stage_params();
       nodes += nodes_[i];
       kernels += kernels_[i];
-    } else {
+    }
+    MTC_BCUDA(cudaEventRecord(t0_, origin_));
+    MTC_BCUDA(cudaGraphLaunch(parent_exec_, origin_));
+  } else {
+    MTC_BCUDA(cudaEventRecord(t0_, origin_));
+    MTC_BCUDA(cudaEventRecord(fork_, origin_));
+    for (size_t i = 0; i < engs_.size(); i++) {
+      MTC_BCUDA(cudaStreamWaitEvent(streams_[i], fork_, 0));
+      engs_[i]->stage_params();
       int rc = engs_[i]->enqueue(data[i], lens[i], false);
       if (rc) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
+      MTC_BCUDA(cudaEventRecord(joins_[i], streams_[i]));
+      MTC_BCUDA(cudaStreamWaitEvent(origin_, joins_[i], 0));
     }
-    MTC_BCUDA(cudaEventRecord(joins_[i], streams_[i]));
-    MTC_BCUDA(cudaStreamWaitEvent(origin_, joins_[i], 0));
   }
   MTC_BCUDA(cudaEventRecord(t1_, origin_));
   if (graph) {

@@ -4,12 +4,13 @@
 // on its own CUDA stream.  One call checkpoints every member:
 //   * a step in which some member starts a new baseline runs eagerly, every
 //     member's work issued on its own stream so that they overlap;
-//   * every other step replays one CUDA graph per member -- its whole launch
-//     sequence -- on the member's stream, all members between a fork and a
-//     join on the origin stream.  A graph reads the per-step values
-//     (checkpoint id, epochs) from pinned host memory, so it is captured once
-//     and replayed until that member's device buffers move (map growth, a
-//     new input pointer); only that member is captured again.
+//   * every other step replays one CUDA graph holding every member's launch
+//     sequence as an independent child graph, in one launch on the origin
+//     stream.  A member's sequence reads the per-step values (checkpoint id,
+//     epochs) from pinned host memory, so it is captured once and replayed
+//     until that member's device buffers move (map growth, a new input
+//     pointer); only that member is captured again, and the parent graph is
+//     rebuilt from the members' graphs.
 // A step starts after all work already issued to the legacy default stream
 // (where the inputs are usually written); inputs written on other streams
 // must be synchronised by the caller.
@@ -55,6 +56,8 @@ class Batch {
  private:
   int fail(int code, const std::string& msg);
   int capture_member(size_t i, const uint8_t* data, uint64_t len);
+  int build_parent();
+  void drop_parent();
   void drop_graph();
 
   std::vector<Engine*> engs_;
@@ -62,8 +65,10 @@ class Batch {
   std::vector<cudaEvent_t> joins_;
   cudaStream_t origin_ = nullptr;
   cudaEvent_t fork_ = nullptr, in_ = nullptr, t0_ = nullptr, t1_ = nullptr;
-  std::vector<cudaGraphExec_t> execs_;
+  std::vector<cudaGraph_t> graphs_;  // each member's captured sequence
   std::vector<uint64_t> sigs_, nodes_, kernels_;
+  cudaGraph_t parent_ = nullptr;     // one child graph node per member
+  cudaGraphExec_t parent_exec_ = nullptr;
   bool use_graph_ = true;
   uint32_t headroom_ = 64;
   BatchStats stats_;

@@ -158,6 +158,7 @@ int Engine::ensure_state(uint32_t N, bool fresh, uint32_t id_headroom) {
     if (epoch_ + kEpochsPerCheckpoint >= kEpochLimit) {
       if (map_cap_) MTC_CUDA(launch_map_rebase(DigestMap{slots_.p, map_cap_ - 1, map_size_.p}, map_cap_, stream_));
       epoch_ = 0;
+      stream_work_ = true;
     }
   }
   return ensure_sort(current_id + 1 + id_headroom);

@@ -107,6 +107,13 @@ class Engine {
   // Fingerprint of everything a captured sequence depends on.
   uint64_t signature(const uint8_t* dev_data, uint64_t len) const;
   bool fresh() const { return fresh_; }
+  // True once after prepare() put work on the engine's stream that leaves
+  // every device pointer in place (so the signature does not show it).
+  bool take_stream_work() {
+    const bool w = stream_work_;
+    stream_work_ = false;
+    return w;
+  }
   void set_max_load(double f) { max_load_ = f; }
   double max_load() const { return max_load_; }
   void set_leaf_tune(const LeafTune& t) { leaf_tune_ = t; }
@@ -184,6 +191,7 @@ class Engine {
   double max_load_ = 0.75;
   LeafTune leaf_tune_{};
   uint32_t N_ = 0, M_ = 0;
+  bool stream_work_ = false;
   uint32_t epoch_ = 0;
   uint64_t map_cap_ = 0;
   uint32_t map_size_host_ = 0;

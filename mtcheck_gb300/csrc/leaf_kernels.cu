@@ -37,16 +37,17 @@ __device__ __forceinline__ uint32_t swz(uint32_t logical) {
 constexpr uint8_t PENDING = 0xFE;  // changed chunk, classified by the insert pass
 
 // Append chunk c to the changed list (one atomic per warp).
-__device__ __forceinline__ void append_changed(bool changed, uint32_t c, uint32_t* list, uint32_t* count) {
+// Appends a changed chunk to the list the map inserts read (warp-aggregated).
+__device__ __forceinline__ void append_changed(const LeafArgs& a, bool changed, uint32_t c) {
   const unsigned act = __activemask();
   const unsigned b = __ballot_sync(act, changed);
   if (!b) return;
   const int lane = threadIdx.x & 31;
   const int leader = __ffs(b) - 1;
   uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(b));
+  if (lane == leader) base = atomicAdd(a.changed_count, (uint32_t)__popc(b));
   base = __shfl_sync(act, base, leader);
-  if (changed) list[base + __popc(b & ((1u << lane) - 1))] = c;
+  if (changed) a.changed_list[base + __popc(b & ((1u << lane) - 1))] = c;
 }
 
 // Streaming part of the per-chunk work: compare with the previous digest,
@@ -76,12 +77,15 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uin
     // A FIXED_DUPL leaf's insert() always finds its digest (every earlier
     // leaf digest was inserted) and changes nothing, so it is not repeated.
   }
-  append_changed(changed, c, a.changed_list, a.changed_count);
+  append_changed(a, changed, c);
 }
 
-__device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t chunk) {
+// A note for the demote pass; kCheckCreator: the chunk met an entry that
+// another insert of this launch created, whose chunk is checked too.
+constexpr uint32_t kCheckCreator = 1u << 31;  // chunk counts stay below 2^31
+__device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t note) {
   const uint32_t k = atomicAdd(a.dup_count, 1u);
-  if (k < a.dup_cap) a.dup_list[k] = chunk;
+  if (k < a.dup_cap) a.dup_list[k] = note;
 }
 
 // Map insert of one changed chunk (src/tree_approach.cpp:325-349,
@@ -90,7 +94,8 @@ __device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t chunk) {
 // chunk keeping the entry; an older digest -> shifted duplicate, except (tree)
 // one whose entry carries this checkpoint's id, which an id that was not
 // advanced (the header overload) leaves in place: the reference lowers its
-// node and keeps the chunk a first occurrence there too.
+// node and keeps the chunk a first occurrence there too.  The creator of an
+// entry waits for nothing after its claim.
 template <int EPI>
 __global__ void leaf_insert_kernel(LeafArgs a) {
   const uint32_t n = *a.changed_count;
@@ -98,29 +103,28 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
   uint32_t created = 0;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = a.changed_list[k];
-    const Digest dg = ld_digest(a.prev + c);
+    const Digest dg = map_key(ld_digest(a.prev + c));
     const uint32_t node = EPI == EPI_TREE ? a.leaf_base + c : c;
     uint64_t slot = 0;
-    unsigned long long old = kWinEmpty;
     uint8_t label = SHIFT_DUPL;
-    const int r = map_insert_win(a.map, dg, win_of(epoch, node), cur, &slot, &old, a.err);
-    // every chunk that may lose its entry to another of this launch is noted
-    // for the demote pass: the creator once another thread's priority was
-    // there first, the others with the owner they displaced
+    const int r = map_claim(a.map, dg, &slot, a.err);
+    MapSlot* s = &a.map.slots[slot];
     if (r == INS_NEW) {
+      s->tree = cur;
+      s->first_chunk = c;
+      atomicMin(&s->win, win_of(epoch, node));
       label = FIRST_OCUR;
       created++;
-      if (old != kWinEmpty) note_dup(a, c);
     } else if (r == INS_EXISTING) {
+      const unsigned long long old = atomicMin(&s->win, win_of(epoch, node));
       if (old == kWinEmpty || win_epoch(old) == epoch) {
-        label = FIRST_OCUR;  // first seen by this launch
-        note_dup(a, c);
-        if (old != kWinEmpty) note_dup(a, win_node(old) - (EPI == EPI_TREE ? a.leaf_base : 0u));
-      } else if (EPI == EPI_TREE && __ldcg(&a.map.slots[slot].tree) == cur) {
+        label = FIRST_OCUR;  // first seen by this launch: the lowest chunk keeps it
+        note_dup(a, c | kCheckCreator);
+      } else if (EPI == EPI_TREE && __ldcg(&s->tree) == cur) {
         // lowest node within the older entry, its epoch kept
         unsigned long long w = old;
         for (int i = 0; i < 64 && win_node(w) > node; i++) {
-          const unsigned long long seen = atomicCAS(&a.map.slots[slot].win, w, (w & ~0xffffffffull) | node);
+          const unsigned long long seen = atomicCAS(&s->win, w, (w & ~0xffffffffull) | node);
           if (seen == w) break;
           w = seen;
         }
@@ -135,8 +139,18 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
 }
 
 // Second pass (src/tree_approach.cpp:356-369): a first occurrence that does
-// not own its digest becomes a shifted duplicate.  Only the noted chunks can
-// be such (every changed chunk when the note list overflowed).
+// not own its digest becomes a shifted duplicate.  Only the noted chunks and
+// the creators of their entries can be such (every changed chunk when the
+// note list overflowed).
+__device__ __forceinline__ void demote_chunk(const LeafArgs& a, uint32_t c, const MapSlot* s, uint32_t cur) {
+  if (a.labels[c] != FIRST_OCUR) return;
+  const uint32_t node = a.leaf_base + c;
+  const uint32_t owner = win_node(s->win);
+  if (a.epi == EPI_TREE ? (s->tree == cur && owner != node) : (owner != node)) {
+    a.labels[c] = SHIFT_DUPL;
+    if (a.demoted) atomicOr(a.demoted, 1u);
+  }
+}
 __global__ void leaf_demote_kernel(LeafArgs a) {
   const uint32_t nd = *a.dup_count;
   const bool all = nd > a.dup_cap;
@@ -144,15 +158,11 @@ __global__ void leaf_demote_kernel(LeafArgs a) {
   const uint32_t* list = all ? a.changed_list : a.dup_list;
   const uint32_t cur = a.sp->cur;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = list[k];
-    if (a.labels[c] != FIRST_OCUR) continue;
+    const uint32_t e = list[k];
+    const uint32_t c = all ? e : (e & ~kCheckCreator);
     const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
-    const uint32_t node = a.leaf_base + c;
-    const uint32_t owner = win_node(s->win);
-    if (a.epi == EPI_TREE ? (s->tree == cur && owner != node) : (owner != node)) {
-      a.labels[c] = SHIFT_DUPL;
-      if (a.demoted) atomicOr(a.demoted, 1u);
-    }
+    demote_chunk(a, c, s, cur);
+    if (!all && (e & kCheckCreator)) demote_chunk(a, s->first_chunk, s, cur);
   }
 }
 

@@ -267,13 +267,15 @@ __host__ __device__ __forceinline__ uint32_t leftmost_leaf(uint32_t node, uint32
 // and the old value an insert gets back tells whether the entry is older
 // than its launch.  The node is win's low 32 bits.  `tree` (the checkpoint id
 // of the first occurrence) is written by the creator and read by later
-// launches.  No insert waits on another thread.
+// launches; so is `first_chunk`, the chunk whose leaf insert created the
+// entry (read by that checkpoint's demote pass).  No insert waits on another
+// thread.
 // ---------------------------------------------------------------------------
 struct __align__(32) MapSlot {
   uint32_t key[4];
   unsigned long long win;
   uint32_t tree;
-  uint32_t reserved;
+  uint32_t first_chunk;
 };
 struct DigestMap {
   MapSlot* slots;
