@@ -9,7 +9,8 @@ one incremental checkpoint of the whole buffer.
   value : buffer bytes / device time per checkpoint, inputs resident in HBM,
           diff assembled in HBM (GB/s, whole job over all ranks)
   e2e   : the same through the C ABI with pinned host buffers: H2D of the
-          state, checkpoint, D2H of the diff inside the timed region
+          state, checkpoint, D2H of the diff inside the timed region (the
+          next state's upload overlaps the current checkpoint)
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun every rank deduplicates its own buffer (replicas, no
@@ -730,26 +731,48 @@ def main():
     if not a.no_e2e:
         host = [s.cpu().pin_memory() for s in states[1 + W:]]
         devbuf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
-        outs = [np.empty(sz, dtype=np.uint8) for sz in sizes]
-        pinned_out = [torch.empty(sz, dtype=torch.uint8).pin_memory() for sz in sizes]
+        # two device input buffers: step i+1 uploads on a side stream while
+        # step i is checkpointed (every upload stays inside the timed region)
+        bufs = [devbuf, torch.empty(nbytes, dtype=torch.uint8, device=dev)]
+        side = torch.cuda.Stream(device=dev)
+        ready = [torch.cuda.Event(), torch.cuda.Event()]
+        # one pinned result buffer for the largest diff a checkpoint can have
+        # (header, region and repeat metadata, every chunk), allocated before
+        # the timed region
+        max_diff = nbytes + 12 * (N + 1) + 32 + 8 * 4096
+        pinned_out = torch.empty(max_diff, dtype=torch.uint8).pin_memory()
+        out_view = pinned_out.numpy()
         de = mc.TreeDeduplicator(cs, kind)
+        # the handle works on its own stream, ordered after each upload by an
+        # event, so that the next upload runs beside it
+        work = torch.cuda.Stream(device=dev)
+        de.set_stream(work.cuda_stream)
         devbuf.copy_(states[W])
+        work.wait_stream(torch.cuda.current_stream())
         de.checkpoint_device(devbuf, True)
         barrier()
+
+        def upload(i):
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                bufs[i % 2].copy_(host[i], non_blocking=True)
+                ready[i % 2].record(side)
+
         t0 = time.perf_counter()
         d2h = 0
-        for i, h in enumerate(host):
-            devbuf.copy_(h, non_blocking=True)
-            n = de.checkpoint_device(devbuf, False)
-            if pinned_out[i].numel() < n:
-                pinned_out[i] = torch.empty(n, dtype=torch.uint8).pin_memory()
-            de.copy_diff(pinned_out[i].numpy())
+        upload(0)
+        for i in range(len(host)):
+            work.wait_event(ready[i % 2])
+            if i + 1 < len(host):
+                upload(i + 1)  # the other buffer's last checkpoint has returned
+            n = de.checkpoint_device(bufs[i % 2], False)
+            de.copy_diff(out_view[:n])
             d2h += n
         barrier()
         te = max_over_ranks(torch, time.perf_counter() - t0, dev, ws)
         e2e = {"value": round(whole_job_rate(nbytes * K, te, ws), 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": int(d2h / K)}
-        del host, pinned_out, outs
+        del host, pinned_out, out_view, bufs
 
     rst = None
     if not a.no_restart and rank == 0:
