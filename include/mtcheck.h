@@ -282,7 +282,8 @@ typedef struct mtc_tune {
   int32_t rows;         /* chunks per CTA tile: 128 or 256 */
   int32_t ctas_per_sm;  /* 0: as many as fit (at most 3) */
   int32_t direct;       /* 1: per-thread global loads instead of TMA staging */
-  int32_t reserved;
+  int32_t eager;        /* 1: issue every launch of a checkpoint from the host instead of
+                           replaying the captured sequence (single-handle calls) */
   double max_load;      /* digest-map load factor bound, (0.1, 0.95] */
 } mtc_tune_t;
 int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t);

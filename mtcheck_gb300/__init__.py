@@ -59,11 +59,11 @@ class BatchInfo(ctypes.Structure):
 
 class Tune(ctypes.Structure):
     _fields_ = [("rows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("direct", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("max_load", ctypes.c_double)]
+                ("eager", ctypes.c_int32), ("max_load", ctypes.c_double)]
 
     def as_dict(self):
         return {"rows": self.rows, "ctas_per_sm": self.ctas_per_sm, "direct": self.direct,
-                "max_load": self.max_load}
+                "eager": self.eager, "max_load": self.max_load}
 
 
 class ServerOptions(ctypes.Structure):
@@ -305,8 +305,8 @@ class Deduplicator:
         _check(load().mtc_write_restart_log(self.h, select_chkpt, logname.encode()))
 
     # -- tuning ------------------------------------------------------------
-    def set_tuning(self, rows=256, ctas_per_sm=0, direct=0, max_load=0.75):
-        t = Tune(rows, ctas_per_sm, direct, 0, max_load)
+    def set_tuning(self, rows=256, ctas_per_sm=0, direct=0, max_load=0.75, eager=0):
+        t = Tune(rows, ctas_per_sm, direct, eager, max_load)
         _check(load().mtc_set_tuning(self.h, ctypes.byref(t)))
 
     def tuning(self):

@@ -317,6 +317,11 @@ int autotune(int mode, int hash_kind, uint32_t chunk_size, uint64_t len, bool us
     rc = e.checkpoint(buf, len, true, &h);
     if (rc) break;
     e.current_id++;
+    // one untimed incremental step: captures the replayed launch sequence
+    tune_touch_kernel<<<grid, 256, 0, s>>>(buf, len, chunk_size, 50, 0x0fff);
+    rc = e.checkpoint(buf, len, false, &h);
+    if (rc) break;
+    e.current_id++;
     double sum = 0;
     for (int st = 0; st < kSteps; st++) {
       tune_touch_kernel<<<grid, 256, 0, s>>>(buf, len, chunk_size, 50, 0x1000 + st);

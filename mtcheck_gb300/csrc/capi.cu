@@ -501,6 +501,7 @@ int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t) {
   if (!(t->max_load > 0.1 && t->max_load <= 0.95)) return ret(MTC_EINVAL, "max_load outside (0.1, 0.95]");
   h->eng->set_leaf_tune(mtc::LeafTune{t->rows, t->ctas_per_sm, t->direct ? 1 : 0});
   h->eng->set_max_load(t->max_load);
+  h->eng->set_own_graph(t->eager == 0);
   return MTC_OK;
 }
 
@@ -511,6 +512,7 @@ int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* o) {
   o->rows = t.rows;
   o->ctas_per_sm = t.ctas_per_sm;
   o->direct = t.direct;
+  o->eager = h->eng->own_graph() ? 0 : 1;
   o->max_load = h->eng->max_load();
   return MTC_OK;
 }

@@ -34,6 +34,8 @@ Engine::Engine(int mode, int hash_kind, uint32_t chunk_size) : mode_(mode), hash
 
 Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_); else cudaDeviceSynchronize();
+  drop_own_graph();
+  if (cap_stream_) cudaStreamDestroy(cap_stream_);
   for (auto& e : ev_) if (e) cudaEventDestroy(e);
   if (lay_host_) cudaFreeHost(lay_host_);
   if (err_host_) cudaFreeHost(err_host_);
@@ -52,6 +54,11 @@ int Engine::fail(int code, const std::string& msg) {
     cudaError_t e_ = (call);                                                             \
     if (e_ != cudaSuccess) return fail(e_ == cudaErrorMemoryAllocation ? ST_ENOMEM : ST_ECUDA, \
                                        std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+#define MTC_TRY(call)         \
+  do {                        \
+    const int rc_ = (call);   \
+    if (rc_) return rc_;      \
   } while (0)
 
 int Engine::ensure_map(uint64_t want_entries, bool reset) {
@@ -225,7 +232,7 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.dup_cap = (uint32_t)fo_list_.n;
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
-  if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
+  if (timed_) MTC_TRY(mark(4));
   MTC_CUDA(launch_leaf_inserts(la, stream_));
 
   ForestArgs fa{};
@@ -276,7 +283,7 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.dup_cap = (uint32_t)fo_list_.n;
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
-  if (timed_) MTC_CUDA(cudaEventRecord(ev_[4], stream_));
+  if (timed_) MTC_TRY(mark(4));
   if (mode_ == MODE_LIST) MTC_CUDA(launch_leaf_inserts(la, stream_));
   MTC_CUDA(launch_chunk_compaction(labels_.p, N_, mode_ == MODE_BASIC ? 1 : 0, fo_list_.p, sh_list_.p, lay_.p, scan_.p,
                                    scan_total_.p, stream_));
@@ -319,23 +326,23 @@ void Engine::stage_params() {
 
 int Engine::enqueue(const uint8_t* data, uint64_t len, bool timed) {
   timed_ = timed;
-  if (timed) MTC_CUDA(cudaEventRecord(ev_[0], stream_));
+  if (timed) MTC_TRY(mark(0));
   if (mode_ == MODE_FULL) {
     // FullDeduplicator: the checkpoint is the raw buffer (src/full_approach.cpp:66-72)
-    if (timed) MTC_CUDA(cudaEventRecord(ev_[1], stream_));
-    if (timed) MTC_CUDA(cudaEventRecord(ev_[2], stream_));
+    if (timed) MTC_TRY(mark(1));
+    if (timed) MTC_TRY(mark(2));
     MTC_CUDA(cudaMemcpyAsync(stage_.p, data, len, cudaMemcpyDeviceToDevice, stream_));
-    if (timed) MTC_CUDA(cudaEventRecord(ev_[3], stream_));
+    if (timed) MTC_TRY(mark(3));
     return ST_OK;
   }
   MTC_CUDA(cudaMemcpyAsync(sp_.p, sp_host_, sizeof(StepParams), cudaMemcpyHostToDevice, stream_));
   MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
-  if (timed) MTC_CUDA(cudaEventRecord(ev_[1], stream_));
+  if (timed) MTC_TRY(mark(1));
   int rc = (mode_ == MODE_LIST || mode_ == MODE_BASIC) ? run_list_basic(data, len) : run_tree(data, len, baseline_path_);
   if (rc) return rc;
-  if (timed) MTC_CUDA(cudaEventRecord(ev_[2], stream_));
+  if (timed) MTC_TRY(mark(2));
   MTC_CUDA(launch_assemble(gather_args(data, len), (uint64_t)N_ + 1, stream_));
-  if (timed) MTC_CUDA(cudaEventRecord(ev_[3], stream_));
+  if (timed) MTC_TRY(mark(3));
   MTC_CUDA(cudaMemcpyAsync(lay_host_, lay_.p, sizeof(Layout), cudaMemcpyDeviceToHost, stream_));
   MTC_CUDA(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
   if (map_size_.p) MTC_CUDA(cudaMemcpyAsync(err_host_ + 1, map_size_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
@@ -349,24 +356,185 @@ int Engine::order_inputs() {
   return ST_OK;
 }
 
+void Engine::drop_own_graph() {
+  for (auto& sg : own_segs_) {
+    if (sg.exec) cudaGraphExecDestroy(sg.exec);
+    if (sg.graph) cudaGraphDestroy(sg.graph);
+  }
+  own_segs_.clear();
+  input_nodes_.clear();
+  own_sig_ = 0;
+  own_data_ = nullptr;
+}
+
+// Points the captured sequence at another input buffer of the same length
+// and alignment: the leaf kernels' descriptor and pointer, the chunk gather's
+// pointer (no other kernel reads the input).
+int Engine::retarget_own(const uint8_t* data, uint64_t len) {
+  for (auto& in : input_nodes_) {
+    void* args[3] = {nullptr, nullptr, nullptr};
+    if (in.kind == INPUT_LEAF_TMA) {
+      if (!input_tmap(&tma_, data, len, cs_, leaf_tune_)) return fail(ST_ECUDA, "tensor map for the new input");
+      in.tmap = tma_.map;
+      in.la.data = data;
+      args[0] = &in.tmap;
+      args[1] = &in.la;
+      args[2] = &in.u[0];
+    } else if (in.kind == INPUT_LEAF_DIRECT) {
+      in.la.data = data;
+      args[0] = &in.la;
+      args[1] = &in.u[0];
+      args[2] = &in.u[1];
+    } else {
+      in.ga.data = data;
+      args[0] = &in.ga;
+    }
+    cudaKernelNodeParams q = in.p;
+    q.kernelParams = args;
+    q.extra = nullptr;
+    MTC_CUDA(cudaGraphExecKernelNodeSetParams(own_segs_[in.seg].exec, in.node, &q));
+  }
+  own_data_ = data;
+  return ST_OK;
+}
+
+void Engine::set_own_graph(bool on) {
+  own_graph_ = on;
+  if (!on) drop_own_graph();
+}
+
+// A timing mark of the launch sequence: an event on the stream, or, while
+// the sequence is being captured, the end of one segment and the start of the
+// next (an event recorded by a graph cannot be timed, so the events are
+// recorded between the segments' launches).
+int Engine::mark(int i) {
+  if (!seg_capture_) {
+    MTC_CUDA(cudaEventRecord(ev_[i], stream_));
+    return ST_OK;
+  }
+  cudaGraph_t g = nullptr;
+  MTC_CUDA(cudaStreamEndCapture(cap_stream_, &g));
+  seg_graphs_.emplace_back(seg_mark_, g);
+  seg_mark_ = i;
+  MTC_CUDA(cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeRelaxed));
+  return ST_OK;
+}
+
+// The launch sequence of an incremental checkpoint as a few graph launches:
+// the sequence reads the step values from pinned host memory at run time, so
+// one capture serves every checkpoint until a device buffer, the input or
+// the launch shape changes (the signature).
+int Engine::replay_own(const uint8_t* data, uint64_t len) {
+  const uint64_t sig = shape_signature(data, len);
+  if (!own_segs_.empty() && sig == own_sig_ && data != own_data_) MTC_TRY(retarget_own(data, len));
+  if (own_segs_.empty() || sig != own_sig_) {
+    drop_own_graph();
+    if (!cap_stream_) MTC_CUDA(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
+    const uint64_t l0 = launch_count();
+    seg_graphs_.clear();
+    seg_mark_ = -1;
+    MTC_CUDA(cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeRelaxed));
+    cudaStream_t keep = stream_;
+    stream_ = cap_stream_;
+    seg_capture_ = true;
+    int rc = enqueue(data, len, true);
+    seg_capture_ = false;
+    stream_ = keep;
+    cudaGraph_t g = nullptr;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(cap_stream_, &st);
+    const cudaError_t ee = st == cudaStreamCaptureStatusActive ? cudaStreamEndCapture(cap_stream_, &g) : cudaSuccess;
+    if (g) seg_graphs_.emplace_back(seg_mark_, g);
+    cudaError_t ie = cudaSuccess;
+    if (rc == ST_OK && ee == cudaSuccess) {
+      for (auto& sg : seg_graphs_) {
+        size_t n = 0;
+        cudaGraphGetNodes(sg.second, nullptr, &n);
+        cudaGraphExec_t x = nullptr;
+        if (n && ie == cudaSuccess) ie = cudaGraphInstantiate(&x, sg.second, 0);
+        own_segs_.push_back(OwnSeg{sg.first, sg.second, x});
+        sg.second = nullptr;  // owned by own_segs_ (node handles stay valid for updates)
+        if (!n || ie != cudaSuccess) continue;
+        std::vector<cudaGraphNode_t> nodes(n);
+        cudaGraphGetNodes(own_segs_.back().graph, nodes.data(), &n);
+        for (cudaGraphNode_t nd : nodes) {
+          cudaGraphNodeType ty;
+          if (cudaGraphNodeGetType(nd, &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
+          InputNode in{};
+          if (cudaGraphKernelNodeGetParams(nd, &in.p) != cudaSuccess) continue;
+          in.kind = input_kernel_kind(in.p.func);
+          if (in.kind == INPUT_NONE) continue;
+          in.seg = own_segs_.size() - 1;
+          in.node = nd;
+          if (in.kind == INPUT_LEAF_TMA) {
+            std::memcpy(&in.tmap, in.p.kernelParams[0], sizeof(CUtensorMap));
+            std::memcpy(&in.la, in.p.kernelParams[1], sizeof(LeafArgs));
+            std::memcpy(&in.u[0], in.p.kernelParams[2], sizeof(uint32_t));
+          } else if (in.kind == INPUT_LEAF_DIRECT) {
+            std::memcpy(&in.la, in.p.kernelParams[0], sizeof(LeafArgs));
+            std::memcpy(&in.u[0], in.p.kernelParams[1], sizeof(uint32_t));
+            std::memcpy(&in.u[1], in.p.kernelParams[2], sizeof(uint32_t));
+          } else {
+            std::memcpy(&in.ga, in.p.kernelParams[0], sizeof(GatherArgs));
+          }
+          in.p.kernelParams = nullptr;
+          input_nodes_.push_back(in);
+        }
+      }
+    }
+    for (auto& sg : seg_graphs_)
+      if (sg.second) cudaGraphDestroy(sg.second);
+    seg_graphs_.clear();
+    if (rc != ST_OK || ee != cudaSuccess || ie != cudaSuccess) {
+      drop_own_graph();
+      cudaGetLastError();
+      if (rc != ST_OK) return rc;
+      return fail(ST_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ee != cudaSuccess ? ee : ie));
+    }
+    own_sig_ = sig;
+    own_data_ = data;
+    own_kernels_ = launch_count() - l0;  // counted while capturing, run by the launches below
+  } else {
+    note_launch((uint32_t)own_kernels_);
+  }
+  for (auto& sg : own_segs_) {
+    if (sg.mark >= 0) MTC_CUDA(cudaEventRecord(ev_[sg.mark], stream_));
+    if (sg.exec) MTC_CUDA(cudaGraphLaunch(sg.exec, stream_));
+  }
+  return ST_OK;
+}
+
 int Engine::checkpoint(const uint8_t* data, uint64_t len, bool make_baseline, HeaderHost* header) {
   int rc = prepare(data, len, make_baseline, 0);
   if (rc) return rc;
   if ((rc = order_inputs()) != ST_OK) return rc;
   if (mode_ != MODE_FULL) stage_params();
-  rc = enqueue(data, len, true);
+  // a step that allocates (a first checkpoint or a new baseline) runs eagerly
+  if (own_graph_ && mode_ != MODE_FULL && !fresh_) rc = replay_own(data, len);
+  else rc = enqueue(data, len, true);
   if (rc) return rc;
   MTC_CUDA(cudaStreamSynchronize(stream_));
   release_retired();
   return complete(len, header);
 }
 
+// Milliseconds between two of the engine's events; 0 when they cannot be
+// timed (the error is consumed, not left for the next call to find).
+static float event_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return ms;
+}
+
 int Engine::complete(uint64_t len, HeaderHost* header) {
   float ms[3] = {0, 0, 0};
   if (timed_) {
-    cudaEventElapsedTime(&ms[0], ev_[0], ev_[1]);
-    cudaEventElapsedTime(&ms[1], ev_[1], ev_[2]);
-    cudaEventElapsedTime(&ms[2], ev_[2], ev_[3]);
+    ms[0] = event_ms(ev_[0], ev_[1]);
+    ms[1] = event_ms(ev_[1], ev_[2]);
+    ms[2] = event_ms(ev_[2], ev_[3]);
     timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
   }
   if (mode_ == MODE_FULL) {
@@ -381,9 +549,7 @@ int Engine::complete(uint64_t len, HeaderHost* header) {
   last_device_error = err_host_[0];
   if (map_size_.p) map_size_host_ = err_host_[1];
   if (timed_) {
-    float leaf = 0, rest = 0;
-    cudaEventElapsedTime(&leaf, ev_[1], ev_[4]);
-    cudaEventElapsedTime(&rest, ev_[4], ev_[2]);
+    const float leaf = event_ms(ev_[1], ev_[4]), rest = event_ms(ev_[4], ev_[2]);
     phase_times[0] = leaf * 1e-3; phase_times[1] = rest * 1e-3; phase_times[2] = ms[2] * 1e-3;
   }
   if (last_device_error & DERR_SPIN) return fail(ST_ETIMEOUT, "bounded device wait expired");
@@ -413,7 +579,14 @@ int Engine::complete(uint64_t len, HeaderHost* header) {
 uint64_t Engine::signature(const uint8_t* data, uint64_t len) const {
   // everything a captured launch sequence bakes in: the input, every device
   // buffer, the map and sort capacities, the baseline branch
-  const uint64_t v[] = {(uint64_t)data, len, (uint64_t)digests_.p, (uint64_t)labels_.p, (uint64_t)rflag_.p,
+  return (shape_signature(data, len) ^ (uint64_t)data) * 1099511628211ull;
+}
+
+uint64_t Engine::shape_signature(const uint8_t* data, uint64_t len) const {
+  // the signature without the input's address, only its alignment (which
+  // chooses the kernels that read it): the single-call graph follows a moved
+  // input by retarget_own
+  const uint64_t v[] = {(uint64_t)data & 15, len, (uint64_t)digests_.p, (uint64_t)labels_.p, (uint64_t)rflag_.p,
                         (uint64_t)chunk_slot_.p, (uint64_t)changed_list_.p, (uint64_t)changed_count_.p,
                         (uint64_t)slots_.p, map_cap_, (uint64_t)map_size_.p, (uint64_t)err_.p, (uint64_t)fo_list_.p,
                         (uint64_t)sh_list_.p, (uint64_t)reg_chunk_.p, (uint64_t)reg_slot_.p, (uint64_t)reg_len_.p,

@@ -106,9 +106,16 @@ class Engine {
   int complete(uint64_t len, HeaderHost* header);
   // Fingerprint of everything a captured sequence depends on.
   uint64_t signature(const uint8_t* dev_data, uint64_t len) const;
+  // The same without the input's address (only its alignment).
+  uint64_t shape_signature(const uint8_t* dev_data, uint64_t len) const;
   bool fresh() const { return fresh_; }
   // True once after prepare() put work on the engine's stream that leaves
   // every device pointer in place (so the signature does not show it).
+  // The single-call path replays its launch sequence as a CUDA graph,
+  // captured at the first incremental checkpoint and again whenever the
+  // signature changes (on by default; a Batch never uses it).
+  void set_own_graph(bool on);
+  bool own_graph() const { return own_graph_; }
   bool take_stream_work() {
     const bool w = stream_work_;
     stream_work_ = false;
@@ -191,6 +198,37 @@ class Engine {
   double max_load_ = 0.75;
   LeafTune leaf_tune_{};
   uint32_t N_ = 0, M_ = 0;
+  bool own_graph_ = true;
+  // the captured sequence, cut at the timing marks: the event recorded
+  // before each segment (or -1) and the segment's graph (null when empty)
+  struct OwnSeg {
+    int mark;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+  };
+  std::vector<OwnSeg> own_segs_;
+  // kernel nodes that read the input buffer, with their captured arguments
+  struct InputNode {
+    size_t seg;
+    cudaGraphNode_t node;
+    int kind;
+    cudaKernelNodeParams p;
+    CUtensorMap tmap;
+    LeafArgs la;
+    uint32_t u[2];
+    GatherArgs ga;
+  };
+  std::vector<InputNode> input_nodes_;
+  const uint8_t* own_data_ = nullptr;  // input pointer the graphs currently read
+  cudaStream_t cap_stream_ = nullptr;  // private stream the sequence is captured on
+  uint64_t own_sig_ = 0, own_kernels_ = 0;
+  int retarget_own(const uint8_t* data, uint64_t len);
+  bool seg_capture_ = false;  // enqueue runs under a capture cut at each mark
+  int seg_mark_ = -1;
+  std::vector<std::pair<int, cudaGraph_t>> seg_graphs_;
+  int replay_own(const uint8_t* data, uint64_t len);
+  int mark(int i);
+  void drop_own_graph();
   bool stream_work_ = false;
   uint32_t epoch_ = 0;
   uint64_t map_cap_ = 0;

@@ -1340,6 +1340,9 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
     note_launch(2);
   }
   const bool vec = (g.cs % 16 == 0) && ((reinterpret_cast<uintptr_t>(g.data) & 15) == 0);
+  static const bool reg = (register_input_kernel(reinterpret_cast<const void*>(copy_kernel), INPUT_GATHER),
+                           register_input_kernel(reinterpret_cast<const void*>(copy_bytes_kernel), INPUT_GATHER), true);
+  (void)reg;
   if (vec) copy_kernel<<<num_sms() * 8, 256, 0, s>>>(g);
   else copy_bytes_kernel<<<num_sms() * 8, 256, 0, s>>>(g);
   note_launch();

@@ -16,6 +16,8 @@
 #include <cstdio>
 #include <atomic>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "mtc_common.cuh"
 #include "mtc_internal.hpp"
@@ -343,6 +345,8 @@ bool make_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, int 
 template <int HK, int EPI, int W, int R>
 cudaError_t launch_tma_t(const LeafArgs& a, const CUtensorMap& m, uint32_t n_full, int ctas_per_sm, cudaStream_t s) {
   auto k = leaf_tma_kernel<HK, EPI, W, R>;
+  static const bool reg = (register_input_kernel(reinterpret_cast<const void*>(k), INPUT_LEAF_TMA), true);
+  (void)reg;
   const size_t smem = 1024 + (size_t)kStages * R * W + 2 * kStages * sizeof(uint64_t);
   static std::atomic<bool> attr_set{false};
   if (!attr_set.load(std::memory_order_acquire)) {
@@ -390,6 +394,9 @@ cudaError_t launch_direct(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStrea
   uint32_t grid = (uint32_t)((n + 127) / 128);
   uint32_t cap = (uint32_t)num_sms() * 16;
   if (grid > cap) grid = cap;
+  static const bool reg =
+      (register_input_kernel(reinterpret_cast<const void*>(leaf_direct_kernel<EPI>), INPUT_LEAF_DIRECT), true);
+  (void)reg;
   leaf_direct_kernel<EPI><<<grid, 128, 0, s>>>(a, c0, c1);
   note_launch();
   return cudaGetLastError();
@@ -414,6 +421,21 @@ cudaError_t dispatch_tma(const LeafArgs& a, const CUtensorMap& m, uint32_t n_ful
 }
 }  // namespace
 
+namespace {
+std::mutex g_input_mu;
+std::vector<std::pair<const void*, int>> g_input_kernels;
+}  // namespace
+void register_input_kernel(const void* func, int kind) {
+  std::lock_guard<std::mutex> lk(g_input_mu);
+  g_input_kernels.emplace_back(func, kind);
+}
+int input_kernel_kind(const void* func) {
+  std::lock_guard<std::mutex> lk(g_input_mu);
+  for (auto& e : g_input_kernels)
+    if (e.first == func) return e.second;
+  return INPUT_NONE;
+}
+
 static std::atomic<uint64_t> g_launches{0};
 void note_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
@@ -427,6 +449,14 @@ int num_sms() {
     if (n <= 0) n = 1;
   }
   return n;
+}
+
+bool input_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, const LeafTune& tune) {
+  const uint32_t n_full = (uint32_t)(len / cs);
+  const int W = tma_width(cs);
+  const int rows = tune.rows != 128 ? 256 : 128;
+  return W && n_full > 0 && (reinterpret_cast<uintptr_t>(data) & 15) == 0 &&
+         make_tmap(c, data, len, cs, W, rows, n_full);
 }
 
 cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, const LeafTune& tune) {

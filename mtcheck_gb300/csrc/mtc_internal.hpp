@@ -91,6 +91,21 @@ int num_sms();
 // Running count of kernel launches issued by the library (all handles).
 void note_launch(uint32_t n = 1);
 uint64_t launch_count();
+
+// Kernels that read the checkpointed buffer itself, by argument layout: a
+// captured launch sequence follows a new input pointer by updating exactly
+// these nodes.  Registered once per kernel by its launch site.
+enum : int {
+  INPUT_NONE = 0,
+  INPUT_LEAF_TMA = 1,     // (const CUtensorMap, LeafArgs, uint32_t)
+  INPUT_LEAF_DIRECT = 2,  // (LeafArgs, uint32_t, uint32_t)
+  INPUT_GATHER = 3,       // (GatherArgs)
+};
+void register_input_kernel(const void* func, int kind);
+int input_kernel_kind(const void* func);
+// The descriptor launch_leaves gives the TMA leaf kernel for this buffer and
+// launch shape (in c->map); false when TMA does not apply.
+bool input_tmap(TmaCache* c, const uint8_t* data, uint64_t len, uint32_t cs, const LeafTune& tune);
 // Message returned by mtc_last_error() on this thread.
 void set_last_error(const char* msg);
 
