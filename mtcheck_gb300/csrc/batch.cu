@@ -47,6 +47,7 @@ void Batch::drop_parent() {
   if (parent_) cudaGraphDestroy(parent_);
   parent_exec_ = nullptr;
   parent_ = nullptr;
+  child_nodes_.clear();
 }
 
 void Batch::drop_graph() {
@@ -85,7 +86,6 @@ int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
   } while (0)
 
 int Batch::capture_member(size_t i, const uint8_t* data, uint64_t len) {
-  drop_parent();
   if (graphs_[i]) cudaGraphDestroy(graphs_[i]);
   graphs_[i] = nullptr;
   const uint64_t l0 = launch_count();
@@ -110,11 +110,11 @@ int Batch::capture_member(size_t i, const uint8_t* data, uint64_t len) {
 }
 
 int Batch::build_parent() {
+  drop_parent();
   MTC_BCUDA(cudaGraphCreate(&parent_, 0));
-  for (size_t i = 0; i < engs_.size(); i++) {
-    cudaGraphNode_t node;
-    MTC_BCUDA(cudaGraphAddChildGraphNode(&node, parent_, nullptr, 0, graphs_[i]));
-  }
+  child_nodes_.assign(engs_.size(), nullptr);
+  for (size_t i = 0; i < engs_.size(); i++)
+    MTC_BCUDA(cudaGraphAddChildGraphNode(&child_nodes_[i], parent_, nullptr, 0, graphs_[i]));
   cudaError_t ie = cudaGraphInstantiate(&parent_exec_, parent_, 0);
   if (ie != cudaSuccess) {
     parent_exec_ = nullptr;
@@ -144,15 +144,21 @@ int Batch::checkpoint(const uint8_t* const* data, const uint64_t* lens, bool mak
   // work are joined into the origin stream before the step
   std::vector<char> join(engs_.size(), 0);
   if (graph) {
+    bool rebuild = !parent_exec_;
     for (size_t i = 0; i < engs_.size(); i++) {
       if (engs_[i]->take_stream_work()) join[i] = 1;
       if (!graphs_[i] || sigs_[i] != engs_[i]->signature(data[i], lens[i])) {
         int rc = capture_member(i, data[i], lens[i]);
         if (rc) return rc;
         join[i] = 1;
+        // same launch sequence on moved buffers: update the member's node
+        if (!rebuild && cudaGraphExecChildGraphNodeSetParams(parent_exec_, child_nodes_[i], graphs_[i]) != cudaSuccess) {
+          cudaGetLastError();
+          rebuild = true;
+        }
       }
     }
-    if (!parent_exec_) {
+    if (rebuild) {
       int rc = build_parent();
       if (rc) return rc;
     }

@@ -9,8 +9,9 @@
 //     stream.  A member's sequence reads the per-step values (checkpoint id,
 //     epochs) from pinned host memory, so it is captured once and replayed
 //     until that member's device buffers move (map growth, a new input
-//     pointer); only that member is captured again, and the parent graph is
-//     rebuilt from the members' graphs.
+//     pointer); only that member is captured again and its child node of
+//     the instantiated parent updated (the parent is rebuilt when the
+//     update is refused).
 // A step starts after all work already issued to the legacy default stream
 // (where the inputs are usually written); inputs written on other streams
 // must be synchronised by the caller.
@@ -69,6 +70,7 @@ class Batch {
   std::vector<uint64_t> sigs_, nodes_, kernels_;
   cudaGraph_t parent_ = nullptr;     // one child graph node per member
   cudaGraphExec_t parent_exec_ = nullptr;
+  std::vector<cudaGraphNode_t> child_nodes_;  // member i's node in parent_
   bool use_graph_ = true;
   uint32_t headroom_ = 64;
   BatchStats stats_;

@@ -153,7 +153,8 @@ def test_member_handles_are_owned(cuda, mtc):
 
 @pytest.mark.parametrize("tune", [
     dict(rows=128), dict(rows=256, ctas_per_sm=1), dict(rows=128, ctas_per_sm=4), dict(direct=1),
-    dict(max_load=0.5), dict(max_load=0.9), dict(rows=128, ctas_per_sm=2, max_load=0.6),
+    dict(max_load=0.5), dict(max_load=0.9), dict(rows=128, ctas_per_sm=2, max_load=0.6), dict(eager=1),
+    dict(direct=1, eager=1),
 ])
 def test_tuning_does_not_change_output(cuda, mtc, states, lone, tune):
     for i in (0, 1, 3, 4, 5, 6):

@@ -116,6 +116,28 @@ def test_epochs_rebased_near_their_limit(cuda, mtc, oracle, monkeypatch):
         run_both(cuda, mtc, oracle, approach, 0, seq, 128)
 
 
+@pytest.mark.parametrize("kind", [0, 1], ids=["murmur3", "md5"])
+@pytest.mark.parametrize("approach", [3, 4], ids=["list", "tree"])
+@pytest.mark.parametrize("issue", ["in_place", "alternating", "eager"])
+def test_graph_replay_matches_oracle(cuda, mtc, oracle, kind, approach, issue):
+    # the single-call path replays a captured launch sequence: on the same
+    # buffer rewritten in place, on two buffers taking turns (the sequence
+    # retargeted to the other input), and issued eagerly
+    nbytes, cs = (1 << 20) + 77, 256
+    seq = series(2, nbytes, cs, 7, seed=11 + kind)
+    ref = oracle.Deduplicator(approach, cs, kind)
+    gpu = mtc.Deduplicator(cs, kind, approach=approach)
+    if issue == "eager":
+        gpu.set_tuning(eager=1)
+    bufs = [cuda.empty(nbytes, dtype=cuda.uint8, device="cuda") for _ in range(2)]
+    for i, s in enumerate(seq):
+        buf = bufs[i % 2] if issue == "alternating" else bufs[0]
+        buf.copy_(cuda.from_numpy(s))
+        assert gpu.checkpoint(buf, i == 0) == ref.checkpoint(s, i == 0), (issue, i)
+    assert gpu.tuning()["eager"] == (1 if issue == "eager" else 0)
+    gpu.close()
+
+
 def test_same_id_header_overload(cuda, mtc, oracle):
     # checkpoint(header_t&, ...) does not advance current_id
     seq = series(1, 1 << 18, 128, 3, seed=2)
