@@ -82,8 +82,9 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uin
   append_changed(a, changed, c);
 }
 
-// A note for the demote pass; kCheckCreator: the chunk met an entry that
-// another insert of this launch created, whose chunk is checked too.
+// A note for the demote pass (a changed-list position); kCheckCreator: the
+// chunk met an entry that another insert of this launch created, whose chunk
+// is checked too.
 constexpr uint32_t kCheckCreator = 1u << 31;  // chunk counts stay below 2^31
 __device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t note) {
   const uint32_t k = atomicAdd(a.dup_count, 1u);
@@ -121,7 +122,7 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
       const unsigned long long old = atomicMin(&s->win, win_of(epoch, node));
       if (old == kWinEmpty || win_epoch(old) == epoch) {
         label = FIRST_OCUR;  // first seen by this launch: the lowest chunk keeps it
-        note_dup(a, c | kCheckCreator);
+        note_dup(a, (uint32_t)k | kCheckCreator);
       } else if (EPI == EPI_TREE && __ldcg(&s->tree) == cur) {
         // lowest node within the older entry, its epoch kept
         unsigned long long w = old;
@@ -131,10 +132,10 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
           w = seen;
         }
         label = FIRST_OCUR;
-        note_dup(a, c);
+        note_dup(a, (uint32_t)k);
       }
     }
-    a.chunk_slot[c] = (uint32_t)slot;
+    a.chunk_slot[k] = (uint32_t)slot;  // by list position: a sequential write
     a.labels[c] = label;
   }
   count_new_entries(a.map, created);
@@ -157,12 +158,12 @@ __global__ void leaf_demote_kernel(LeafArgs a) {
   const uint32_t nd = *a.dup_count;
   const bool all = nd > a.dup_cap;
   const uint32_t n = all ? *a.changed_count : nd;
-  const uint32_t* list = all ? a.changed_list : a.dup_list;
   const uint32_t cur = a.sp->cur;
-  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t e = list[k];
-    const uint32_t c = all ? e : (e & ~kCheckCreator);
-    const MapSlot* s = &a.map.slots[a.chunk_slot[c]];
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t e = all ? (uint32_t)i : a.dup_list[i];
+    const uint32_t k = e & ~kCheckCreator;
+    const uint32_t c = a.changed_list[k];
+    const MapSlot* s = &a.map.slots[a.chunk_slot[k]];
     demote_chunk(a, c, s, cur);
     if (!all && (e & kCheckCreator)) demote_chunk(a, s->first_chunk, s, cur);
   }

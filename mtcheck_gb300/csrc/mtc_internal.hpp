@@ -38,7 +38,7 @@ struct LeafArgs {
   uint32_t n_chunks = 0;          // ceil(len / cs)
   Digest* prev = nullptr;         // per-chunk digest of the previous checkpoint (tree leaves or hash list)
   uint8_t* labels = nullptr;      // per-chunk label / changed flag out
-  uint32_t* chunk_slot = nullptr; // per-chunk map slot of a changed chunk
+  uint32_t* chunk_slot = nullptr; // map slot of each changed-list entry (by list position)
   Digest* out = nullptr;          // EPI_HASH output
   DigestMap map{};
   const StepParams* sp = nullptr; // current checkpoint id and launch epoch (device)
@@ -47,7 +47,7 @@ struct LeafArgs {
   uint32_t* changed_list = nullptr;  // chunks whose digest changed (tree, list)
   uint32_t* changed_count = nullptr;
   uint32_t* demoted = nullptr;    // set to 1 when a first occurrence is demoted (tree; may be null)
-  uint32_t* dup_list = nullptr;   // chunks that met a duplicate of their digest inserted by the same launch
+  uint32_t* dup_list = nullptr;   // changed-list positions that met a duplicate inserted by the same launch
   uint32_t* dup_count = nullptr;  // appends; above dup_cap the demote pass visits every changed chunk
   uint32_t dup_cap = 0;
   int hash_kind = HASH_MURMUR3;

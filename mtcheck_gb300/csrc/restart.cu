@@ -583,33 +583,60 @@ __global__ void walk_kernel(RArgs a) {
 }
 
 // 5. one copy per chunk from the diff that owns it; one thread per 16-byte
-//    unit of the output (chunk sizes that are not multiples of 16 go byte by byte)
+//    unit of the output, two units in flight (chunk sizes that are not
+//    multiples of 16 go byte by byte)
+struct GatherUnit {
+  const uint8_t* src;
+  uint8_t* dst;
+  uint32_t n;  // bytes to copy, 0 for none
+};
+__device__ __forceinline__ GatherUnit gather_unit(const RArgs& a, uint64_t u, uint64_t upc, int lg) {
+  GatherUnit g{nullptr, nullptr, 0};
+  const uint64_t cs = a.cs;
+  const uint64_t c = lg >= 0 ? u >> lg : u / upc;
+  const uint64_t byte = u * 16, within = (u - c * upc) * 16;
+  const uint64_t r = a.res[c];
+  if (r == kNone) return g;
+  const DiffInfo& d = a.di[r >> kOffBits];
+  const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1)) + within;
+  uint64_t n = 16;
+  if (byte + n > a.datalen) n = a.datalen - byte;
+  if (c * cs + cs > a.datalen && within + n > a.datalen - c * cs) n = a.datalen - c * cs - within;
+  if (off >= d.len) return g;
+  if (off + n > d.len) n = d.len - off;
+  g.src = d.base + off;
+  g.dst = a.out + byte;
+  g.n = (uint32_t)n;
+  return g;
+}
+__device__ __forceinline__ void gather_copy(const GatherUnit& g, const uint4& v) {
+  if (g.n == 16 && (((uintptr_t)g.src | (uintptr_t)g.dst) & 15) == 0) {
+    *reinterpret_cast<uint4*>(g.dst) = v;
+  } else if (g.n == 16 && (((uintptr_t)g.src | (uintptr_t)g.dst) & 3) == 0) {
+    const uint32_t* s4 = reinterpret_cast<const uint32_t*>(g.src);
+    *reinterpret_cast<uint4*>(g.dst) = make_uint4(s4[0], s4[1], s4[2], s4[3]);
+  } else {
+    for (uint32_t b = 0; b < g.n; b++) g.dst[b] = g.src[b];
+  }
+}
+__device__ __forceinline__ uint4 gather_load(const GatherUnit& g) {
+  if (g.n == 16 && (((uintptr_t)g.src | (uintptr_t)g.dst) & 15) == 0)
+    return __ldcs(reinterpret_cast<const uint4*>(g.src));
+  return make_uint4(0, 0, 0, 0);
+}
 __global__ void gather_kernel(RArgs a) {
   const uint64_t cs = a.cs;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   if (cs % 16 == 0) {
     const uint64_t units = (a.datalen + 15) / 16;
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += stride) {
-      const uint64_t byte = u * 16, c = byte / cs, within = byte - c * cs;
-      const uint64_t r = a.res[c];
-      if (r == kNone) continue;
-      const DiffInfo& d = a.di[r >> kOffBits];
-      const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1)) + within;
-      uint64_t n = 16;
-      if (byte + n > a.datalen) n = a.datalen - byte;
-      if (c * cs + cs > a.datalen && within + n > a.datalen - c * cs) n = a.datalen - c * cs - within;
-      if (off >= d.len) continue;
-      if (off + n > d.len) n = d.len - off;
-      const uint8_t* src = d.base + off;
-      uint8_t* dst = a.out + byte;
-      if (n == 16 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
-        *reinterpret_cast<uint4*>(dst) = __ldcs(reinterpret_cast<const uint4*>(src));
-      } else if (n == 16 && (((uintptr_t)src | (uintptr_t)dst) & 3) == 0) {
-        const uint32_t* s4 = reinterpret_cast<const uint32_t*>(src);
-        *reinterpret_cast<uint4*>(dst) = make_uint4(s4[0], s4[1], s4[2], s4[3]);
-      } else {
-        for (uint64_t b = 0; b < n; b++) dst[b] = src[b];
-      }
+    const uint64_t upc = cs / 16;  // units per chunk; a power of two is a shift
+    const int lg = (upc & (upc - 1)) == 0 ? __ffsll((long long)upc) - 1 : -1;
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += 2 * stride) {
+      const GatherUnit g0 = gather_unit(a, u, upc, lg);
+      const GatherUnit g1 = u + stride < units ? gather_unit(a, u + stride, upc, lg) : GatherUnit{nullptr, nullptr, 0};
+      const uint4 v0 = gather_load(g0), v1 = gather_load(g1);
+      if (g0.n) gather_copy(g0, v0);
+      if (g1.n) gather_copy(g1, v1);
     }
     return;
   }
