@@ -45,6 +45,9 @@ def parse():
     p.add_argument("--hash", default="murmur3", choices=["murmur3", "md5"])
     p.add_argument("--size-gib", type=float, default=4.0)
     p.add_argument("--chunk", type=int, default=512)
+    p.add_argument("--pattern", default="4gib", choices=["4gib", "64mib"],
+                   help="update series: the 4 GiB one (sparse chunks, runs, shifted copies, a zero range) or the "
+                        "64 MiB one (20%% duplicated chunks at first, then 1%% rewritten per step in runs of 1-32)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-restart", action="store_true")
@@ -164,13 +167,20 @@ def whole_job_rate(bytes_per_rank, seconds, ws):
     return bytes_per_rank * ws / seconds / 1e9
 
 
-def make_states(torch, nbytes, cs, count, seed, device):
+PATTERN_NAME = {"4gib": "the 4 GiB update pattern", "64mib": "the 64 MiB update pattern"}
+
+
+def series(pattern, nbytes, cs, count, seed, device=None):
+    """States of one of the two update series (generator)."""
     from mtcheck_gb300 import workloads
+    if pattern == "64mib":
+        return workloads.pattern1(nbytes, cs, count, seed=seed, device=device)
     z = (GIB, GIB + GIB // 2) if nbytes >= 2 * GIB else (nbytes // 4, nbytes // 4 + nbytes // 8)
-    states = []
-    for s in workloads.pattern2(nbytes, cs, count, seed=seed, device=device, zero_range=z):
-        states.append(s.clone())
-    return states
+    return workloads.pattern2(nbytes, cs, count, seed=seed, device=device, zero_range=z)
+
+
+def make_states(torch, nbytes, cs, count, seed, device, pattern="4gib"):
+    return [s.clone() for s in series(pattern, nbytes, cs, count, seed, device)]
 
 
 def restart_bench(torch, mc, dev, a, kind, approach=None):
@@ -236,14 +246,11 @@ def restart_bench(torch, mc, dev, a, kind, approach=None):
                     "host_chain_value: chain in pageable host memory, copied to HBM inside the call"}
 
 
-def cpu_sample(kind, cs, seconds_hint=20.0):
-    """Single-thread oracle on a 1 GiB sample of the same pattern: baseline + incrementals."""
-    import numpy as np
-    from mtcheck_gb300 import workloads
+def cpu_sample(kind, cs, pattern="4gib", nbytes=GIB):
+    """Single-thread oracle on a sample of the same pattern (at most 1 GiB): baseline + incrementals."""
     from oracle import pyoracle
-    n = GIB
-    z = (n // 4, n // 4 + n // 8)
-    seq = workloads.pattern2(n, cs, 4, seed=123, zero_range=z)
+    n = min(nbytes, GIB) // cs * cs
+    seq = series(pattern, n, cs, 4, seed=123)
     d = pyoracle.Deduplicator(pyoracle.TREE, cs, kind)
     first = next(seq).copy()
     d.checkpoint(first, True)
@@ -258,11 +265,9 @@ def cpu_sample(kind, cs, seconds_hint=20.0):
 def reference_worker(args):
     """One host thread of the CPU reference arm: oracle dedup of an independent slice."""
     sys.path.insert(0, ROOT)
-    nbytes, cs, kind, steps, warmup, seed = args
-    from mtcheck_gb300 import workloads
+    nbytes, cs, kind, steps, warmup, seed, pattern = args
     from oracle import pyoracle
-    z = (nbytes // 4, nbytes // 4 + nbytes // 8)
-    seq = [s.copy() for s in workloads.pattern2(nbytes, cs, 1 + warmup + steps, seed=seed, zero_range=z)]
+    seq = [s.copy() for s in series(pattern, nbytes, cs, 1 + warmup + steps, seed)]
     d = pyoracle.Deduplicator(pyoracle.TREE, cs, kind)
     d.checkpoint(seq[0], True)
     for s in seq[1:1 + warmup]:
@@ -285,15 +290,16 @@ def run_reference(a, ws, rank):
     per = max(a.chunk, (total // cores) // a.chunk * a.chunk)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        t = pool.map(reference_worker, [(per, a.chunk, kind, a.steps, a.warmup, 1000 + i) for i in range(cores)])
+        t = pool.map(reference_worker, [(per, a.chunk, kind, a.steps, a.warmup, 1000 + i, a.pattern)
+                                        for i in range(cores)])
     elapsed = max(t)
     value = per * cores * a.steps / elapsed / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(elapsed / a.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "tree dedup, %s, %.3g GiB buffer, %d B chunks, 4 GiB update pattern"
-                   % (a.hash, a.size_gib, a.chunk), "approach": "tree", "hash": a.hash},
+        "config": {"workload": "tree dedup, %s, %.3g GiB buffer, %d B chunks, %s"
+                   % (a.hash, a.size_gib, a.chunk, PATTERN_NAME[a.pattern]), "approach": "tree", "hash": a.hash},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
                          "sample": "%d host processes, each deduplicating an independent %d MiB slice (own map and "
                                    "tree) for %d timed incremental checkpoints after a baseline and %d warm-up"
@@ -677,7 +683,7 @@ def main():
     N = (nbytes + cs - 1) // cs
     dev = torch.device("cuda", local)
     K, W = a.steps, a.warmup
-    states = make_states(torch, nbytes, cs, 1 + W + K, seed=77 + rank, device=dev)
+    states = make_states(torch, nbytes, cs, 1 + W + K, seed=77 + rank, device=dev, pattern=a.pattern)
     torch.cuda.synchronize()
 
     def barrier():
@@ -691,13 +697,23 @@ def main():
     for s in states[1:1 + W]:
         dd.checkpoint_device(s, False)
     leaf_t, tree_t, asm_t, ckpt_t, sizes, sdata, smeta = [], [], [], [], [], [], []
+    # inputs that fit in L2 (129 MB) several times over: every step timed on
+    # its own, after a 256 MiB write that flushes L2 (outside its events)
+    small = nbytes < (512 << 20)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if small else None
+    step_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     l0 = mc.launch_count()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
         start.record()
-        for s in states[1 + W:]:
+        for i, s in enumerate(states[1 + W:]):
+            if small:
+                flush.zero_()
+                step_ev[i][0].record()
             n = dd.checkpoint_device(s, False)
+            if small:
+                step_ev[i][1].record()
             info = dd.info()
             leaf_t.append(info.phase_times[0])
             tree_t.append(info.phase_times[1])
@@ -709,7 +725,11 @@ def main():
         stop.record()
         barrier()
     launches = mc.launch_count() - l0
-    elapsed = max_over_ranks(torch, start.elapsed_time(stop) / 1e3, dev, ws)
+    if small:
+        timed = sum(e0.elapsed_time(e1) for e0, e1 in step_ev) / 1e3
+    else:
+        timed = start.elapsed_time(stop) / 1e3
+    elapsed = max_over_ranks(torch, timed, dev, ws)
     value = whole_job_rate(nbytes * K, elapsed, ws)
 
     # roofline of the dominant kernel (leaf hashing): per chunk the chunk bytes,
@@ -801,10 +821,11 @@ def main():
 
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu:
-        v, nsteps = cpu_sample(1 if a.hash == "md5" else 0, cs)
+        v, nsteps = cpu_sample(1 if a.hash == "md5" else 0, cs, a.pattern, nbytes)
         cpu = {"value": round(v, 3), "unit": "GB/s", "cores": 1, "kind": "port",
-               "sample": "oracle restatement, one host thread, 1 GiB buffer of the same update pattern and chunk "
-                         "size, mean of %d incremental checkpoints after a baseline" % nsteps}
+               "sample": "oracle restatement, one host thread, %d MiB buffer of the same update pattern and chunk "
+                         "size, mean of %d incremental checkpoints after a baseline" % (min(nbytes, GIB) >> 20,
+                                                                                      nsteps)}
 
     if rank == 0:
         line = {
@@ -812,9 +833,11 @@ def main():
             "ms_per_step": round(elapsed / K * 1e3, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "config": {"workload": "tree dedup (lowest offset), %s, %.3g GiB buffer, %d B chunks, incremental "
-                                   "checkpoints of the 4 GiB update pattern" % (a.hash, a.size_gib, cs),
+                                   "checkpoints of %s" % (a.hash, a.size_gib, cs, PATTERN_NAME[a.pattern]),
                        "approach": "tree", "hash": a.hash, "buffer_bytes": nbytes, "chunk_size": cs,
-                       "chunks": N, "l2": "inputs (%d MiB) larger than L2" % (nbytes >> 20),
+                       "chunks": N,
+                       "l2": ("L2 flushed before every step (256 MiB write outside the step's events)" if small
+                              else "inputs (%d MiB) larger than L2" % (nbytes >> 20)),
                        "parallelism": "replicas" if ws > 1 else "single GPU",
                        "host_cpus": host_cpus,
                        "diff_bytes_mean": int(sum(sizes) / K),
