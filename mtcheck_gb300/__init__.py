@@ -305,8 +305,12 @@ class Deduplicator:
         _check(load().mtc_write_restart_log(self.h, select_chkpt, logname.encode()))
 
     # -- tuning ------------------------------------------------------------
-    def set_tuning(self, rows=256, ctas_per_sm=0, direct=0, max_load=0.75, eager=0):
-        t = Tune(rows, ctas_per_sm, direct, eager, max_load)
+    def set_tuning(self, rows=None, ctas_per_sm=None, direct=None, max_load=None, eager=None):
+        """Set the given fields of the launch tuning; the others keep their values."""
+        cur = self.tuning()
+        pick = lambda v, k: cur[k] if v is None else v
+        t = Tune(pick(rows, "rows"), pick(ctas_per_sm, "ctas_per_sm"), pick(direct, "direct"), pick(eager, "eager"),
+                 pick(max_load, "max_load"))
         _check(load().mtc_set_tuning(self.h, ctypes.byref(t)))
 
     def tuning(self):

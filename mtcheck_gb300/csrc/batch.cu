@@ -299,7 +299,7 @@ int autotune(int mode, int hash_kind, uint32_t chunk_size, uint64_t len, bool us
     double load;
   };
   std::vector<Cand> cands;
-  cands.push_back({LeafTune{256, 0, 0}, 0.75});  // the default shape first
+  cands.push_back({default_leaf_tune(hash_kind), 0.75});  // the default shape first
   const double loads_tree[] = {0.5, 0.75, 0.9};
   const bool has_map = mode != MODE_BASIC && mode != MODE_FULL;
   for (int rows : {256, 128})

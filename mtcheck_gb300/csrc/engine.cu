@@ -21,7 +21,8 @@ static uint64_t next_pow2(uint64_t v) {
   return c;
 }
 
-Engine::Engine(int mode, int hash_kind, uint32_t chunk_size) : mode_(mode), hash_kind_(hash_kind), cs_(chunk_size) {
+Engine::Engine(int mode, int hash_kind, uint32_t chunk_size)
+    : mode_(mode), hash_kind_(hash_kind), cs_(chunk_size), leaf_tune_(default_leaf_tune(hash_kind)) {
   for (auto& e : ev_) cudaEventCreate(&e);
   cudaMallocHost(&lay_host_, sizeof(Layout));
   cudaMallocHost(&err_host_, 2 * sizeof(uint32_t));

@@ -178,7 +178,7 @@ __device__ __forceinline__ bool needs_old(const LeafArgs& a) {
 // TMA pipeline kernel.
 // ---------------------------------------------------------------------------
 template <int HK, int EPI, int W, int kRows>
-__global__ void __launch_bounds__(kRows + 32) leaf_tma_kernel(const __grid_constant__ CUtensorMap tmap, LeafArgs a,
+__global__ void __launch_bounds__(kRows + 32, 2) leaf_tma_kernel(const __grid_constant__ CUtensorMap tmap, LeafArgs a,
                                                               uint32_t n_full) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -235,13 +235,22 @@ __global__ void __launch_bounds__(kRows + 32) leaf_tma_kernel(const __grid_const
       if (!mbar_wait(&full[s], ph)) { atomicOr(a.err, DERR_SPIN); return; }
       const uint8_t* stage = smem + s * kStageBytes;
       const uint32_t rowbase = (uint32_t)tid * W;
+      // the row into registers, then the stage goes back to the producer
+      // before any hashing: the refill overlaps this thread's hash work
+      uint4 row[W / 16];
+#pragma unroll
+      for (int q = 0; q < W / 16; q++) row[q] = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + q * 16));
+      // release the stage: this thread's reads before the refill's TMA write
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
       if (HK == HASH_MD5) {
         if (W >= 64) {
 #pragma unroll
           for (int blk = 0; blk < W / 64; blk++) {
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-              uint4 v = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + blk * 64 + q * 16));
+              const uint4 v = row[blk * 4 + q];
               X[4 * q] = v.x; X[4 * q + 1] = v.y; X[4 * q + 2] = v.z; X[4 * q + 3] = v.w;
             }
             md.block(X);
@@ -251,21 +260,14 @@ __global__ void __launch_bounds__(kRows + 32) leaf_tma_kernel(const __grid_const
           for (int i = 0; i < 16; i++) X[i] = 0;
 #pragma unroll
           for (int q = 0; q < W / 16; q++) {
-            uint4 v = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + q * 16));
+            const uint4 v = row[q];
             X[4 * q] = v.x; X[4 * q + 1] = v.y; X[4 * q + 2] = v.z; X[4 * q + 3] = v.w;
           }
         }
       } else {
 #pragma unroll
-        for (int q = 0; q < W / 16; q++) {
-          uint4 v = *reinterpret_cast<const uint4*>(stage + swz<W>(rowbase + q * 16));
-          mm.block(v.x, v.y, v.z, v.w);
-        }
+        for (int q = 0; q < W / 16; q++) mm.block(row[q].x, row[q].y, row[q].z, row[q].w);
       }
-      // release the stage: this thread's reads before the refill's TMA write
-      fence_proxy_async_smem();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[s]);
     }
     Digest dg;
     if (HK == HASH_MD5) {
