@@ -1,7 +1,8 @@
 // gather_kernels.cu -- everything between the leaf kernel and the finished
 // incremental checkpoint in HBM:
-//   * Merkle forest passes, one launch per tree level (src/tree_approach.cpp
-//     :124-227 baseline, :378-477 incremental);
+//   * Merkle forest passes, several tree levels per launch (src/tree_approach.cpp
+//     :124-227 baseline, :378-477 incremental; both incremental passes in
+//     one traversal when no leaf was demoted);
 //   * deterministic compaction of region roots in the order a serial backend
 //     pushes them (replaces the atomic Vector::push, include/kokkos_vector.hpp:37-40);
 //   * diff assembly: region sizes, repeat-count table, stable sort of the

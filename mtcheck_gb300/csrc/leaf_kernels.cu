@@ -86,9 +86,12 @@ __device__ __forceinline__ void leaf_epilogue(const LeafArgs& a, bool valid, uin
 // chunk met an entry that another insert of this launch created, whose chunk
 // is checked too.
 constexpr uint32_t kCheckCreator = 1u << 31;  // chunk counts stay below 2^31
+// Every changed chunk notes itself at most once, so the notes never outnumber
+// the changed chunks (the list holds N + 1 entries).
 __device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t note) {
   const uint32_t k = atomicAdd(a.dup_count, 1u);
   if (k < a.dup_cap) a.dup_list[k] = note;
+  else atomicOr(a.err, DERR_CAPACITY);
 }
 
 // Map insert of one changed chunk (src/tree_approach.cpp:325-349,
@@ -143,8 +146,7 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
 
 // Second pass (src/tree_approach.cpp:356-369): a first occurrence that does
 // not own its digest becomes a shifted duplicate.  Only the noted chunks and
-// the creators of their entries can be such (every changed chunk when the
-// note list overflowed).
+// the creators of their entries can be such.
 __device__ __forceinline__ void demote_chunk(const LeafArgs& a, uint32_t c, const MapSlot* s, uint32_t cur) {
   if (a.labels[c] != FIRST_OCUR) return;
   const uint32_t node = a.leaf_base + c;
@@ -155,17 +157,15 @@ __device__ __forceinline__ void demote_chunk(const LeafArgs& a, uint32_t c, cons
   }
 }
 __global__ void leaf_demote_kernel(LeafArgs a) {
-  const uint32_t nd = *a.dup_count;
-  const bool all = nd > a.dup_cap;
-  const uint32_t n = all ? *a.changed_count : nd;
+  const uint32_t n = min(*a.dup_count, a.dup_cap);
   const uint32_t cur = a.sp->cur;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t e = all ? (uint32_t)i : a.dup_list[i];
+    const uint32_t e = a.dup_list[i];
     const uint32_t k = e & ~kCheckCreator;
     const uint32_t c = a.changed_list[k];
     const MapSlot* s = &a.map.slots[a.chunk_slot[k]];
     demote_chunk(a, c, s, cur);
-    if (!all && (e & kCheckCreator)) demote_chunk(a, s->first_chunk, s, cur);
+    if (e & kCheckCreator) demote_chunk(a, s->first_chunk, s, cur);
   }
 }
 

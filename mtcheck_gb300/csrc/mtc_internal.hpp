@@ -48,7 +48,7 @@ struct LeafArgs {
   uint32_t* changed_count = nullptr;
   uint32_t* demoted = nullptr;    // set to 1 when a first occurrence is demoted (tree; may be null)
   uint32_t* dup_list = nullptr;   // changed-list positions that met a duplicate inserted by the same launch
-  uint32_t* dup_count = nullptr;  // appends; above dup_cap the demote pass visits every changed chunk
+  uint32_t* dup_count = nullptr;  // appends (at most the changed chunks)
   uint32_t dup_cap = 0;
   int hash_kind = HASH_MURMUR3;
   int epi = EPI_HASH;
