@@ -71,6 +71,7 @@ int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
   auto* e = new Engine(mode, hash_kind, chunk_size);
   e->set_stream(s);
   e->set_order_after_legacy(true);
+  e->set_params_from_host(true);  // the batch's graph replays the member's sequence as captured
   engs_.push_back(e);
   streams_.push_back(s);
   joins_.push_back(j);

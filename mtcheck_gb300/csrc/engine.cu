@@ -15,6 +15,19 @@ namespace mtc {
 
 static __global__ void set_word_kernel(uint32_t* p, uint32_t v) { *p = v; }
 
+// The step values as a kernel argument, and the error word cleared: nothing
+// crosses the host link, so a large transfer already queued there (the next
+// input's upload, say) cannot delay the checkpoint -- a host-to-device copy
+// would wait behind it on the copy engine, and a kernel reading mapped host
+// memory behind it on the link.  A replayed graph gets each step's values
+// by an update of this node (Engine::replay_own).
+static __global__ void params_in_kernel(StepParams p, StepParams* dev, uint32_t* err) {
+  if (threadIdx.x == 0) {
+    *dev = p;
+    *err = 0;
+  }
+}
+
 static uint64_t next_pow2(uint64_t v) {
   uint64_t c = 1;
   while (c < v) c <<= 1;
@@ -336,14 +349,25 @@ int Engine::enqueue(const uint8_t* data, uint64_t len, bool timed) {
     if (timed) MTC_TRY(mark(3));
     return ST_OK;
   }
-  MTC_CUDA(cudaMemcpyAsync(sp_.p, sp_host_, sizeof(StepParams), cudaMemcpyHostToDevice, stream_));
-  MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
+  if (params_by_value_) {
+    static const bool reg = (register_input_kernel(reinterpret_cast<const void*>(params_in_kernel), INPUT_PARAMS), true);
+    (void)reg;
+    params_in_kernel<<<1, 32, 0, stream_>>>(*sp_host_, sp_.p, err_.p);
+    note_launch();
+    MTC_CUDA(cudaGetLastError());
+  } else {
+    // a batch member: its sequence, replayed inside the batch's graph, copies
+    // the step values staged in the pinned block
+    MTC_CUDA(cudaMemcpyAsync(sp_.p, sp_host_, sizeof(StepParams), cudaMemcpyHostToDevice, stream_));
+    MTC_CUDA(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), stream_));
+  }
   if (timed) MTC_TRY(mark(1));
   int rc = (mode_ == MODE_LIST || mode_ == MODE_BASIC) ? run_list_basic(data, len) : run_tree(data, len, baseline_path_);
   if (rc) return rc;
   if (timed) MTC_TRY(mark(2));
   MTC_CUDA(launch_assemble(gather_args(data, len), (uint64_t)N_ + 1, stream_));
   if (timed) MTC_TRY(mark(3));
+  // results by device-to-host copies: that direction has its own copy engine
   MTC_CUDA(cudaMemcpyAsync(lay_host_, lay_.p, sizeof(Layout), cudaMemcpyDeviceToHost, stream_));
   MTC_CUDA(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
   if (map_size_.p) MTC_CUDA(cudaMemcpyAsync(err_host_ + 1, map_size_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
@@ -374,6 +398,7 @@ void Engine::drop_own_graph() {
 int Engine::retarget_own(const uint8_t* data, uint64_t len) {
   for (auto& in : input_nodes_) {
     void* args[3] = {nullptr, nullptr, nullptr};
+    if (in.kind == INPUT_PARAMS) continue;
     if (in.kind == INPUT_LEAF_TMA) {
       if (!input_tmap(&tma_, data, len, cs_, leaf_tune_)) return fail(ST_ECUDA, "tensor map for the new input");
       in.tmap = tma_.map;
@@ -396,6 +421,21 @@ int Engine::retarget_own(const uint8_t* data, uint64_t len) {
     MTC_CUDA(cudaGraphExecKernelNodeSetParams(own_segs_[in.seg].exec, in.node, &q));
   }
   own_data_ = data;
+  return ST_OK;
+}
+
+// Gives the captured sequence this step's values (the argument of its first
+// kernel).
+int Engine::update_own_params() {
+  for (auto& in : input_nodes_) {
+    if (in.kind != INPUT_PARAMS) continue;
+    StepParams sp = *sp_host_;
+    void* args[3] = {&sp, &in.sp_dev, &in.err_dev};
+    cudaKernelNodeParams q = in.p;
+    q.kernelParams = args;
+    q.extra = nullptr;
+    MTC_CUDA(cudaGraphExecKernelNodeSetParams(own_segs_[in.seg].exec, in.node, &q));
+  }
   return ST_OK;
 }
 
@@ -422,9 +462,10 @@ int Engine::mark(int i) {
 }
 
 // The launch sequence of an incremental checkpoint as a few graph launches:
-// the sequence reads the step values from pinned host memory at run time, so
-// one capture serves every checkpoint until a device buffer, the input or
-// the launch shape changes (the signature).
+// each replay updates the step values (an argument of the first kernel) and,
+// for a new input buffer, the nodes that read the input, so one capture
+// serves every checkpoint until a device buffer or the launch shape changes
+// (the signature).
 int Engine::replay_own(const uint8_t* data, uint64_t len) {
   const uint64_t sig = shape_signature(data, len);
   if (!own_segs_.empty() && sig == own_sig_ && data != own_data_) MTC_TRY(retarget_own(data, len));
@@ -475,6 +516,9 @@ int Engine::replay_own(const uint8_t* data, uint64_t len) {
             std::memcpy(&in.la, in.p.kernelParams[0], sizeof(LeafArgs));
             std::memcpy(&in.u[0], in.p.kernelParams[1], sizeof(uint32_t));
             std::memcpy(&in.u[1], in.p.kernelParams[2], sizeof(uint32_t));
+          } else if (in.kind == INPUT_PARAMS) {
+            std::memcpy(&in.sp_dev, in.p.kernelParams[1], sizeof(StepParams*));
+            std::memcpy(&in.err_dev, in.p.kernelParams[2], sizeof(uint32_t*));
           } else {
             std::memcpy(&in.ga, in.p.kernelParams[0], sizeof(GatherArgs));
           }
@@ -496,6 +540,7 @@ int Engine::replay_own(const uint8_t* data, uint64_t len) {
     own_data_ = data;
     own_kernels_ = launch_count() - l0;  // counted while capturing, run by the launches below
   } else {
+    MTC_TRY(update_own_params());
     note_launch((uint32_t)own_kernels_);
   }
   for (auto& sg : own_segs_) {

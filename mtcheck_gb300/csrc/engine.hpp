@@ -116,6 +116,8 @@ class Engine {
   // signature changes (on by default; a Batch never uses it).
   void set_own_graph(bool on);
   bool own_graph() const { return own_graph_; }
+  // Batch members read their step values from the pinned block at run time.
+  void set_params_from_host(bool on) { params_by_value_ = !on; }
   bool take_stream_work() {
     const bool w = stream_work_;
     stream_work_ = false;
@@ -217,12 +219,15 @@ class Engine {
     LeafArgs la;
     uint32_t u[2];
     GatherArgs ga;
+    StepParams* sp_dev;  // INPUT_PARAMS: the kernel's pointer arguments
+    uint32_t* err_dev;
   };
   std::vector<InputNode> input_nodes_;
   const uint8_t* own_data_ = nullptr;  // input pointer the graphs currently read
   cudaStream_t cap_stream_ = nullptr;  // private stream the sequence is captured on
   uint64_t own_sig_ = 0, own_kernels_ = 0;
   int retarget_own(const uint8_t* data, uint64_t len);
+  int update_own_params();
   bool seg_capture_ = false;  // enqueue runs under a capture cut at each mark
   int seg_mark_ = -1;
   std::vector<std::pair<int, cudaGraph_t>> seg_graphs_;
@@ -248,6 +253,7 @@ class Engine {
   StepParams* sp_host_ = nullptr;   // pinned
   Layout* lay_host_ = nullptr;      // pinned
   uint32_t* err_host_ = nullptr;    // pinned [err, map size]
+  bool params_by_value_ = true;     // false for batch members (their graphs copy sp_host_)
   uint64_t diff_len_ = 0, diff_pad_ = 0;
   TmaCache tma_;
   cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

@@ -106,6 +106,7 @@ enum : int {
   INPUT_LEAF_TMA = 1,     // (const CUtensorMap, LeafArgs, uint32_t)
   INPUT_LEAF_DIRECT = 2,  // (LeafArgs, uint32_t, uint32_t)
   INPUT_GATHER = 3,       // (GatherArgs)
+  INPUT_PARAMS = 4,       // (StepParams, StepParams*, uint32_t*): the step values
 };
 void register_input_kernel(const void* func, int kind);
 int input_kernel_kind(const void* func);

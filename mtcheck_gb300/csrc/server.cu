@@ -173,6 +173,7 @@ int Server::add_process(int mode, int hash_kind, uint32_t chunk_size, uint32_t* 
   p->eng = std::make_unique<Engine>(mode, hash_kind, chunk_size);
   p->eng->set_stream(p->s);
   p->eng->set_pool(pool_);
+  p->eng->set_params_from_host(true);  // its captured graphs replay as captured
   std::lock_guard<std::mutex> g(mu_);
   procs_.push_back(std::move(p));
   *pid = (uint32_t)procs_.size() - 1;
