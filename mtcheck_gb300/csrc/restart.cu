@@ -45,18 +45,22 @@ struct RArgs {
   uint32_t cur_main;             // id of the main checkpoint
   const DiffInfo* di;
   uint32_t nfo, nsh;
+  uint32_t F0, S0;               // FO and shift entries of the main checkpoint
+  uint32_t fo_cb, sh_cb;         // first FO / shift entry of the chain (nfo / nsh without one)
+  uint64_t tag;                  // this restart's epoch << 32 (chain table cells)
   uint32_t *fo_node, *fo_seg, *fo_clen;
   uint64_t* fo_excl;
   uint32_t *sh_node, *sh_prev, *sh_tree, *sh_seg;
   uint64_t *sh_off, *sh_excl;
   uint32_t* rrs;
-  uint64_t *nl, *res, *nl_rank, *cp_rank;
+  uint64_t *nl_rank, *cp_rank;
+  uint64_t* srcp;                // per chunk: source address (TMA restore path)
+  uint32_t* nbv;                 // per chunk: bytes to copy, 0 for none
   uint32_t* fo_at;  // main checkpoint: lowest FO entry per node (tree) or chunk (list)
-  uint32_t *dm_tab, *rm_tab, *dm_mask, *rm_mask;
+  uint64_t *dm_tab, *rm_tab;     // [step][key] cells, tag | (2^32-1 - entry index)
+  uint32_t *dm_mask, *rm_mask;   // [key][step / 32] bits: the step's map holds the key
   uint64_t *dm_excl, *rm_excl;  // per-entry item prefix of the chain tables
   uint4* fo_rng;                // chain FO entries: leaf key ranges {lo0, n0, lo1, n1}
-  uint2 *bnd0, *bnd1;           // per expansion tile: first and last entry
-  uint32_t max_tiles;           // capacity of bnd0 / bnd1
   uint64_t *tot;                // [0] dm items, [1] rm items, [2] main FO chunks, [3] main shift chunks
   uint8_t* out;
   uint32_t* err;
@@ -159,10 +163,14 @@ struct StoreExcl {
   __device__ __forceinline__ void operator()(uint64_t g, uint64_t ex, uint64_t) const { out[g] = ex; }
 };
 // chunk_len of each FO entry relative to its own diff (src/tree_approach.cpp:803-816)
+// and the main checkpoint's item total (its entries lead the list, so their
+// prefix is fo_excl itself)
 __global__ void clen_kernel(RArgs a) {
   for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.nfo; g += (uint64_t)gridDim.x * blockDim.x) {
     const DiffInfo& d = a.di[a.fo_seg[g]];
     a.fo_clen[g] = (uint32_t)(a.fo_excl[g] - a.fo_excl[d.fo_begin]);
+    if (g + 1 == a.F0)
+      a.tot[2] = a.fo_excl[g] + (a.approach == APPROACH_TREE ? num_leaf_descendents(a.fo_node[g], a.M) : 1);
   }
 }
 
@@ -241,85 +249,94 @@ __device__ __forceinline__ uint32_t upper_entry(const uint64_t* excl, uint32_t n
   return lo;
 }
 
+// The same search by one whole warp: each round compares 32 evenly spaced
+// pivots and keeps the span after the last pivot not above `item`, so n
+// entries take ceil(log32 n) rounds of one load per lane (excl[0] = 0).
+__device__ __forceinline__ uint32_t warp_upper_entry(const uint64_t* excl, uint32_t n, uint64_t item) {
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const uint32_t step = (hi - lo) / 32 + 1;
+    const uint64_t p = (uint64_t)lo + (uint64_t)lane * step;
+    const bool ok = p <= hi && excl[p] <= item;
+    const uint32_t b = __ballot_sync(0xffffffffu, ok);
+    lo += (31 - __clz(b)) * step;
+    const uint64_t h2 = (uint64_t)lo + step - 1;
+    if (h2 < hi) hi = (uint32_t)h2;
+  }
+  return lo;
+}
+
 // Items numbered by an exclusive prefix over entries are processed in tiles of
-// kExpandTile per block: the entries overlapping a tile (each entry has at
-// least one item) are staged in shared memory once, and every item finds its
-// entry by a binary search there instead of in global memory.
+// kExpandTile per block: two warps find the tile's first and last entry, the
+// entries in between (each owns at least one item, or the tile falls back to
+// searches in global memory) are staged in shared memory, and every item
+// finds its entry by a binary search there.
 constexpr uint32_t kExpandTile = 2048;
 struct ExpandTile {
   uint64_t ex[kExpandTile + 1];
-  uint32_t e0, cnt;
+  uint32_t e0, e1;
 };
-// The first and last entry of every tile, for all tiles at once, written
-// from the entries' side: entry k owns items [excl[k], excl[k+1]) and records
-// itself for every tile that starts or ends inside that range.  No dependent
-// loads (a per-tile binary search would chain ~log2(n) of them).
-__global__ void expand_bounds_kernel(const uint64_t* excl, uint32_t n, const uint64_t* total, uint2* bounds,
-                                     uint32_t max_tiles) {
-  const uint64_t tot = *total;
-  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t s = excl[k], e = k + 1 < n ? excl[k + 1] : tot;
-    if (e <= s) continue;  // no items: never the owner of one
-    for (uint64_t b = s / kExpandTile; b * kExpandTile < e && b < max_tiles; b++) {
-      const uint64_t first = b * kExpandTile;
-      const uint64_t last = (first + kExpandTile < tot ? first + kExpandTile : tot) - 1;
-      if (first >= s) bounds[b].x = (uint32_t)k;
-      if (last >= s && last < e) bounds[b].y = (uint32_t)k;
-    }
-  }
-}
-
 __device__ __forceinline__ void expand_stage(ExpandTile& T, const uint64_t* excl, uint32_t n, uint64_t t0,
-                                             uint64_t t1, const uint2* bounds = nullptr,
-                                             uint32_t max_tiles = 0) {
-  if (threadIdx.x == 0) {
-    const uint64_t b = t0 / kExpandTile;  // tiles start at multiples of kExpandTile
-    uint32_t e0, e1;
-    if (bounds && b < max_tiles) {
-      const uint2 v = bounds[b];
-      e0 = v.x;
-      e1 = v.y;
-    } else {
-      e0 = upper_entry(excl, n, t0);
-      e1 = upper_entry(excl, n, t1 - 1);
-    }
-    T.e0 = e0;
-    T.cnt = e1 - e0 + 1;
+                                             uint64_t t1) {
+  const uint32_t warp = threadIdx.x >> 5;
+  if (warp < 2) {
+    const uint32_t e = warp_upper_entry(excl, n, warp == 0 ? t0 : t1 - 1);
+    if ((threadIdx.x & 31) == 0) (warp == 0 ? T.e0 : T.e1) = e;
   }
   __syncthreads();
-  const uint32_t cnt = T.cnt <= kExpandTile + 1 ? T.cnt : 0;
-  for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) T.ex[i] = excl[T.e0 + i];
+  const uint32_t cnt = T.e1 - T.e0 + 1;
+  if (cnt <= kExpandTile + 1)
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) T.ex[i] = excl[T.e0 + i];
   __syncthreads();
 }
+// entry owning `item` and the item's position within it
 __device__ __forceinline__ uint32_t expand_entry(const ExpandTile& T, const uint64_t* excl, uint32_t n,
-                                                 uint64_t item) {
-  if (T.cnt > kExpandTile + 1) return upper_entry(excl, n, item);
-  uint32_t lo = 0, hi = T.cnt - 1;
+                                                 uint64_t item, uint64_t* j) {
+  const uint32_t cnt = T.e1 - T.e0 + 1;
+  if (cnt > kExpandTile + 1) {
+    const uint32_t k = upper_entry(excl, n, item);
+    *j = item - excl[k];
+    return k;
+  }
+  uint32_t lo = 0, hi = cnt - 1;
   while (lo < hi) {
     uint32_t mid = (lo + hi + 1) >> 1;
     if (T.ex[mid] <= item) lo = mid; else hi = mid - 1;
   }
+  *j = item - T.ex[lo];
   return T.e0 + lo;
 }
 
+// Tiles of two item lists taken in one grid: list 0's tiles first.
+struct TwoLists {
+  uint64_t tot0, tot1, nt0, nt1;
+  __device__ __forceinline__ TwoLists(uint64_t a0, uint64_t a1)
+      : tot0(a0), tot1(a1), nt0((a0 + kExpandTile - 1) / kExpandTile), nt1((a1 + kExpandTile - 1) / kExpandTile) {}
+  __device__ __forceinline__ uint64_t tiles() const { return nt0 + nt1; }
+};
+
 // main scatter: which entry writes node_list / copies each chunk last
-// (src/tree_approach.cpp:825-925; ranks: FO entries 1+i, shift entries 2^32+i)
-// which = 0: FO regions (prefix fo_excl, total tot[2]); 1: shift regions
-// (prefix sh_excl, total tot[3])
-__global__ void __launch_bounds__(256) main_cover_kernel(RArgs a, int which) {
+// (src/tree_approach.cpp:825-925; ranks: FO entries 1+i, shift entries 2^32+i);
+// the FO regions (prefix fo_excl, total tot[2]) and the shift regions (prefix
+// sh_excl, total tot[3]) in one launch
+__global__ void __launch_bounds__(256) main_cover_kernel(RArgs a) {
   __shared__ ExpandTile T;
-  const DiffInfo& d = a.di[0];
-  const uint64_t total = a.tot[2 + which];
-  const uint64_t* excl = which ? a.sh_excl : a.fo_excl;
-  const uint32_t n = which ? d.S : d.F;
+  const TwoLists L(a.tot[2], a.tot[3]);
   const bool tree = a.approach == APPROACH_TREE;
-  for (uint64_t t0 = (uint64_t)blockIdx.x * kExpandTile; t0 < total; t0 += (uint64_t)gridDim.x * kExpandTile) {
+  for (uint64_t tile = blockIdx.x; tile < L.tiles(); tile += gridDim.x) {
+    const bool sh = tile >= L.nt0;
+    const uint64_t total = sh ? L.tot1 : L.tot0;
+    const uint64_t t0 = (sh ? tile - L.nt0 : tile) * kExpandTile;
     const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
-    expand_stage(T, excl, n, t0, t1, which ? a.bnd1 : a.bnd0, a.max_tiles);
+    const uint64_t* excl = sh ? a.sh_excl : a.fo_excl;
+    const uint32_t n = sh ? a.S0 : a.F0;
+    expand_stage(T, excl, n, t0, t1);
     for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-      const uint32_t i = expand_entry(T, excl, n, t);
-      const uint32_t j = (uint32_t)(t - excl[i]);
-      if (which == 0) {
+      uint64_t j64;
+      const uint32_t i = expand_entry(T, excl, n, t, &j64);
+      const uint32_t j = (uint32_t)j64;
+      if (!sh) {
         uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.fo_node[i], a.M) - (a.N - 1) + j) : a.fo_node[i];
         if (c >= a.N) continue;
         const unsigned long long r = 1ull + i;
@@ -330,53 +347,10 @@ __global__ void __launch_bounds__(256) main_cover_kernel(RArgs a, int which) {
         if (c >= a.N) continue;
         const unsigned long long r = (1ull << 32) + i;
         atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
-        if (a.sh_tree[i] == d.id) atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
+        if (a.sh_tree[i] == a.cur_main) atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
       }
     }
     __syncthreads();
-  }
-}
-
-__device__ __forceinline__ uint64_t pack_nl(uint32_t node, uint32_t tree) { return ((uint64_t)tree << 32) | node; }
-
-// node_list and first copy source of every chunk after the main checkpoint
-__global__ void main_resolve_kernel(RArgs a) {
-  const DiffInfo& d = a.di[0];
-  const uint32_t cur = d.id;
-  const bool tree = a.approach == APPROACH_TREE;
-  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.N; c += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t nr = a.nl_rank[c], cr = a.cp_rank[c];
-    uint64_t nl;
-    if (nr == 0) {
-      // "same as previous" (src/tree_approach.cpp:932-937)
-      nl = pack_nl(tree ? (uint32_t)c + a.N - 1 : (uint32_t)c, cur - 1);
-    } else if (nr < (1ull << 32)) {
-      nl = pack_nl((uint32_t)c, cur);
-    } else {
-      const uint32_t i = (uint32_t)(nr - (1ull << 32));
-      if (tree) {
-        const uint32_t j = (uint32_t)c - (leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1));
-        nl = pack_nl(leftmost_leaf(a.sh_prev[i], a.M) + j, a.sh_tree[i]);
-      } else {
-        nl = pack_nl(a.sh_prev[i], a.sh_tree[i]);
-      }
-    }
-    a.nl[c] = nl;
-    uint64_t res = kNone;
-    if (cr != 0) {
-      if (cr < (1ull << 32)) {
-        const uint32_t i = (uint32_t)(cr - 1);
-        uint64_t base = tree ? (uint64_t)a.fo_clen[i] * a.cs : (uint64_t)i * a.cs;
-        uint64_t within = tree ? (c - (leftmost_leaf(a.fo_node[i], a.M) - (a.N - 1))) * (uint64_t)a.cs : 0;
-        res = base + within;
-      } else {
-        const uint32_t i = (uint32_t)(cr - (1ull << 32));
-        uint64_t within = tree ? (c - (leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1))) * (uint64_t)a.cs : 0;
-        res = a.sh_off[i] + within;
-      }
-      if (res >= (1ull << kOffBits)) res = kNone;
-    }
-    a.res[c] = res;
   }
 }
 
@@ -410,7 +384,7 @@ __device__ __forceinline__ int fo_leaf_ranges(uint32_t u, uint32_t N, uint32_t M
 __global__ void chain_ranges_kernel(RArgs a, uint32_t n) {
   const bool tree = a.approach == APPROACH_TREE;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t g = a.di[1].fo_begin + k;  // chain entries follow the main ones
+    const uint64_t g = a.fo_cb + k;  // chain entries follow the main ones
     uint4 r = make_uint4(0, 0, 0, 0);
     if (tree) {
       uint32_t lo[2], hi[2];
@@ -428,14 +402,14 @@ __global__ void chain_ranges_kernel(RArgs a, uint32_t n) {
 struct ChainDmCount {
   RArgs a;
   __device__ __forceinline__ uint64_t operator()(uint64_t k) const {
-    const uint4 r = a.fo_rng[a.di[1].fo_begin + k];
+    const uint4 r = a.fo_rng[a.fo_cb + k];
     return (uint64_t)r.y + r.w;
   }
 };
 struct ChainRmCount {
   RArgs a;
   __device__ __forceinline__ uint64_t operator()(uint64_t k) const {
-    const uint64_t h = a.di[1].sh_begin + k;
+    const uint64_t h = a.sh_cb + k;
     if (a.approach == APPROACH_LIST) return 1;
     const uint32_t node = a.sh_node[h];
     // repeat_map keys: the root (src/tree_approach.cpp:1069) and the leaf
@@ -449,27 +423,35 @@ struct ChainRmCount {
 
 __device__ __forceinline__ uint32_t key_of_leaf(const RArgs& a, uint32_t x) { return x - (a.N - 1); }
 
-// pass 0: set the initial value of every covered table cell and its mask bit;
-// pass 1: lowest rank wins.  which = 0: distinct-map keys of the FO entries,
-// 1: repeat-map keys of the shift entries.
-__global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a, int pass, int which) {
+// Every (step, key) cell that a chain step's distinct map (FO entries) or
+// repeat map (shift entries) holds, both item lists in one launch.  A cell
+// keeps the entry that the reference inserts first (the lowest entry index;
+// shift entries as 2h for the root key, 2h+1 for the leaf keys) through an
+// atomicMax of tag | (2^32-1 - index): `tag` is this restart's epoch in the
+// high word, so a cell written by an earlier restart loses to any write of
+// this one and needs no clearing pass.  The key's mask bit for the step is
+// set beside it (masks are cleared for every restart).
+__global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a) {
   __shared__ ExpandTile T;
   if (a.nsteps == 0) return;
-  const uint64_t total = a.tot[which];
-  const uint32_t n = which ? a.nsh - a.di[1].sh_begin : a.nfo - a.di[1].fo_begin;
-  const uint64_t* excl = which ? a.rm_excl : a.dm_excl;
+  const TwoLists L(a.tot[0], a.tot[1]);
   const bool tree = a.approach == APPROACH_TREE;
-  for (uint64_t t0 = (uint64_t)blockIdx.x * kExpandTile; t0 < total; t0 += (uint64_t)gridDim.x * kExpandTile) {
+  for (uint64_t tile = blockIdx.x; tile < L.tiles(); tile += gridDim.x) {
+    const bool rm = tile >= L.nt0;
+    const uint64_t total = rm ? L.tot1 : L.tot0;
+    const uint64_t t0 = (rm ? tile - L.nt0 : tile) * kExpandTile;
     const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
-    expand_stage(T, excl, n, t0, t1, which ? a.bnd1 : a.bnd0, a.max_tiles);
+    const uint64_t* excl = rm ? a.rm_excl : a.dm_excl;
+    const uint32_t n = rm ? a.nsh - a.sh_cb : a.nfo - a.fo_cb;
+    expand_stage(T, excl, n, t0, t1);
     for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-      const uint32_t k = expand_entry(T, excl, n, t);
-      uint64_t j = t - excl[k];
-      uint32_t key, rank, s;
-      if (which == 0) {
-        const uint64_t g = a.di[1].fo_begin + k;  // chain entries follow the main ones
+      uint64_t j;
+      const uint32_t k = expand_entry(T, excl, n, t, &j);
+      uint32_t key, s, idx;
+      if (!rm) {
+        const uint32_t g = a.fo_cb + k;
         s = a.fo_seg[g] - 1;
-        rank = (uint32_t)g - a.di[1 + s].fo_begin;
+        idx = g;
         const uint4 r = a.fo_rng[g];
         if (tree) {
           const uint32_t x = j < r.y ? r.x + (uint32_t)j : r.z + (uint32_t)(j - r.y);
@@ -479,9 +461,8 @@ __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a, int pass, in
           if (key >= a.N) continue;
         }
       } else {
-        const uint64_t h = a.di[1].sh_begin + k;
+        const uint32_t h = a.sh_cb + k;
         s = a.sh_seg[h] - 1;
-        const uint32_t i = (uint32_t)h - a.di[1 + s].sh_begin;
         if (tree) {
           const uint32_t node = a.sh_node[h];
           const uint32_t len = num_leaf_descendents(node, a.M);
@@ -489,164 +470,286 @@ __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a, int pass, in
             const uint32_t x = leftmost_leaf(node, a.M) + (uint32_t)j;
             if (x < a.N - 1 || x > a.M) continue;
             key = key_of_leaf(a, x);
-            rank = 2 * i + 1;
+            idx = 2 * h + 1;
           } else {
             key = key_of_leaf(a, node);
-            rank = 2 * i;
+            idx = 2 * h;
           }
         } else {
           key = a.sh_node[h];
           if (key >= a.N) continue;
-          rank = 2 * i;
+          idx = 2 * h;
         }
       }
-      uint32_t* tab = (which ? a.rm_tab : a.dm_tab) + (uint64_t)s * a.K + key;
-      if (pass == 0) {
-        *tab = 0xffffffffu;
-        atomicOr((which ? a.rm_mask : a.dm_mask) + (uint64_t)key * a.W + (s >> 5), 1u << (s & 31));
-      } else {
-        atomicMin(tab, rank);
-      }
+      unsigned long long* cell =
+          reinterpret_cast<unsigned long long*>((rm ? a.rm_tab : a.dm_tab) + (uint64_t)s * a.K + key);
+      atomicMax(cell, a.tag | (0xffffffffull - idx));
+      atomicOr((rm ? a.rm_mask : a.dm_mask) + (uint64_t)key * a.W + (s >> 5), 1u << (s & 31));
     }
     __syncthreads();
   }
 }
 
-// offset of leaf/chunk x in step s's data through its distinct map, or kNone
-__device__ __forceinline__ uint64_t chain_dm_offset(const RArgs& a, uint32_t s, uint32_t x) {
-  const bool tree = a.approach == APPROACH_TREE;
-  uint32_t key;
-  if (tree) {
-    if (x < a.N - 1 || x > a.M) return kNone;
-    key = key_of_leaf(a, x);
-  } else {
-    if (x >= a.N) return kNone;
-    key = x;
-  }
-  if (!(a.dm_mask[(uint64_t)key * a.W + (s >> 5)] & (1u << (s & 31)))) return kNone;
-  const uint32_t i = a.dm_tab[(uint64_t)s * a.K + key];
-  if (!tree) return (uint64_t)i * a.cs;
-  const uint64_t g = a.di[1 + s].fo_begin + i;
+// entry index stored in a chain table cell
+__device__ __forceinline__ uint32_t cell_index(uint64_t v) { return 0xffffffffu - (uint32_t)v; }
+
+// offset of leaf/chunk x in step s's data through its distinct map (the
+// caller has seen the step's mask bit for x), or kNone
+__device__ __forceinline__ uint64_t chain_dm_offset(const RArgs& a, uint32_t s, uint32_t x, uint32_t key) {
+  const uint32_t g = cell_index(a.dm_tab[(uint64_t)s * a.K + key]);
+  // list and basic: one chunk per entry, fo_clen = its position in the data
+  if (a.approach != APPROACH_TREE) return (uint64_t)a.fo_clen[g] * a.cs;
   return (uint64_t)(uint32_t)(a.fo_clen[g] + x - leftmost_leaf(a.fo_node[g], a.M)) * a.cs;
 }
+__device__ __forceinline__ bool dm_has(const RArgs& a, uint32_t s, uint32_t key) {
+  return (a.dm_mask[(uint64_t)key * a.W + (s >> 5)] >> (s & 31)) & 1u;
+}
 
-// 4. per-chunk walk down the chain (src/tree_approach.cpp:1083-1118,
-//    src/list_approach.cpp:520-567, src/basic_approach.cpp:293-312)
-__global__ void walk_kernel(RArgs a) {
-  if (a.nsteps == 0) return;
-  const uint32_t id0 = a.cur_main - 1;              // id of step 0
-  const uint32_t idl = id0 - (a.nsteps - 1);       // id of the last step
+// 4. where chunk c's bytes come from: node_list and the first copy source
+//    after the main checkpoint (src/tree_approach.cpp:825-937), then the walk
+//    down the chain (src/tree_approach.cpp:1083-1118,
+//    src/list_approach.cpp:520-567, src/basic_approach.cpp:293-312).
+//    seg 0 is the main diff; off = kNone: the reference writes nothing.
+__device__ __forceinline__ void resolve_chunk(const RArgs& a, uint64_t c, uint32_t& seg, uint64_t& off) {
+  const uint32_t cur = a.cur_main;
   const bool tree = a.approach == APPROACH_TREE;
-  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.N; c += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t nl = a.nl[c];
-    uint32_t x = (uint32_t)nl, t = (uint32_t)(nl >> 32);
-    for (uint32_t hop = 0; hop <= a.nsteps + 1; hop++) {
-      if (t > id0 || t < idl) break;  // owned by the main checkpoint, or beyond the chain
-      uint32_t key;
-      if (tree) {
-        if (x < a.N - 1 || x > a.M) { atomicOr(a.err, DERR_INTERIOR); break; }
-        key = key_of_leaf(a, x);
-      } else {
-        if (x >= a.N) break;
-        key = x;
-      }
-      // next step at or below t that mentions this key
-      uint32_t s = id0 - t, found = 0xffffffffu;
-      for (uint32_t w = s >> 5; w < a.W; w++) {
-        uint32_t m = a.dm_mask[(uint64_t)key * a.W + w] | a.rm_mask[(uint64_t)key * a.W + w];
-        if (w == (s >> 5)) m &= ~0u << (s & 31);
-        if (m) { found = w * 32 + __ffs(m) - 1; break; }
-      }
-      if (found >= a.nsteps) break;  // never mentioned again: left as is
-      s = found;
-      const uint32_t ts = id0 - s;
-      const uint64_t off = chain_dm_offset(a, s, x);
-      if (off != kNone) {
-        if (off < (1ull << kOffBits)) a.res[c] = ((uint64_t)(1 + s) << kOffBits) | off;
-        break;
-      }
-      if (a.approach == APPROACH_BASIC) break;
-      const uint32_t r = a.rm_tab[(uint64_t)s * a.K + key];
-      const uint64_t h = a.di[1 + s].sh_begin + (r >> 1);
-      uint32_t pnode, ptree = a.sh_tree[h];
-      if (tree && (r & 1)) pnode = leftmost_leaf(a.sh_prev[h], a.M) + (x - leftmost_leaf(a.sh_node[h], a.M));
-      else pnode = a.sh_prev[h];
-      if (ptree == ts) {
-        const uint64_t o2 = chain_dm_offset(a, s, pnode);
-        if (o2 != kNone && o2 < (1ull << kOffBits)) a.res[c] = ((uint64_t)(1 + s) << kOffBits) | o2;
-        break;
-      }
-      x = pnode;
-      t = ptree;
+  const uint64_t nr = a.nl_rank[c], cr = a.cp_rank[c];
+  uint32_t x, t;
+  if (nr == 0) {
+    // "same as previous" (src/tree_approach.cpp:932-937)
+    x = tree ? (uint32_t)c + a.N - 1 : (uint32_t)c;
+    t = cur - 1;
+  } else if (nr < (1ull << 32)) {
+    x = (uint32_t)c;
+    t = cur;
+  } else {
+    const uint32_t i = (uint32_t)(nr - (1ull << 32));
+    if (tree) {
+      const uint32_t j = (uint32_t)c - (leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1));
+      x = leftmost_leaf(a.sh_prev[i], a.M) + j;
+    } else {
+      x = a.sh_prev[i];
     }
+    t = a.sh_tree[i];
+  }
+  seg = 0;
+  off = kNone;
+  if (cr != 0) {
+    uint64_t res;
+    if (cr < (1ull << 32)) {
+      const uint32_t i = (uint32_t)(cr - 1);
+      const uint64_t base = tree ? (uint64_t)a.fo_clen[i] * a.cs : (uint64_t)i * a.cs;
+      const uint64_t within = tree ? (c - (leftmost_leaf(a.fo_node[i], a.M) - (a.N - 1))) * (uint64_t)a.cs : 0;
+      res = base + within;
+    } else {
+      const uint32_t i = (uint32_t)(cr - (1ull << 32));
+      const uint64_t within = tree ? (c - (leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1))) * (uint64_t)a.cs : 0;
+      res = a.sh_off[i] + within;
+    }
+    if (res < (1ull << kOffBits)) off = res;
+  }
+  if (a.nsteps == 0) return;
+  const uint32_t id0 = cur - 1;                // id of step 0
+  const uint32_t idl = id0 - (a.nsteps - 1);  // id of the last step
+  for (uint32_t hop = 0; hop <= a.nsteps + 1; hop++) {
+    if (t > id0 || t < idl) break;  // owned by the main checkpoint, or beyond the chain
+    uint32_t key;
+    if (tree) {
+      if (x < a.N - 1 || x > a.M) { atomicOr(a.err, DERR_INTERIOR); break; }
+      key = key_of_leaf(a, x);
+    } else {
+      if (x >= a.N) break;
+      key = x;
+    }
+    // next step at or below t that mentions this key
+    uint32_t s = id0 - t, found = 0xffffffffu;
+    bool in_dm = false;
+    for (uint32_t w = s >> 5; w < a.W; w++) {
+      const uint32_t dmw = a.dm_mask[(uint64_t)key * a.W + w], rmw = a.rm_mask[(uint64_t)key * a.W + w];
+      uint32_t m = dmw | rmw;
+      if (w == (s >> 5)) m &= ~0u << (s & 31);
+      if (m) {
+        const uint32_t b = __ffs(m) - 1;
+        found = w * 32 + b;
+        in_dm = (dmw >> b) & 1u;
+        break;
+      }
+    }
+    if (found >= a.nsteps) break;  // never mentioned again: left as is
+    s = found;
+    const uint32_t ts = id0 - s;
+    if (in_dm) {
+      const uint64_t o = chain_dm_offset(a, s, x, key);
+      if (o < (1ull << kOffBits)) { seg = 1 + s; off = o; }
+      break;
+    }
+    if (a.approach == APPROACH_BASIC) break;
+    const uint32_t r = cell_index(a.rm_tab[(uint64_t)s * a.K + key]);
+    const uint32_t h = r >> 1;
+    uint32_t pnode;
+    const uint32_t ptree = a.sh_tree[h];
+    if (tree && (r & 1)) pnode = leftmost_leaf(a.sh_prev[h], a.M) + (x - leftmost_leaf(a.sh_node[h], a.M));
+    else pnode = a.sh_prev[h];
+    if (ptree == ts) {
+      uint32_t pkey = 0;
+      bool ok;
+      if (tree) {
+        ok = pnode >= a.N - 1 && pnode <= a.M;
+        if (ok) pkey = key_of_leaf(a, pnode);
+      } else {
+        ok = pnode < a.N;
+        pkey = pnode;
+      }
+      if (ok && dm_has(a, s, pkey)) {
+        const uint64_t o2 = chain_dm_offset(a, s, pnode, pkey);
+        if (o2 < (1ull << kOffBits)) { seg = 1 + s; off = o2; }
+      }
+      break;
+    }
+    x = pnode;
+    t = ptree;
   }
 }
 
-// 5. one copy per chunk from the diff that owns it; one thread per 16-byte
-//    unit of the output, two units in flight (chunk sizes that are not
-//    multiples of 16 go byte by byte)
-struct GatherUnit {
-  const uint8_t* src;
-  uint8_t* dst;
-  uint32_t n;  // bytes to copy, 0 for none
-};
-__device__ __forceinline__ GatherUnit gather_unit(const RArgs& a, uint64_t u, uint64_t upc, int lg) {
-  GatherUnit g{nullptr, nullptr, 0};
-  const uint64_t cs = a.cs;
-  const uint64_t c = lg >= 0 ? u >> lg : u / upc;
-  const uint64_t byte = u * 16, within = (u - c * upc) * 16;
-  const uint64_t r = a.res[c];
-  if (r == kNone) return g;
-  const DiffInfo& d = a.di[r >> kOffBits];
-  const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1)) + within;
-  uint64_t n = 16;
-  if (byte + n > a.datalen) n = a.datalen - byte;
-  if (c * cs + cs > a.datalen && within + n > a.datalen - c * cs) n = a.datalen - c * cs - within;
-  if (off >= d.len) return g;
-  if (off + n > d.len) n = d.len - off;
-  g.src = d.base + off;
-  g.dst = a.out + byte;
-  g.n = (uint32_t)n;
-  return g;
-}
-__device__ __forceinline__ void gather_copy(const GatherUnit& g, const uint4& v) {
-  if (g.n == 16 && (((uintptr_t)g.src | (uintptr_t)g.dst) & 15) == 0) {
-    *reinterpret_cast<uint4*>(g.dst) = v;
-  } else if (g.n == 16 && (((uintptr_t)g.src | (uintptr_t)g.dst) & 3) == 0) {
-    const uint32_t* s4 = reinterpret_cast<const uint32_t*>(g.src);
-    *reinterpret_cast<uint4*>(g.dst) = make_uint4(s4[0], s4[1], s4[2], s4[3]);
-  } else {
-    for (uint32_t b = 0; b < g.n; b++) g.dst[b] = g.src[b];
+// 5. Each warp copies its 32 chunks: lane q holds chunk q's source and byte
+//    count, and the warp moves the chunks' 16-byte units with every lane busy
+//    (unit f of the tile is chunk f / units-per-chunk).  A source that is not
+//    16-byte aligned (diff data sections are only 4-byte aligned) is read as
+//    aligned 16-byte words, the word after a unit taken from the next lane,
+//    and the unit is cut out with funnel shifts; every load stays inside a
+//    16-byte word holding at least one byte of the source region.
+__device__ __forceinline__ uint4 cut16(const uint4& w0, const uint4& w1, uint32_t d) {
+  uint32_t v[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+  uint32_t o[5];
+  const uint32_t sh = (d & 3) * 8;
+  switch (d >> 2) {
+    case 0: o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; o[3] = v[3]; o[4] = v[4]; break;
+    case 1: o[0] = v[1]; o[1] = v[2]; o[2] = v[3]; o[3] = v[4]; o[4] = v[5]; break;
+    case 2: o[0] = v[2]; o[1] = v[3]; o[2] = v[4]; o[3] = v[5]; o[4] = v[6]; break;
+    default: o[0] = v[3]; o[1] = v[4]; o[2] = v[5]; o[3] = v[6]; o[4] = v[7]; break;
   }
+  if (sh == 0) return make_uint4(o[0], o[1], o[2], o[3]);
+  return make_uint4(__funnelshift_r(o[0], o[1], sh), __funnelshift_r(o[1], o[2], sh), __funnelshift_r(o[2], o[3], sh),
+                    __funnelshift_r(o[3], o[4], sh));
 }
-__device__ __forceinline__ uint4 gather_load(const GatherUnit& g) {
-  if (g.n == 16 && (((uintptr_t)g.src | (uintptr_t)g.dst) & 15) == 0)
-    return __ldcs(reinterpret_cast<const uint4*>(g.src));
-  return make_uint4(0, 0, 0, 0);
-}
-__global__ void gather_kernel(RArgs a) {
-  const uint64_t cs = a.cs;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  if (cs % 16 == 0) {
-    const uint64_t units = (a.datalen + 15) / 16;
-    const uint64_t upc = cs / 16;  // units per chunk; a power of two is a shift
-    const int lg = (upc & (upc - 1)) == 0 ? __ffsll((long long)upc) - 1 : -1;
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += 2 * stride) {
-      const GatherUnit g0 = gather_unit(a, u, upc, lg);
-      const GatherUnit g1 = u + stride < units ? gather_unit(a, u + stride, upc, lg) : GatherUnit{nullptr, nullptr, 0};
-      const uint4 v0 = gather_load(g0), v1 = gather_load(g1);
-      if (g0.n) gather_copy(g0, v0);
-      if (g1.n) gather_copy(g1, v1);
+constexpr int kCopyUnroll = 4;
+__device__ __forceinline__ void copy_tile(const RArgs& a, uint64_t c0, const uint8_t* src, uint32_t nb) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t cs = a.cs;
+  const unsigned long long sp = reinterpret_cast<unsigned long long>(src);
+  uint8_t* out0 = a.out + c0 * cs;
+  if ((cs & 15) != 0 || (reinterpret_cast<uintptr_t>(a.out) & 15) != 0) {
+    // byte by byte (odd chunk sizes)
+    const uint64_t total = (uint64_t)cs * 32;
+    for (uint64_t f = lane; f < total; f += 32) {
+      const uint32_t q = (uint32_t)(f / cs), b = (uint32_t)(f - (uint64_t)q * cs);
+      const uint8_t* s = reinterpret_cast<const uint8_t*>(__shfl_sync(0xffffffffu, sp, q));
+      const uint32_t n = __shfl_sync(0xffffffffu, nb, q);
+      if (b < n) out0[(uint64_t)q * cs + b] = s[b];
     }
     return;
   }
-  for (uint64_t byte = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; byte < a.datalen; byte += stride) {
-    const uint64_t c = byte / cs, within = byte - c * cs;
-    const uint64_t r = a.res[c];
-    if (r == kNone) continue;
-    const DiffInfo& d = a.di[r >> kOffBits];
-    const uint64_t off = d.data_off + (r & ((1ull << kOffBits) - 1)) + within;
-    if (off < d.len) a.out[byte] = d.base[off];
+  const uint32_t upc = cs >> 4;
+  const int lg = (upc & (upc - 1)) == 0 ? __ffs(upc) - 1 : -1;
+  const uint64_t total = (uint64_t)upc * 32;
+  for (uint64_t f0 = 0; f0 < total; f0 += 32 * kCopyUnroll) {
+    uint4 w0[kCopyUnroll], w1[kCopyUnroll];
+    uint32_t qv[kCopyUnroll], byte[kCopyUnroll], m[kCopyUnroll], dv[kCopyUnroll];
+    bool own1[kCopyUnroll];
+#pragma unroll
+    for (int k = 0; k < kCopyUnroll; k++) {
+      const uint64_t f = f0 + (uint64_t)k * 32 + lane;
+      const bool in = f < total;
+      const uint32_t q = in ? (lg >= 0 ? (uint32_t)(f >> lg) : (uint32_t)(f / upc)) : 31;
+      const uint32_t u = in ? (uint32_t)(f - (uint64_t)q * upc) : 0;
+      const unsigned long long s = __shfl_sync(0xffffffffu, sp, q);
+      const uint32_t n = __shfl_sync(0xffffffffu, nb, q);
+      const uint32_t b = u * 16;
+      const uint32_t mm = in && b < n ? (n - b < 16 ? n - b : 16) : 0;
+      const uint32_t d = (uint32_t)(s & 15);
+      const unsigned long long A = s - d;
+      // the next unit's lane holds the following word when it is in the same
+      // chunk and live; otherwise this lane reads that word itself
+      const bool need1 = mm && d + mm > 16;
+      const bool next_live = lane < 31 && u + 1 < upc && b + 16 < n;
+      own1[k] = need1 && !next_live;
+      w0[k] = mm ? __ldcs(reinterpret_cast<const uint4*>(A + b)) : make_uint4(0, 0, 0, 0);
+      w1[k] = own1[k] ? __ldcs(reinterpret_cast<const uint4*>(A + b + 16)) : make_uint4(0, 0, 0, 0);
+      qv[k] = q;
+      byte[k] = b;
+      m[k] = mm;
+      dv[k] = d;
+    }
+#pragma unroll
+    for (int k = 0; k < kCopyUnroll; k++) {
+      uint4 nx;
+      nx.x = __shfl_down_sync(0xffffffffu, w0[k].x, 1);
+      nx.y = __shfl_down_sync(0xffffffffu, w0[k].y, 1);
+      nx.z = __shfl_down_sync(0xffffffffu, w0[k].z, 1);
+      nx.w = __shfl_down_sync(0xffffffffu, w0[k].w, 1);
+      if (!m[k]) continue;
+      const uint4 v = dv[k] == 0 ? w0[k] : cut16(w0[k], own1[k] ? w1[k] : nx, dv[k]);
+      uint8_t* dst = out0 + (uint64_t)qv[k] * cs + byte[k];
+      if (m[k] == 16) {
+        *reinterpret_cast<uint4*>(dst) = v;
+      } else {
+        for (uint32_t i = 0; i < m[k]; i++) {
+          const uint32_t w = i < 4 ? v.x : i < 8 ? v.y : i < 12 ? v.z : v.w;
+          dst[i] = (uint8_t)(w >> ((i & 3) * 8));
+        }
+      }
+    }
+  }
+}
+
+// Where chunk c of a tile comes from: a source address and byte count (0:
+// the chunk is not written).
+__device__ __forceinline__ void chunk_source(const RArgs& a, uint64_t c, const uint8_t*& src, uint32_t& nb) {
+  src = nullptr;
+  nb = 0;
+  if (c >= a.N) return;
+  uint32_t seg;
+  uint64_t off;
+  resolve_chunk(a, c, seg, off);
+  if (off == kNone) return;
+  const DiffInfo& d = a.di[seg];
+  const uint64_t o = d.data_off + off;
+  if (o >= d.len) return;
+  uint64_t n = a.cs;
+  const uint64_t left = a.datalen - c * a.cs;
+  if (n > left) n = left;
+  if (n > d.len - o) n = d.len - o;
+  src = d.base + o;
+  nb = (uint32_t)n;
+}
+
+// 4. Every chunk's source address and byte count, in a pass of its own: the
+// walks' dependent loads want all the warps an SM can hold, the copy wants
+// bytes in flight per warp.
+__global__ void __launch_bounds__(256, 8) resolve_kernel(RArgs a) {
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.N; c += (uint64_t)gridDim.x * blockDim.x) {
+    const uint8_t* src;
+    uint32_t nb;
+    chunk_source(a, c, src, nb);
+    a.srcp[c] = reinterpret_cast<uint64_t>(src);
+    a.nbv[c] = nb;
+  }
+}
+
+// 5. Each warp copies 32 consecutive chunks from the sources resolved above.
+__global__ void __launch_bounds__(256, 3) restore_copy_kernel(RArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  const uint64_t tiles = ((uint64_t)a.N + 31) / 32;
+  for (uint64_t wt = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wt < tiles; wt += warps) {
+    const uint64_t c = wt * 32 + lane;
+    const uint8_t* src = nullptr;
+    uint32_t nb = 0;
+    if (c < a.N) {
+      src = reinterpret_cast<const uint8_t*>(a.srcp[c]);
+      nb = a.nbv[c];
+    }
+    copy_tile(a, wt * 32, src, nb);
   }
 }
 
@@ -663,11 +766,15 @@ inline uint32_t gsz(uint64_t n, int threads = 256, int per_sm = 8) {
 // Restart scratch owned by the engine between calls.
 struct RestartScratch {
   DevBuf<DiffInfo> di;
-  DevBuf<uint32_t> fo_node, fo_seg, fo_clen, sh_node, sh_prev, sh_tree, sh_seg, rrs, fo_at, dm_tab, rm_tab, dm_mask,
-      rm_mask;
-  DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl, res, nl_rank, cp_rank, dm_excl, rm_excl, tot, scan, scan_total;
+  DevBuf<uint32_t> fo_node, fo_seg, fo_clen, sh_node, sh_prev, sh_tree, sh_seg, rrs, fo_at, dm_mask, rm_mask;
+  DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl_rank, cp_rank, dm_excl, rm_excl, tot, scan, scan_total, dm_tab, rm_tab,
+      srcp;
+  DevBuf<uint32_t> nbv;
   DevBuf<uint4> fo_rng;
-  DevBuf<uint2> bnd0, bnd1;
+  // chain table epochs: cells hold the epoch of the restart that wrote them;
+  // the tables are zeroed when they are (re)allocated or the epoch wraps
+  uint32_t epoch = 0;
+  const void* tabs_seen[2] = {nullptr, nullptr};
 };
 
 void destroy_restart_scratch(RestartScratch* r) { delete r; }
@@ -675,14 +782,13 @@ void destroy_restart_scratch(RestartScratch* r) { delete r; }
 static void set_scratch_pool(RestartScratch* r, cudaMemPool_t pool) {
   r->di.pool = pool;
   r->fo_rng.pool = pool;
-  r->bnd0.pool = pool;
-  r->bnd1.pool = pool;
   for (auto* b : {&r->fo_node, &r->fo_seg, &r->fo_clen, &r->sh_node, &r->sh_prev, &r->sh_tree, &r->sh_seg, &r->rrs,
-                  &r->fo_at, &r->dm_tab, &r->rm_tab, &r->dm_mask, &r->rm_mask})
+                  &r->fo_at, &r->dm_mask, &r->rm_mask})
     b->pool = pool;
-  for (auto* b : {&r->fo_excl, &r->sh_off, &r->sh_excl, &r->nl, &r->res, &r->nl_rank, &r->cp_rank, &r->dm_excl,
-                  &r->rm_excl, &r->tot, &r->scan, &r->scan_total})
+  for (auto* b : {&r->fo_excl, &r->sh_off, &r->sh_excl, &r->nl_rank, &r->cp_rank, &r->dm_excl, &r->rm_excl, &r->tot,
+                  &r->scan, &r->scan_total, &r->dm_tab, &r->rm_tab, &r->srcp})
     b->pool = pool;
+  r->nbv.pool = pool;
 }
 
 int Engine::restart(uint8_t* dev_out, uint64_t len, const std::vector<const uint8_t*>& dev_diffs,
@@ -786,11 +892,6 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(R.fo_node.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_seg.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_rng.ensure(nfo + 1, s));
-  // expansion tiles: a chain step covers at most every leaf of its tree twice
-  const uint64_t max_items = (uint64_t)(nsteps + 2) * 2ull * M + nfo + nsh + 16;
-  const uint32_t max_tiles = (uint32_t)std::min<uint64_t>(max_items / kExpandTile + 2, 1u << 26);
-  MTC_CUDA_R(R.bnd0.ensure(max_tiles, s));
-  MTC_CUDA_R(R.bnd1.ensure(max_tiles, s));
   MTC_CUDA_R(R.fo_clen.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_excl.ensure(nfo + 1, s));
   MTC_CUDA_R(R.sh_node.ensure(nsh + 1, s));
@@ -800,16 +901,24 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(R.sh_off.ensure(nsh + 1, s));
   MTC_CUDA_R(R.sh_excl.ensure(nsh + 1, s));
   MTC_CUDA_R(R.rrs.ensure(nrrs + 1, s));
-  MTC_CUDA_R(R.nl.ensure(N, s));
-  MTC_CUDA_R(R.res.ensure(N, s));
   MTC_CUDA_R(R.nl_rank.ensure(N, s));
   MTC_CUDA_R(R.cp_rank.ensure(N, s));
+  MTC_CUDA_R(R.srcp.ensure(N, s));
+  MTC_CUDA_R(R.nbv.ensure(N, s));
   MTC_CUDA_R(R.fo_at.ensure((size_t)M + 2, s));
   MTC_CUDA_R(R.dm_excl.ensure(nfo + 1, s));
   MTC_CUDA_R(R.rm_excl.ensure(nsh + 1, s));
   MTC_CUDA_R(R.tot.ensure(4, s));
   MTC_CUDA_R(R.dm_tab.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
   MTC_CUDA_R(R.rm_tab.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
+  if (R.dm_tab.p != R.tabs_seen[0] || R.rm_tab.p != R.tabs_seen[1] || R.epoch == 0xffffffffu) {
+    MTC_CUDA_R(cudaMemsetAsync(R.dm_tab.p, 0, sizeof(uint64_t) * R.dm_tab.n, s));
+    MTC_CUDA_R(cudaMemsetAsync(R.rm_tab.p, 0, sizeof(uint64_t) * R.rm_tab.n, s));
+    R.tabs_seen[0] = R.dm_tab.p;
+    R.tabs_seen[1] = R.rm_tab.p;
+    R.epoch = 0;
+  }
+  R.epoch++;
   MTC_CUDA_R(R.dm_mask.ensure((size_t)K * W, s));
   MTC_CUDA_R(R.rm_mask.ensure((size_t)K * W, s));
   const uint64_t scan_n = std::max<uint64_t>(nfo, nsh) + 1;
@@ -824,27 +933,31 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   a.ndiff = (uint32_t)di.size(); a.nsteps = nsteps; a.W = W; a.K = K; a.cur_main = H.chkpt_id;
   a.di = R.di.p;
   a.nfo = nfo; a.nsh = nsh;
+  a.F0 = di[0].F; a.S0 = di[0].S;
+  a.fo_cb = di.size() > 1 ? di[1].fo_begin : nfo;
+  a.sh_cb = di.size() > 1 ? di[1].sh_begin : nsh;
+  a.tag = (uint64_t)R.epoch << 32;
   a.fo_node = R.fo_node.p; a.fo_seg = R.fo_seg.p; a.fo_clen = R.fo_clen.p; a.fo_excl = R.fo_excl.p;
   a.sh_node = R.sh_node.p; a.sh_prev = R.sh_prev.p; a.sh_tree = R.sh_tree.p; a.sh_seg = R.sh_seg.p;
   a.sh_off = R.sh_off.p; a.sh_excl = R.sh_excl.p;
   a.rrs = R.rrs.p;
-  a.nl = R.nl.p; a.res = R.res.p; a.nl_rank = R.nl_rank.p; a.cp_rank = R.cp_rank.p;
+  a.nl_rank = R.nl_rank.p; a.cp_rank = R.cp_rank.p;
+  a.srcp = R.srcp.p; a.nbv = R.nbv.p;
   a.fo_at = R.fo_at.p;
   a.dm_tab = R.dm_tab.p; a.rm_tab = R.rm_tab.p; a.dm_mask = R.dm_mask.p; a.rm_mask = R.rm_mask.p;
   a.dm_excl = R.dm_excl.p; a.rm_excl = R.rm_excl.p; a.tot = R.tot.p;
   a.fo_rng = R.fo_rng.p;
-  a.bnd0 = R.bnd0.p;
-  a.bnd1 = R.bnd1.p;
-  a.max_tiles = max_tiles;
   a.out = dev_out; a.err = err_.p;
   const bool tree = approach == APPROACH_TREE;
 
   // 1-3: decode entries, repeat tables, source checkpoints
+  MTC_CUDA_R(cudaMemsetAsync(R.tot.p, 0, sizeof(uint64_t) * 4, s));
   if (nfo + nsh) { load_entries_kernel<<<gsz((uint64_t)nfo + nsh), 256, 0, s>>>(a); note_launch(); }
   rrs_kernel<<<gsz(di.size(), 1, 4), 256, 0, s>>>(a);
   note_launch();
   if (nsh) { shift_tree_kernel<<<gsz(nsh), 256, 0, s>>>(a); note_launch(); }
-  // chunk_len of every FO entry within its own diff
+  // chunk_len of every FO entry within its own diff; the main checkpoint's
+  // FO items (tot[2])
   if (nfo) {
     MTC_CUDA_R(grid_scan(FoLen{R.fo_node.p, M, tree ? 1 : 0}, StoreExcl{R.fo_excl.p}, nullptr, nfo, R.scan.p,
                          R.scan_total.p, s));
@@ -856,61 +969,36 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(cudaMemsetAsync(R.nl_rank.p, 0, sizeof(uint64_t) * N, s));
   MTC_CUDA_R(cudaMemsetAsync(R.cp_rank.p, 0, sizeof(uint64_t) * N, s));
   if (di[0].F) { fo_at_kernel<<<gsz(di[0].F), 256, 0, s>>>(a); note_launch(); }
-  if (di[0].S) { main_shift_kernel<<<gsz(di[0].S), 256, 0, s>>>(a); note_launch(); }
-  // items of the main scatter: FO regions (prefix = chunk_len), shift regions
-  MTC_CUDA_R(cudaMemsetAsync(R.tot.p, 0, sizeof(uint64_t) * 4, s));
-  if (di[0].F) {
-    MTC_CUDA_R(grid_scan(FoLen{R.fo_node.p, M, tree ? 1 : 0}, StoreExcl{R.fo_excl.p}, nullptr, di[0].F, R.scan.p,
-                         R.tot.p + 2, s));
-  }
   if (di[0].S) {
+    main_shift_kernel<<<gsz(di[0].S), 256, 0, s>>>(a);
+    note_launch();
+    // items of the main shift regions
     MTC_CUDA_R(grid_scan(MainShiftLen{R.sh_prev.p, M, tree ? 1 : 0}, StoreExcl{R.sh_excl.p}, nullptr, di[0].S,
                          R.scan.p, R.tot.p + 3, s));
   }
-  if (di[0].F) {
-    expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.fo_excl.p, di[0].F, R.tot.p + 2, R.bnd0.p, a.max_tiles);
+  if (di[0].F || di[0].S) {
+    main_cover_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
     note_launch();
   }
-  if (di[0].S) {
-    expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.sh_excl.p, di[0].S, R.tot.p + 3, R.bnd1.p, a.max_tiles);
-    note_launch();
-  }
-  main_cover_kernel<<<num_sms() * 4, 256, 0, s>>>(a, 0);
-  main_cover_kernel<<<num_sms() * 4, 256, 0, s>>>(a, 1);
-  main_resolve_kernel<<<gsz(N), 256, 0, s>>>(a);
-  note_launch(3);
   // chain
   if (nsteps) {
     MTC_CUDA_R(cudaMemsetAsync(R.dm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
     MTC_CUDA_R(cudaMemsetAsync(R.rm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
-    const uint32_t nfo_chain = nfo - di[1].fo_begin, nsh_chain = nsh - di[1].sh_begin;
+    const uint32_t nfo_chain = nfo - a.fo_cb, nsh_chain = nsh - a.sh_cb;
     if (nfo_chain) {
       chain_ranges_kernel<<<gsz(nfo_chain), 256, 0, s>>>(a, nfo_chain);
       note_launch();
-    }
-    if (nfo_chain)
       MTC_CUDA_R(grid_scan(ChainDmCount{a}, StoreExcl{R.dm_excl.p}, nullptr, nfo_chain, R.scan.p, R.tot.p + 0, s));
+    }
     if (nsh_chain && !basic)
       MTC_CUDA_R(grid_scan(ChainRmCount{a}, StoreExcl{R.rm_excl.p}, nullptr, nsh_chain, R.scan.p, R.tot.p + 1, s));
-    if (nfo_chain) {
-      expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.dm_excl.p, nfo_chain, R.tot.p + 0, R.bnd0.p,
-                                                         a.max_tiles);
-      note_launch();
-    }
-    if (nsh_chain && !basic) {
-      expand_bounds_kernel<<<num_sms() * 2, 256, 0, s>>>(R.rm_excl.p, nsh_chain, R.tot.p + 1, R.bnd1.p,
-                                                         a.max_tiles);
-      note_launch();
-    }
-    // per table: every cell initialised (pass 0) before the lowest rank wins (pass 1)
-    for (int which = 0; which < 2; which++)
-      for (int pass = 0; pass < 2; pass++)
-        chain_tables_kernel<<<num_sms() * 4, 256, 0, s>>>(a, pass, which);
-    walk_kernel<<<gsz(N), 256, 0, s>>>(a);
-    note_launch(5);
+    chain_tables_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
+    note_launch();
   }
-  gather_kernel<<<num_sms() * 16, 256, 0, s>>>(a);
-  note_launch();
+  // 4: every chunk's source; 5: the copy
+  resolve_kernel<<<gsz(N), 256, 0, s>>>(a);
+  restore_copy_kernel<<<num_sms() * 3, 256, 0, s>>>(a);
+  note_launch(2);
   cudaEventRecord(e1, s);
   MTC_CUDA_R(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   return ST_OK;

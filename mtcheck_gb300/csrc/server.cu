@@ -321,7 +321,7 @@ uint64_t Server::need_bytes(const Req& r, const Proc& p) const {
   } else {
     for (uint32_t k = 0; k <= r.chkpt_id && k < p.chain.size(); k++)
       if (!p.chain[k].dev) need += p.chain[k].len;  // staged back for the restart
-    need += N * 96 + (uint64_t)(r.chkpt_id + 1) * (N + 1) * 8;  // restart scratch
+    need += N * 96 + (uint64_t)(r.chkpt_id + 1) * (N + 1) * 16;  // restart scratch (64-bit table cells)
   }
   return need;
 }

@@ -119,3 +119,35 @@ def test_corrupt_checkpoints_are_rejected(cuda, mtc):
     # the handle keeps working after an error
     gpu.restart(out, diffs, 2)
     assert np.array_equal(out.cpu().numpy(), seq[2])
+
+
+@pytest.mark.parametrize("approach", [3, 4], ids=["list", "tree"])
+def test_long_chain_restart(cuda, mtc, oracle, approach):
+    # 40 checkpoints: the per-key step masks of the chain span two words
+    nbytes, cs = (1 << 17) + 77, 128
+    seq = series(2, nbytes, cs, 40, seed=21)
+    gpu, diffs = chain(cuda, mtc, approach, 0, seq, cs)
+    for i in (39, 33, 32, 31, 5):
+        want = oracle_restart(oracle, approach, diffs, i, nbytes)
+        out = cuda.full((nbytes,), FILL, dtype=cuda.uint8, device="cuda")
+        gpu.restart(out, diffs, i)
+        assert np.array_equal(out.cpu().numpy(), want), i
+
+
+def test_restart_handle_reused_across_chains(cuda, mtc, oracle):
+    # one restarting handle alternates between chains of different lengths and
+    # buffer sizes (its chain tables keep cells of earlier restarts), and
+    # writes into an output that is not 16-byte aligned
+    cs = 128
+    sa, sb = series(2, 1 << 18, cs, 6, seed=31), series(1, (1 << 17) + 77, cs, 4, seed=32)
+    _, da = chain(cuda, mtc, 4, 0, sa, cs)
+    _, db = chain(cuda, mtc, 4, 0, sb, cs)
+    r = mtc.TreeDeduplicator(cs)
+    for seqs, diffs, i in ((sa, da, 5), (sb, db, 3), (sa, da, 2), (sb, db, 1), (sa, da, 5)):
+        n = len(seqs[0])
+        want = oracle_restart(oracle, 4, diffs, i, n)
+        buf = cuda.full((n + 16,), FILL, dtype=cuda.uint8, device="cuda")
+        for view in (buf[:n], buf[3:3 + n]):
+            view.fill_(FILL)
+            r.restart(view, diffs, i)
+            assert np.array_equal(view.cpu().numpy(), want), (n, i, view.data_ptr() % 16)
