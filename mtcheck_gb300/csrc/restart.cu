@@ -53,15 +53,16 @@ struct RArgs {
   uint32_t *sh_node, *sh_prev, *sh_tree, *sh_seg;
   uint64_t *sh_off, *sh_excl;
   uint32_t* rrs;
-  uint64_t *nl_rank, *cp_rank;
+  uint64_t *nl_rank, *cp_rank;  // main scatter ranks, tagged: ntag | rank (older tags read as 0)
+  uint64_t ntag;                 // this restart's epoch << 34
   uint64_t* srcp;                // per chunk: source address (TMA restore path)
   uint32_t* nbv;                 // per chunk: bytes to copy, 0 for none
   uint32_t* fo_at;  // main checkpoint: lowest FO entry per node (tree) or chunk (list)
   uint64_t *dm_tab, *rm_tab;     // [step][key] cells, tag | (2^32-1 - entry index)
   uint32_t *dm_mask, *rm_mask;   // [key][step / 32] bits: the step's map holds the key
-  uint64_t *dm_excl, *rm_excl;  // per-entry item prefix of the chain tables
+  uint64_t* dm_excl;            // per chain FO entry: item prefix of the distinct-map table
   uint4* fo_rng;                // chain FO entries: leaf key ranges {lo0, n0, lo1, n1}
-  uint64_t *tot;                // [0] dm items, [1] rm items, [2] main FO chunks, [3] main shift chunks
+  uint64_t *tot;                // [0] dm items, [2] main FO chunks, [3] main shift chunks, [4] [3] + rm items
   uint8_t* out;
   uint32_t* err;
 };
@@ -115,21 +116,40 @@ __global__ void load_entries_kernel(RArgs a) {
 // 2. inclusive prefix of the repeat-count table of every diff over ids 0..id
 //    (src/tree_approach.cpp:868-883); a table naming an id above the diff's
 //    own id is corrupt
+//    The (checkpoint, count) pairs are read by the whole block and applied in
+//    table order by one thread (a repeated checkpoint keeps its last count);
+//    the prefix is a block scan (modulo 2^32, as the reference's uint32 sum).
 __global__ void rrs_kernel(RArgs a) {
+  __shared__ uint2 pairs[256];
+  __shared__ uint64_t sh[33];
   for (uint32_t s = blockIdx.x; s < a.ndiff; s += gridDim.x) {
     const DiffInfo& d = a.di[s];
     uint32_t* r = a.rrs + d.rrs_begin;
     for (uint32_t j = threadIdx.x; j <= d.id; j += blockDim.x) r[j] = 0;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      for (uint32_t i = 0; i < d.P; i++) {
-        uint32_t ck = rd32(d.base + d.cnt_off + 8ull * i);
-        uint32_t n = rd32(d.base + d.cnt_off + 8ull * i + 4);
-        if (ck > d.id) { atomicOr(a.err, DERR_RANGE); continue; }
-        r[ck] = n;
+    for (uint32_t i0 = 0; i0 < d.P; i0 += blockDim.x) {
+      const uint32_t i = i0 + threadIdx.x;
+      if (i < d.P && threadIdx.x < 256)
+        pairs[threadIdx.x] = make_uint2(rd32(d.base + d.cnt_off + 8ull * i), rd32(d.base + d.cnt_off + 8ull * i + 4));
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const uint32_t m = d.P - i0 < blockDim.x ? d.P - i0 : blockDim.x;
+        for (uint32_t k = 0; k < m; k++) {
+          const uint2 p = pairs[k];
+          if (p.x > d.id) { atomicOr(a.err, DERR_RANGE); continue; }
+          r[p.x] = p.y;
+        }
       }
-      uint32_t acc = 0;
-      for (uint32_t j = 0; j <= d.id; j++) { acc += r[j]; r[j] = acc; }
+      __syncthreads();
+    }
+    uint64_t carry = 0;
+    for (uint32_t j0 = 0; j0 <= d.id; j0 += blockDim.x) {
+      const uint32_t j = j0 + threadIdx.x;
+      const uint64_t v = j <= d.id ? r[j] : 0;
+      uint64_t tot;
+      const uint64_t ex = block_excl_scan(v, sh, &tot);
+      if (j <= d.id) r[j] = (uint32_t)(carry + ex + v);
+      carry += tot;
     }
     __syncthreads();
   }
@@ -231,14 +251,6 @@ __global__ void main_shift_kernel(RArgs a) {
     a.sh_off[i] = off;
   }
 }
-// chunks touched by a main shift entry (tree: num_leaf_descendents(prev))
-struct MainShiftLen {
-  const uint32_t* prev;
-  uint32_t M;
-  int tree;
-  __device__ __forceinline__ uint64_t operator()(uint64_t i) const { return tree ? num_leaf_descendents(prev[i], M) : 1; }
-};
-
 __device__ __forceinline__ uint32_t upper_entry(const uint64_t* excl, uint32_t n, uint64_t item) {
   // last entry e with excl[e] <= item
   uint32_t lo = 0, hi = n - 1;
@@ -339,13 +351,13 @@ __global__ void __launch_bounds__(256) main_cover_kernel(RArgs a) {
       if (!sh) {
         uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.fo_node[i], a.M) - (a.N - 1) + j) : a.fo_node[i];
         if (c >= a.N) continue;
-        const unsigned long long r = 1ull + i;
+        const unsigned long long r = a.ntag | (1ull + i);
         atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
         atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
       } else {
         uint64_t c = tree ? (uint64_t)(uint32_t)(leftmost_leaf(a.sh_node[i], a.M) - (a.N - 1) + j) : a.sh_node[i];
         if (c >= a.N) continue;
-        const unsigned long long r = (1ull << 32) + i;
+        const unsigned long long r = a.ntag | ((1ull << 32) + i);
         atomicMax(reinterpret_cast<unsigned long long*>(&a.nl_rank[c]), r);
         if (a.sh_tree[i] == a.cur_main) atomicMax(reinterpret_cast<unsigned long long*>(&a.cp_rank[c]), r);
       }
@@ -421,6 +433,25 @@ struct ChainRmCount {
   }
 };
 
+// Items of every shift entry in one scan: the main checkpoint's regions
+// (num_leaf_descendents(prev) chunks each), then the chain entries' repeat-map
+// keys.  The main total goes to tot[3], the grand total to tot[4]; the chain
+// items are numbered from tot[3] on.
+struct ShiftItems {
+  RArgs a;
+  __device__ __forceinline__ uint64_t operator()(uint64_t h) const {
+    if (h < a.S0) return a.approach == APPROACH_TREE ? num_leaf_descendents(a.sh_prev[h], a.M) : 1;
+    return ChainRmCount{a}(h - a.sh_cb);
+  }
+};
+struct StoreShiftExcl {
+  RArgs a;
+  __device__ __forceinline__ void operator()(uint64_t h, uint64_t ex, uint64_t v) const {
+    a.sh_excl[h] = ex;
+    if (h + 1 == a.S0) a.tot[3] = ex + v;
+  }
+};
+
 __device__ __forceinline__ uint32_t key_of_leaf(const RArgs& a, uint32_t x) { return x - (a.N - 1); }
 
 // Every (step, key) cell that a chain step's distinct map (FO entries) or
@@ -434,19 +465,20 @@ __device__ __forceinline__ uint32_t key_of_leaf(const RArgs& a, uint32_t x) { re
 __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a) {
   __shared__ ExpandTile T;
   if (a.nsteps == 0) return;
-  const TwoLists L(a.tot[0], a.tot[1]);
+  const uint64_t rbase = a.tot[3];  // repeat-map items are numbered from here
+  const TwoLists L(a.tot[0], a.tot[4] - rbase);
   const bool tree = a.approach == APPROACH_TREE;
   for (uint64_t tile = blockIdx.x; tile < L.tiles(); tile += gridDim.x) {
     const bool rm = tile >= L.nt0;
-    const uint64_t total = rm ? L.tot1 : L.tot0;
+    const uint64_t total = rm ? L.tot1 : L.tot0, base = rm ? rbase : 0;
     const uint64_t t0 = (rm ? tile - L.nt0 : tile) * kExpandTile;
     const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
-    const uint64_t* excl = rm ? a.rm_excl : a.dm_excl;
+    const uint64_t* excl = rm ? a.sh_excl + a.sh_cb : a.dm_excl;
     const uint32_t n = rm ? a.nsh - a.sh_cb : a.nfo - a.fo_cb;
-    expand_stage(T, excl, n, t0, t1);
+    expand_stage(T, excl, n, base + t0, base + t1);
     for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
       uint64_t j;
-      const uint32_t k = expand_entry(T, excl, n, t, &j);
+      const uint32_t k = expand_entry(T, excl, n, base + t, &j);
       uint32_t key, s, idx;
       if (!rm) {
         const uint32_t g = a.fo_cb + k;
@@ -513,7 +545,8 @@ __device__ __forceinline__ bool dm_has(const RArgs& a, uint32_t s, uint32_t key)
 __device__ __forceinline__ void resolve_chunk(const RArgs& a, uint64_t c, uint32_t& seg, uint64_t& off) {
   const uint32_t cur = a.cur_main;
   const bool tree = a.approach == APPROACH_TREE;
-  const uint64_t nr = a.nl_rank[c], cr = a.cp_rank[c];
+  const uint64_t nr0 = a.nl_rank[c], cr0 = a.cp_rank[c];
+  const uint64_t nr = nr0 >= a.ntag ? nr0 - a.ntag : 0, cr = cr0 >= a.ntag ? cr0 - a.ntag : 0;
   uint32_t x, t;
   if (nr == 0) {
     // "same as previous" (src/tree_approach.cpp:932-937)
@@ -767,14 +800,15 @@ inline uint32_t gsz(uint64_t n, int threads = 256, int per_sm = 8) {
 struct RestartScratch {
   DevBuf<DiffInfo> di;
   DevBuf<uint32_t> fo_node, fo_seg, fo_clen, sh_node, sh_prev, sh_tree, sh_seg, rrs, fo_at, dm_mask, rm_mask;
-  DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl_rank, cp_rank, dm_excl, rm_excl, tot, scan, scan_total, dm_tab, rm_tab,
+  DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl_rank, cp_rank, dm_excl, tot, scan, scan_total, dm_tab, rm_tab,
       srcp;
   DevBuf<uint32_t> nbv;
   DevBuf<uint4> fo_rng;
-  // chain table epochs: cells hold the epoch of the restart that wrote them;
-  // the tables are zeroed when they are (re)allocated or the epoch wraps
+  // epochs: chain table cells and the main scatter ranks hold the epoch of
+  // the restart that wrote them; the four buffers are zeroed when one of them
+  // is (re)allocated or the epoch reaches 2^30
   uint32_t epoch = 0;
-  const void* tabs_seen[2] = {nullptr, nullptr};
+  const void* seen[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 void destroy_restart_scratch(RestartScratch* r) { delete r; }
@@ -785,7 +819,7 @@ static void set_scratch_pool(RestartScratch* r, cudaMemPool_t pool) {
   for (auto* b : {&r->fo_node, &r->fo_seg, &r->fo_clen, &r->sh_node, &r->sh_prev, &r->sh_tree, &r->sh_seg, &r->rrs,
                   &r->fo_at, &r->dm_mask, &r->rm_mask})
     b->pool = pool;
-  for (auto* b : {&r->fo_excl, &r->sh_off, &r->sh_excl, &r->nl_rank, &r->cp_rank, &r->dm_excl, &r->rm_excl, &r->tot,
+  for (auto* b : {&r->fo_excl, &r->sh_off, &r->sh_excl, &r->nl_rank, &r->cp_rank, &r->dm_excl, &r->tot,
                   &r->scan, &r->scan_total, &r->dm_tab, &r->rm_tab, &r->srcp})
     b->pool = pool;
   r->nbv.pool = pool;
@@ -907,15 +941,19 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(R.nbv.ensure(N, s));
   MTC_CUDA_R(R.fo_at.ensure((size_t)M + 2, s));
   MTC_CUDA_R(R.dm_excl.ensure(nfo + 1, s));
-  MTC_CUDA_R(R.rm_excl.ensure(nsh + 1, s));
-  MTC_CUDA_R(R.tot.ensure(4, s));
+  MTC_CUDA_R(R.tot.ensure(5, s));
   MTC_CUDA_R(R.dm_tab.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
   MTC_CUDA_R(R.rm_tab.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
-  if (R.dm_tab.p != R.tabs_seen[0] || R.rm_tab.p != R.tabs_seen[1] || R.epoch == 0xffffffffu) {
+  if (R.dm_tab.p != R.seen[0] || R.rm_tab.p != R.seen[1] || R.nl_rank.p != R.seen[2] || R.cp_rank.p != R.seen[3] ||
+      R.epoch >= (1u << 30) - 1) {
     MTC_CUDA_R(cudaMemsetAsync(R.dm_tab.p, 0, sizeof(uint64_t) * R.dm_tab.n, s));
     MTC_CUDA_R(cudaMemsetAsync(R.rm_tab.p, 0, sizeof(uint64_t) * R.rm_tab.n, s));
-    R.tabs_seen[0] = R.dm_tab.p;
-    R.tabs_seen[1] = R.rm_tab.p;
+    MTC_CUDA_R(cudaMemsetAsync(R.nl_rank.p, 0, sizeof(uint64_t) * R.nl_rank.n, s));
+    MTC_CUDA_R(cudaMemsetAsync(R.cp_rank.p, 0, sizeof(uint64_t) * R.cp_rank.n, s));
+    R.seen[0] = R.dm_tab.p;
+    R.seen[1] = R.rm_tab.p;
+    R.seen[2] = R.nl_rank.p;
+    R.seen[3] = R.cp_rank.p;
     R.epoch = 0;
   }
   R.epoch++;
@@ -937,6 +975,7 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   a.fo_cb = di.size() > 1 ? di[1].fo_begin : nfo;
   a.sh_cb = di.size() > 1 ? di[1].sh_begin : nsh;
   a.tag = (uint64_t)R.epoch << 32;
+  a.ntag = (uint64_t)R.epoch << 34;
   a.fo_node = R.fo_node.p; a.fo_seg = R.fo_seg.p; a.fo_clen = R.fo_clen.p; a.fo_excl = R.fo_excl.p;
   a.sh_node = R.sh_node.p; a.sh_prev = R.sh_prev.p; a.sh_tree = R.sh_tree.p; a.sh_seg = R.sh_seg.p;
   a.sh_off = R.sh_off.p; a.sh_excl = R.sh_excl.p;
@@ -945,13 +984,13 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   a.srcp = R.srcp.p; a.nbv = R.nbv.p;
   a.fo_at = R.fo_at.p;
   a.dm_tab = R.dm_tab.p; a.rm_tab = R.rm_tab.p; a.dm_mask = R.dm_mask.p; a.rm_mask = R.rm_mask.p;
-  a.dm_excl = R.dm_excl.p; a.rm_excl = R.rm_excl.p; a.tot = R.tot.p;
+  a.dm_excl = R.dm_excl.p; a.tot = R.tot.p;
   a.fo_rng = R.fo_rng.p;
   a.out = dev_out; a.err = err_.p;
   const bool tree = approach == APPROACH_TREE;
 
   // 1-3: decode entries, repeat tables, source checkpoints
-  MTC_CUDA_R(cudaMemsetAsync(R.tot.p, 0, sizeof(uint64_t) * 4, s));
+  MTC_CUDA_R(cudaMemsetAsync(R.tot.p, 0, sizeof(uint64_t) * 5, s));
   if (nfo + nsh) { load_entries_kernel<<<gsz((uint64_t)nfo + nsh), 256, 0, s>>>(a); note_launch(); }
   rrs_kernel<<<gsz(di.size(), 1, 4), 256, 0, s>>>(a);
   note_launch();
@@ -966,16 +1005,13 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   }
   // main checkpoint
   MTC_CUDA_R(cudaMemsetAsync(R.fo_at.p, 0xff, sizeof(uint32_t) * ((size_t)M + 2), s));
-  MTC_CUDA_R(cudaMemsetAsync(R.nl_rank.p, 0, sizeof(uint64_t) * N, s));
-  MTC_CUDA_R(cudaMemsetAsync(R.cp_rank.p, 0, sizeof(uint64_t) * N, s));
   if (di[0].F) { fo_at_kernel<<<gsz(di[0].F), 256, 0, s>>>(a); note_launch(); }
   if (di[0].S) {
     main_shift_kernel<<<gsz(di[0].S), 256, 0, s>>>(a);
     note_launch();
-    // items of the main shift regions
-    MTC_CUDA_R(grid_scan(MainShiftLen{R.sh_prev.p, M, tree ? 1 : 0}, StoreExcl{R.sh_excl.p}, nullptr, di[0].S,
-                         R.scan.p, R.tot.p + 3, s));
   }
+  // items of the main shift regions and of the chain's repeat maps
+  if (nsh) MTC_CUDA_R(grid_scan(ShiftItems{a}, StoreShiftExcl{a}, nullptr, nsh, R.scan.p, R.tot.p + 4, s));
   if (di[0].F || di[0].S) {
     main_cover_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
     note_launch();
@@ -984,14 +1020,12 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   if (nsteps) {
     MTC_CUDA_R(cudaMemsetAsync(R.dm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
     MTC_CUDA_R(cudaMemsetAsync(R.rm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
-    const uint32_t nfo_chain = nfo - a.fo_cb, nsh_chain = nsh - a.sh_cb;
+    const uint32_t nfo_chain = nfo - a.fo_cb;
     if (nfo_chain) {
       chain_ranges_kernel<<<gsz(nfo_chain), 256, 0, s>>>(a, nfo_chain);
       note_launch();
       MTC_CUDA_R(grid_scan(ChainDmCount{a}, StoreExcl{R.dm_excl.p}, nullptr, nfo_chain, R.scan.p, R.tot.p + 0, s));
     }
-    if (nsh_chain && !basic)
-      MTC_CUDA_R(grid_scan(ChainRmCount{a}, StoreExcl{R.rm_excl.p}, nullptr, nsh_chain, R.scan.p, R.tot.p + 1, s));
     chain_tables_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
     note_launch();
   }
