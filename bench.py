@@ -776,6 +776,16 @@ def main():
         for h in host:
             bufs[1].copy_(h, non_blocking=True)
         pinned_out[:nbytes].copy_(bufs[1], non_blocking=True)
+        # W untimed steps through the same path (upload, checkpoint, copy out),
+        # then the handle starts again from the same baseline
+        for i in range(W):
+            bufs[i % 2].copy_(host[i % len(host)], non_blocking=True)
+            work.wait_stream(torch.cuda.current_stream())
+            n = de.checkpoint_device(bufs[i % 2], False)
+            de.copy_diff(out_view[:n])
+        devbuf.copy_(states[W])
+        work.wait_stream(torch.cuda.current_stream())
+        de.checkpoint_device(devbuf, True)
         barrier()
 
         def upload(i):
@@ -800,7 +810,8 @@ def main():
         te = max_over_ranks(torch, time.perf_counter() - t0, dev, ws)
         e2e = {"value": round(whole_job_rate(nbytes * K, te, ws), 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": int(d2h / K),
-               "host_buffers": "pinned; each input and the result buffer moved once before timing",
+               "host_buffers": "pinned; each input and the result buffer moved once, then W untimed steps through "
+                               "the same path, before timing",
                "step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]}
         del host, pinned_out, out_view, bufs
 
