@@ -10,11 +10,14 @@
 //   2. the main checkpoint's scatter is resolved per chunk with last-writer
 //      ranks (its regions are copied in serial order, later ones win);
 //   3. for every later step the keys it covers are written into per-step
-//      first-insert-wins tables plus a per-key bitmask of covering steps;
+//      first-insert-wins tables plus a per-key bitmask of covering steps
+//      (one launch; cells carry a per-restart epoch, so the tables are
+//      never cleared);
 //   4. every chunk then follows its own provenance down the chain: a chunk
 //      that a step does not cover only moves to the next step, so it jumps
-//      straight to the next step whose mask bit is set;
-//   5. one gather pass copies each chunk once from the diff that owns it.
+//      straight to the next step whose mask bit is set; the result is the
+//      chunk's source address and byte count;
+//   5. one copy pass moves each chunk once from the diff that owns it.
 // A chunk that the reference never writes is not written here either.
 #include <algorithm>
 #include <cstring>
