@@ -234,12 +234,17 @@ def restart_bench(torch, mc, dev, a, kind, approach=None):
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
         ok = ok and bool(torch.equal(out, last))
+    # the reference's restart check: hash() of the whole restored buffer
+    # (calculate_digest_host), against the same digest of the original state
+    dig = mc.digest_hex(mc.digest_host(out.cpu().numpy(), kind))
+    dig_ok = dig == mc.digest_hex(mc.digest_host(last.cpu().numpy(), kind))
     name = {mc.TREE: "tree", mc.LIST: "list", mc.BASIC: "basic"}.get(approach, str(approach))
     return {"workload": "restart of checkpoint %d of a %s chain, %.3g GiB buffer, %d B chunks, 4 GiB update "
                         "pattern" % (rid, name, a.restart_gib, a.restart_chunk),
             "value": round(nbytes / dev_t / 1e9, 3), "unit": "GB/s", "ms": round(dev_t * 1e3, 3),
             "call_ms": round(call_t * 1e3, 3),
             "chain_bytes": int(chain_bytes), "verified_byte_identical": ok,
+            "restart_digest": dig.strip(), "digest_matches_original": dig_ok,
             "host_chain_value": round(nbytes / statistics.median(e2e_t) / 1e9, 3),
             "host_chain_ms": round(statistics.median(e2e_t) * 1e3, 3),
             "note": "value: device time with the chain resident in HBM; call_ms adds the host side of the call; "
@@ -825,7 +830,8 @@ def main():
         for name, ap in (("list", mc.LIST), ("basic", mc.BASIC)):
             r2 = restart_bench(torch, mc, dev, a, kind, ap)
             rst["other_approaches"][name] = {k: r2[k] for k in ("value", "ms", "verified_byte_identical",
-                                                                 "host_chain_value", "chain_bytes")}
+                                                                 "digest_matches_original", "host_chain_value",
+                                                                 "chain_bytes")}
             torch.cuda.empty_cache()
 
     bat = None
