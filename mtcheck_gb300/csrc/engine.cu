@@ -712,6 +712,13 @@ int Engine::restore_from_host(const uint8_t* host) {
   return ST_OK;
 }
 
+void Engine::release_restart_scratch() {
+  if (rs_) {
+    destroy_restart_scratch(rs_);  // stream-ordered frees
+    rs_ = nullptr;
+  }
+}
+
 uint64_t Engine::device_bytes() const {
   return sizeof(Digest) * digests_.n + labels_.n + rflag_.n +
          sizeof(uint32_t) * (chunk_slot_.n + changed_list_.n + changed_count_.n + map_size_.n + err_.n + fo_list_.n +

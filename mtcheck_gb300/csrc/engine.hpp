@@ -132,6 +132,9 @@ class Engine {
   // drained (the single-call path does it itself).
   void release_retired();
   uint64_t device_bytes() const;
+  // Frees the restart buffers (stream-ordered); the next restart allocates
+  // and clears them again.
+  void release_restart_scratch();
   // Stream-ordered allocation from `pool` for every device buffer of this
   // engine (set before the first checkpoint).
   void set_pool(cudaMemPool_t pool);

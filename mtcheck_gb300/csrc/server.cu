@@ -605,6 +605,9 @@ void Server::finish(Flight& f) {
     }
   } else {
     int rc = e.restart_complete();
+    // a served restart's tables are not kept: admission counted them for this
+    // request only
+    e.release_restart_scratch();
     c.status = rc;
     c.chkpt_id = f.r.chkpt_id;
     if (rc == ST_OK) {
