@@ -135,6 +135,7 @@ class Engine {
   // Frees the restart buffers (stream-ordered); the next restart allocates
   // and clears them again.
   void release_restart_scratch();
+  uint64_t restart_scratch_bytes() const;
   // Stream-ordered allocation from `pool` for every device buffer of this
   // engine (set before the first checkpoint).
   void set_pool(cudaMemPool_t pool);

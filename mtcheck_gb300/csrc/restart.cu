@@ -816,6 +816,19 @@ struct RestartScratch {
 
 void destroy_restart_scratch(RestartScratch* r) { delete r; }
 
+uint64_t Engine::restart_scratch_bytes() const {
+  if (!rs_) return 0;
+  const RestartScratch& R = *rs_;
+  uint64_t b = sizeof(DiffInfo) * R.di.n + sizeof(uint4) * R.fo_rng.n;
+  for (const auto* x : {&R.fo_node, &R.fo_seg, &R.fo_clen, &R.sh_node, &R.sh_prev, &R.sh_tree, &R.sh_seg, &R.rrs,
+                        &R.fo_at, &R.dm_mask, &R.rm_mask, &R.nbv})
+    b += sizeof(uint32_t) * x->n;
+  for (const auto* x : {&R.fo_excl, &R.sh_off, &R.sh_excl, &R.nl_rank, &R.cp_rank, &R.dm_excl, &R.tot, &R.scan,
+                        &R.scan_total, &R.dm_tab, &R.rm_tab, &R.srcp})
+    b += sizeof(uint64_t) * x->n;
+  return b;
+}
+
 static void set_scratch_pool(RestartScratch* r, cudaMemPool_t pool) {
   r->di.pool = pool;
   r->fo_rng.pool = pool;

@@ -328,6 +328,7 @@ uint64_t Server::need_bytes(const Req& r, const Proc& p) const {
 
 void Server::refresh_state_bytes(Proc& p) {
   p.state_dev = p.eng->spilled() ? 0 : p.eng->device_bytes();
+  p.scratch_dev = p.eng->restart_scratch_bytes();
 }
 
 void Server::spill_diff(Proc& p, Archived& a) {
@@ -378,14 +379,26 @@ int Server::restore_state(Proc& p) {
 bool Server::make_room(uint64_t need, uint32_t except) {
   auto used = [&] {
     uint64_t u = chain_dev_;
-    for (Proc* pp : view_) u += pp->state_dev;
+    for (Proc* pp : view_) u += pp->state_dev + pp->scratch_dev;
     return u;
   };
   // spill down to 95% of the budget, so that the next admissions find room
   const uint64_t target = opt_.hbm_budget - opt_.hbm_budget / 20;
   while (used() + need > target) {
-    // 1. every archived checkpoint of the least recently used idle process
+    // 0. the restart tables of the least recently used idle process (a
+    //    cache: dropping them costs only its next restart's allocation)
     Proc* victim = nullptr;
+    for (uint32_t i = 0; i < view_.size(); i++) {
+      Proc& p = *view_[i];
+      if (p.busy || i == except || p.scratch_dev == 0) continue;
+      if (!victim || p.lru < victim->lru) victim = &p;
+    }
+    if (victim) {
+      victim->eng->release_restart_scratch();
+      victim->scratch_dev = 0;
+      continue;
+    }
+    // 1. every archived checkpoint of the least recently used idle process
     for (uint32_t i = 0; i < view_.size(); i++) {
       Proc& p = *view_[i];
       if (p.busy || i == except || p.chain_dev == 0) continue;
@@ -509,7 +522,7 @@ bool Server::try_start(Req& r) {
   Proc& p = *view_[r.pid];
   const uint64_t need = need_bytes(r, p);
   uint64_t used = chain_dev_;
-  for (Proc* pp : view_) used += pp->state_dev;
+  for (Proc* pp : view_) used += pp->state_dev + pp->scratch_dev;
   const double t_room = now_ms();
   const bool over = used + need > opt_.hbm_budget;
   const bool room = !over || make_room(need, r.pid);
@@ -543,7 +556,7 @@ bool Server::try_start(Req& r) {
   st_.worker_ms[0] += now_ms() - t_start;
   st_.inflight_peak = std::max<uint32_t>(st_.inflight_peak, (uint32_t)flights_.size());
   uint64_t u = chain_dev_;
-  for (Proc* pp : view_) u += pp->state_dev;
+  for (Proc* pp : view_) u += pp->state_dev + pp->scratch_dev;
   st_.hbm_used = u;
   st_.hbm_peak = std::max(st_.hbm_peak, u);
   return true;
@@ -595,7 +608,7 @@ void Server::finish(Flight& f) {
       // nothing (a new input pointer or baseline still re-prepares)
       // (not under memory pressure: the process may be spilled before then)
       uint64_t used = chain_dev_;
-      for (Proc* pp : view_) used += pp->state_dev;
+      for (Proc* pp : view_) used += pp->state_dev + pp->scratch_dev;
       if (c.status == ST_OK && opt_.use_graph && e.mode() != MODE_FULL &&
           used < opt_.hbm_budget - opt_.hbm_budget / 10 &&
           e.prepare(f.r.data, f.r.len, false, opt_.id_headroom) == ST_OK)
@@ -605,9 +618,6 @@ void Server::finish(Flight& f) {
     }
   } else {
     int rc = e.restart_complete();
-    // a served restart's tables are not kept: admission counted them for this
-    // request only
-    e.release_restart_scratch();
     c.status = rc;
     c.chkpt_id = f.r.chkpt_id;
     if (rc == ST_OK) {

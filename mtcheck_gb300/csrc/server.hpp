@@ -130,6 +130,7 @@ class Server {
     bool busy = false;
     uint64_t lru = 0;
     uint64_t state_dev = 0;        // device bytes of the engine when resident
+    uint64_t scratch_dev = 0;      // restart tables the engine keeps (dropped first under pressure)
     uint8_t* spill = nullptr;      // pinned copy of the digest state
     uint64_t spill_len = 0;
     cudaGraphExec_t exec = nullptr;
