@@ -151,3 +151,17 @@ def test_restart_handle_reused_across_chains(cuda, mtc, oracle):
             view.fill_(FILL)
             r.restart(view, diffs, i)
             assert np.array_equal(view.cpu().numpy(), want), (n, i, view.data_ptr() % 16)
+
+
+@pytest.mark.parametrize("cs", [3, 24, 4096])
+def test_restart_odd_chunk_sizes(cuda, mtc, oracle, cs):
+    # chunk sizes that are not multiples of 16 (byte-wise copy) and a large one
+    nbytes = 64 * 1024 + 5
+    seq = series(2, nbytes, cs, 4, seed=cs + 40)
+    for approach in (2, 3, 4):
+        gpu, diffs = chain(cuda, mtc, approach, 0, seq, cs)
+        for i in range(len(seq)):
+            want = oracle_restart(oracle, approach, diffs, i, nbytes)
+            out = cuda.full((nbytes,), FILL, dtype=cuda.uint8, device="cuda")
+            gpu.restart(out, diffs, i)
+            assert np.array_equal(out.cpu().numpy(), want), (approach, i)
