@@ -122,6 +122,10 @@ int mtc_restart_device(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* 
  * the names are complete paths of the incremental checkpoint files */
 int mtc_restart_files(mtc_dedup_t* h, void* dev_out, uint64_t len, const char* const* filenames, uint32_t n,
                       uint32_t chkpt_id);
+/* A handle keeps its restart tables between restarts (about 16 bytes per
+ * chunk per chain step, plus about 100 bytes per chunk); this frees them.
+ * The next restart allocates them again.  No reference counterpart. */
+int mtc_release_restart_buffers(mtc_dedup_t* h);
 
 /* counters and timers */
 int mtc_get_info(const mtc_dedup_t* h, mtc_info_t* out);

@@ -134,6 +134,8 @@ class BaseDeduplicator {
     }
     check(mtc_restart_device(h_, data_ptr, len, p.data(), l.data(), (uint32_t)p.size(), chkpt_id));
   }
+  // frees the restart tables the handle keeps between restarts (no reference counterpart)
+  void release_restart_buffers() { check(mtc_release_restart_buffers(h_)); }
 
   // write_chkpt_log / write_restart_log, :172-183
   void write_chkpt_log(header_t& header, std::vector<uint8_t>& diff_h, std::string& logname) {

@@ -106,6 +106,7 @@ SIGNATURES = {
     "mtc_checkpoint_file": (_I, [_VP, _VP, _U64, ctypes.c_char_p, ctypes.c_char_p, _I]),
     "mtc_restart": (_I, [_VP, _VP, _U64, ctypes.POINTER(_VP), ctypes.POINTER(_U64), _U32, _U32]),
     "mtc_restart_device": (_I, [_VP, _VP, _U64, ctypes.POINTER(_VP), ctypes.POINTER(_U64), _U32, _U32]),
+    "mtc_release_restart_buffers": (_I, [_VP]),
     "mtc_restart_files": (_I, [_VP, _VP, _U64, ctypes.POINTER(ctypes.c_char_p), _U32, _U32]),
     "mtc_get_info": (_I, [_VP, ctypes.POINTER(Info)]),
     "mtc_write_chkpt_log": (_I, [_VP, ctypes.POINTER(Header), _VP, _U64, ctypes.c_char_p]),
@@ -279,6 +280,10 @@ class Deduplicator:
         ptrs = (_VP * len(dev_chkpts))(*[int(p) for p, _ in dev_chkpts])
         lens = (_U64 * len(dev_chkpts))(*[int(l) for _, l in dev_chkpts])
         _check(load().mtc_restart_device(self.h, ptr, n, ptrs, lens, len(dev_chkpts), chkpt_id))
+
+    def release_restart_buffers(self):
+        """Free the restart tables kept between restarts (reallocated by the next one)."""
+        _check(load().mtc_release_restart_buffers(self.h))
 
     def restart_files(self, out, filenames, chkpt_id):
         ptr, n = _dev_ptr(out)

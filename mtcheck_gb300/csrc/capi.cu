@@ -164,6 +164,12 @@ int mtc_restart_device(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* 
   return ret_eng(h->eng->restart(static_cast<uint8_t*>(dev_out), len, ptrs, l, hdrs, chkpt_id), h->eng);
 }
 
+int mtc_release_restart_buffers(mtc_dedup_t* h) {
+  if (!h) return ret(MTC_EINVAL, "NULL argument");
+  h->eng->release_restart_scratch();
+  return MTC_OK;
+}
+
 int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* host_diffs, const uint64_t* lens,
                 uint32_t n, uint32_t chkpt_id) {
   if (!h || !dev_out || !host_diffs || !lens) return ret(MTC_EINVAL, "NULL argument");

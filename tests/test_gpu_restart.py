@@ -136,8 +136,9 @@ def test_long_chain_restart(cuda, mtc, oracle, approach):
 
 def test_restart_handle_reused_across_chains(cuda, mtc, oracle):
     # one restarting handle alternates between chains of different lengths and
-    # buffer sizes (its chain tables keep cells of earlier restarts), and
-    # writes into an output that is not 16-byte aligned
+    # buffer sizes (its chain tables keep cells of earlier restarts; once they
+    # are freed and allocated again), and writes into an output that is not
+    # 16-byte aligned
     cs = 128
     sa, sb = series(2, 1 << 18, cs, 6, seed=31), series(1, (1 << 17) + 77, cs, 4, seed=32)
     _, da = chain(cuda, mtc, 4, 0, sa, cs)
@@ -151,6 +152,8 @@ def test_restart_handle_reused_across_chains(cuda, mtc, oracle):
             view.fill_(FILL)
             r.restart(view, diffs, i)
             assert np.array_equal(view.cpu().numpy(), want), (n, i, view.data_ptr() % 16)
+        if i == 3:
+            r.release_restart_buffers()
 
 
 @pytest.mark.parametrize("cs", [3, 24, 4096])
