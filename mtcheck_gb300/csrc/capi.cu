@@ -154,12 +154,12 @@ int mtc_restart_device(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* 
   std::vector<const uint8_t*> ptrs(n);
   std::vector<uint64_t> l(lens, lens + n);
   std::vector<mtc::HeaderHost> hdrs(n);
-  for (uint32_t i = 0; i < n; i++) {
-    ptrs[i] = static_cast<const uint8_t*>(dev_diffs[i]);
-    if (h->eng->mode() == MTC_FULL) continue;
-    if (l[i] < sizeof(mtc::HeaderHost)) { std::memset(&hdrs[i], 0, sizeof(hdrs[i])); continue; }
-    if (cudaMemcpy(&hdrs[i], ptrs[i], sizeof(mtc::HeaderHost), cudaMemcpyDeviceToHost) != cudaSuccess)
-      return ret(MTC_ECUDA, "cannot read checkpoint header");
+  for (uint32_t i = 0; i < n; i++) ptrs[i] = static_cast<const uint8_t*>(dev_diffs[i]);
+  // the headers of the whole chain in one gather and one copy (a 32-byte
+  // copy per diff cost about 10 us each)
+  if (h->eng->mode() != MTC_FULL) {
+    const int rc = h->eng->read_headers(ptrs, l, hdrs);
+    if (rc) return ret_eng(rc, h->eng);
   }
   return ret_eng(h->eng->restart(static_cast<uint8_t*>(dev_out), len, ptrs, l, hdrs, chkpt_id), h->eng);
 }

@@ -54,6 +54,7 @@ Engine::~Engine() {
   if (lay_host_) cudaFreeHost(lay_host_);
   if (err_host_) cudaFreeHost(err_host_);
   if (sp_host_) cudaFreeHost(sp_host_);
+  if (hdr_host_) cudaFreeHost(hdr_host_);
   release_retired();
   destroy_restart_scratch(rs_);
 }

@@ -136,6 +136,11 @@ class Engine {
   // and clears them again.
   void release_restart_scratch();
   uint64_t restart_scratch_bytes() const;
+  // The 32-byte headers of a chain resident in device memory, read on the
+  // handle's stream by one gather kernel and one copy (zeros for a diff
+  // shorter than a header).
+  int read_headers(const std::vector<const uint8_t*>& ptrs, const std::vector<uint64_t>& lens,
+                   std::vector<HeaderHost>& out);
   // Stream-ordered allocation from `pool` for every device buffer of this
   // engine (set before the first checkpoint).
   void set_pool(cudaMemPool_t pool);
@@ -262,6 +267,9 @@ class Engine {
   TmaCache tma_;
   cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   RestartScratch* rs_ = nullptr;  // restart buffers, created on first use
+  DevBuf<uint8_t> hdr_dev_;         // read_headers: gathered headers
+  uint8_t* hdr_host_ = nullptr;     // pinned copy of them
+  size_t hdr_host_cap_ = 0;
   std::vector<void*> retired_;    // replaced map tables awaiting cudaFree
   uint64_t spill_nd_ = 0, spill_cap_ = 0;
   bool restart_raw_ = false;

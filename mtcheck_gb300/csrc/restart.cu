@@ -816,6 +816,52 @@ struct RestartScratch {
 
 void destroy_restart_scratch(RestartScratch* r) { delete r; }
 
+// Headers of up to kHeaderBatch diffs per launch, one thread per byte (the
+// diffs may start at any address).
+constexpr uint32_t kHeaderBatch = 64;
+struct HeaderSrc {
+  const uint8_t* p[kHeaderBatch];
+  uint64_t len[kHeaderBatch];
+  uint32_t n;
+};
+static __global__ void header_gather_kernel(HeaderSrc s, uint8_t* out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t k = t / (uint32_t)sizeof(HeaderHost), b = t % (uint32_t)sizeof(HeaderHost);
+  if (k >= s.n) return;
+  out[t] = s.len[k] >= sizeof(HeaderHost) && s.p[k] ? s.p[k][b] : 0;
+}
+
+int Engine::read_headers(const std::vector<const uint8_t*>& ptrs, const std::vector<uint64_t>& lens,
+                         std::vector<HeaderHost>& out) {
+  const size_t n = ptrs.size(), bytes = n * sizeof(HeaderHost);
+  out.assign(n, HeaderHost{});
+  if (n == 0) return ST_OK;
+  MTC_CUDA_R(hdr_dev_.ensure(bytes, stream_));
+  if (hdr_host_cap_ < bytes) {
+    if (hdr_host_) cudaFreeHost(hdr_host_);
+    hdr_host_ = nullptr;
+    hdr_host_cap_ = 0;
+    MTC_CUDA_R(cudaMallocHost(reinterpret_cast<void**>(&hdr_host_), bytes));
+    hdr_host_cap_ = bytes;
+  }
+  for (size_t i0 = 0; i0 < n; i0 += kHeaderBatch) {
+    HeaderSrc src{};
+    src.n = (uint32_t)std::min<size_t>(kHeaderBatch, n - i0);
+    for (uint32_t k = 0; k < src.n; k++) {
+      src.p[k] = ptrs[i0 + k];
+      src.len[k] = lens[i0 + k];
+    }
+    const uint32_t threads = src.n * (uint32_t)sizeof(HeaderHost);
+    header_gather_kernel<<<(threads + 255) / 256, 256, 0, stream_>>>(src, hdr_dev_.p + i0 * sizeof(HeaderHost));
+    note_launch();
+    MTC_CUDA_R(cudaGetLastError());
+  }
+  MTC_CUDA_R(cudaMemcpyAsync(hdr_host_, hdr_dev_.p, bytes, cudaMemcpyDeviceToHost, stream_));
+  MTC_CUDA_R(cudaStreamSynchronize(stream_));
+  std::memcpy(out.data(), hdr_host_, bytes);
+  return ST_OK;
+}
+
 uint64_t Engine::restart_scratch_bytes() const {
   if (!rs_) return 0;
   const RestartScratch& R = *rs_;
