@@ -85,6 +85,11 @@ def _copy_chunks(buf, cs, dst, src, nbytes, prev=None):
     dst, src = dst[keep], src[keep]
     if dst.size == 0:
         return
+    # one source per destination, the last one, as numpy's assignment keeps
+    # it (a CUDA index_put with repeated indices keeps an arbitrary one)
+    _, last = np.unique(dst[::-1], return_index=True)
+    pick = dst.size - 1 - last
+    dst, src = dst[pick], src[pick]
     rows = _rows(buf, cs, nbytes)
     srows = rows if prev is None else _rows(prev, cs, nbytes)
     vals = srows[_index(buf, src)]

@@ -85,3 +85,21 @@ def test_every_mode_on_the_gpu(cuda, mtc, oracle, mode):
         for i, s in enumerate(seq):
             assert gpu.checkpoint(cuda.from_numpy(s).cuda(), i == 0) == ref.checkpoint(s, i == 0), (mode, approach, i)
         gpu.close()
+
+
+def test_repeated_copy_destinations_keep_the_last_source():
+    # the update series copy chunks onto random destinations; a destination
+    # drawn twice takes the later source, on numpy and torch buffers alike
+    torch = pytest.importorskip("torch")
+    from mtcheck_gb300.workloads import _copy_chunks
+    cs, n = 4, 8
+    base = np.arange(n * cs, dtype=np.uint8)
+    dst, src = np.array([5, 2, 5, 5, 1]), np.array([0, 3, 1, 4, 6])
+    want = base.copy().reshape(n, cs)
+    want[2], want[1], want[5] = base.reshape(n, cs)[3], base.reshape(n, cs)[6], base.reshape(n, cs)[4]
+    a = base.copy()
+    _copy_chunks(a, cs, dst, src, n * cs, prev=base.copy())
+    t = torch.from_numpy(base.copy())
+    _copy_chunks(t, cs, dst, src, n * cs, prev=torch.from_numpy(base.copy()))
+    assert np.array_equal(a.reshape(n, cs), want)
+    assert np.array_equal(t.numpy().reshape(n, cs), want)
