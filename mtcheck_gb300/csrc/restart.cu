@@ -972,6 +972,11 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     d.fo_begin = nfo;
     d.sh_begin = nsh;
     d.rrs_begin = nrrs;
+    // entry indices are 32-bit on the device, shift entries doubled in the
+    // table cells (2h + 1)
+    if ((uint64_t)nfo + d.F >= 0xffffffffull || (uint64_t)nsh + d.S >= (1ull << 31) ||
+        (uint64_t)nrrs + d.id + 1 >= 0xffffffffull)
+      return fail(ST_ENOTSUP, "restart chain holds too many entries");
     nfo += d.F;
     nsh += d.S;
     nrrs += d.id + 1;
