@@ -30,6 +30,8 @@ namespace mtc {
 namespace {
 
 constexpr uint64_t kNone = ~0ull;
+// a resolved data offset at or above 2^kOffBits (only a corrupt chain gives
+// one) leaves the chunk as it was, like an offset past the diff's end
 constexpr uint32_t kOffBits = 48;
 
 struct DiffInfo {
