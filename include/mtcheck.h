@@ -115,7 +115,8 @@ int mtc_checkpoint_file(mtc_dedup_t* h, const void* dev_data, uint64_t len, cons
  * the device buffer `dev_out` of `len` == header.datalen bytes */
 int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* host_diffs, const uint64_t* lens,
                 uint32_t n, uint32_t chkpt_id);
-/* same, with the chain already resident in device memory */
+/* same, with the chain already resident in device memory; the diffs must be
+ * complete in the order of the handle's stream (their headers are read on it) */
 int mtc_restart_device(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* dev_diffs,
                        const uint64_t* lens, uint32_t n, uint32_t chkpt_id);
 /* restart(View, std::vector<std::string>& filenames, std::string&, uint32_t), :156-159;
