@@ -44,3 +44,6 @@ def test_bad_arguments_fail_without_gpu(mtc):
     assert lib.mtc_create(4, 7, 128, ctypes.byref(h)) == 1
     assert lib.mtc_create(4, 0, 0, ctypes.byref(h)) == 1
     assert b"chunk size" in lib.mtc_last_error()
+    # NULL handles are refused before any CUDA call
+    assert lib.mtc_release_restart_buffers(None) == 1
+    assert b"NULL" in lib.mtc_last_error()
