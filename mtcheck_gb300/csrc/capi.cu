@@ -28,18 +28,28 @@ struct mtc_batch {
 };
 
 namespace {
-thread_local std::string t_err;
+// The message of the last failing call on this thread, in a fixed array (no
+// heap allocation when a call fails).
+constexpr size_t kErrCap = 512;
+thread_local char t_err[kErrCap];
 
-int ret(int rc, const std::string& msg) {
-  if (rc != MTC_OK) t_err = msg;
+int ret(int rc, const char* msg) {
+  if (rc != MTC_OK) mtc::set_last_error(msg);
   return rc;
 }
-int ret_eng(int rc, mtc::Engine* e) { return ret(rc, e ? e->last_error : std::string("error")); }
+int ret(int rc, const std::string& msg) { return ret(rc, msg.c_str()); }
+int ret_eng(int rc, mtc::Engine* e) { return ret(rc, e ? e->last_error.c_str() : "error"); }
 
 bool valid_mode(int a) { return a >= MTC_FULL && a <= MTC_TREE_LOW_OFFSET; }
 }  // namespace
 
-void mtc::set_last_error(const char* msg) { t_err = msg ? msg : ""; }
+void mtc::set_last_error(const char* msg) {
+  if (!msg) msg = "";
+  size_t n = std::strlen(msg);
+  if (n >= kErrCap) n = kErrCap - 1;
+  std::memcpy(t_err, msg, n);
+  t_err[n] = 0;
+}
 
 extern "C" {
 
@@ -89,6 +99,12 @@ int mtc_checkpoint(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_
   int rc = mtc_checkpoint_header(h, nullptr, dev_data, len, make_baseline, diff_len);
   if (rc == MTC_OK) h->eng->current_id += 1;
   return rc;
+}
+
+int mtc_inject_stall(mtc_dedup_t* h, uint32_t checkpoints) {
+  if (!h) return ret(MTC_EINVAL, "NULL handle");
+  h->eng->inject_stall(checkpoints);
+  return MTC_OK;
 }
 
 int mtc_advance(mtc_dedup_t* h) {
@@ -287,9 +303,18 @@ int mtc_hash_chunks(int hash, const void* dev_data, uint64_t len, uint32_t chunk
   a.epi = mtc::EPI_HASH;
   mtc::TmaCache cache;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
-  cudaError_t e = mtc::launch_leaves(a, &cache, s);
+  // a device error word for the call (a bounded wait that runs out sets it)
+  uint32_t* err = nullptr;
+  uint32_t err_host = 0;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&err), sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
+  a.err = err;
+  if (e == cudaSuccess) e = mtc::launch_leaves(a, &cache, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err_host, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (err) cudaFreeAsync(err, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return ret(MTC_ECUDA, cudaGetErrorString(e));
+  if (e != cudaSuccess) return ret(e == cudaErrorMemoryAllocation ? MTC_ENOMEM : MTC_ECUDA, cudaGetErrorString(e));
+  if (err_host & mtc::DERR_SPIN) return ret(MTC_ETIMEOUT, "bounded device wait expired");
   return MTC_OK;
 }
 
@@ -545,6 +570,6 @@ int mtc_autotune(int approach, int hash, uint32_t chunk_size, uint64_t len, mtc_
 
 uint64_t mtc_launch_count(void) { return mtc::launch_count(); }
 
-const char* mtc_last_error(void) { return t_err.c_str(); }
+const char* mtc_last_error(void) { return t_err; }
 
 }  // extern "C"

@@ -17,7 +17,6 @@
 #include <atomic>
 #include <mutex>
 #include <utility>
-#include <vector>
 
 #include "mtc_common.cuh"
 #include "mtc_internal.hpp"
@@ -91,7 +90,7 @@ constexpr uint32_t kCheckCreator = 1u << 31;  // chunk counts stay below 2^31
 __device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t note) {
   const uint32_t k = atomicAdd(a.dup_count, 1u);
   if (k < a.dup_cap) a.dup_list[k] = note;
-  else atomicOr(a.err, DERR_CAPACITY);
+  else raise_err(a.err, DERR_CAPACITY);
 }
 
 // Map insert of one changed chunk (src/tree_approach.cpp:325-349,
@@ -127,13 +126,12 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
         label = FIRST_OCUR;  // first seen by this launch: the lowest chunk keeps it
         note_dup(a, (uint32_t)k | kCheckCreator);
       } else if (EPI == EPI_TREE && __ldcg(&s->tree) == cur) {
-        // lowest node within the older entry, its epoch kept
-        unsigned long long w = old;
-        for (int i = 0; i < 64 && win_node(w) > node; i++) {
-          const unsigned long long seen = atomicCAS(&s->win, w, (w & ~0xffffffffull) | node);
-          if (seen == w) break;
-          w = seen;
-        }
+        // lowest node within the older entry (the reference's atomic_min,
+        // src/tree_approach.cpp:337-339): the entry's high bits (epoch and
+        // serial level) are fixed, since every insert of this launch carries
+        // a larger epoch and leaves them alone, so one atomicMin on the
+        // whole word lowers exactly its node
+        if (win_node(old) > node) atomicMin(&s->win, (old & ~0xffffffffull) | node);
         label = FIRST_OCUR;
         note_dup(a, (uint32_t)k);
       }
@@ -188,6 +186,7 @@ __global__ void __launch_bounds__(kRows + 32, 2) leaf_tma_kernel(const __grid_co
   const int tid = threadIdx.x;
   const uint32_t xsteps = a.cs / W;
   const uint32_t ntiles = (n_full + kRows - 1) / kRows;
+  const uint32_t limit = a.spin_limit ? a.spin_limit : kMbarSpinLimit;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
@@ -203,11 +202,11 @@ __global__ void __launch_bounds__(kRows + 32, 2) leaf_tma_kernel(const __grid_co
     if (tid == kRows) {
       tma_prefetch_desc(&tmap);
       uint32_t it = 0;
-      bool ok = true;
+      bool ok = !a.stall;  // injected fault: no copy is ever issued
       for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         for (uint32_t xs = 0; xs < xsteps; xs++, it++) {
           const uint32_t s = it % kStages, ph = (it / kStages) & 1;
-          if (!mbar_wait(&empty[s], ph ^ 1)) { atomicOr(a.err, DERR_SPIN); ok = false; break; }
+          if (!mbar_wait(&empty[s], ph ^ 1, limit)) { raise_err(a.err, DERR_SPIN); ok = false; break; }
           mbar_arrive_expect_tx(&full[s], kStageBytes);
           tma_load_2d(smem + s * kStageBytes, &tmap, (int32_t)(xs * W), (int32_t)(tile * kRows), &full[s]);
         }
@@ -232,7 +231,7 @@ __global__ void __launch_bounds__(kRows + 32, 2) leaf_tma_kernel(const __grid_co
     uint32_t X[16];
     for (uint32_t xs = 0; xs < xsteps; xs++, it++) {
       const uint32_t s = it % kStages, ph = (it / kStages) & 1;
-      if (!mbar_wait(&full[s], ph)) { atomicOr(a.err, DERR_SPIN); return; }
+      if (!mbar_wait(&full[s], ph, limit)) { raise_err(a.err, DERR_SPIN); return; }
       const uint8_t* stage = smem + s * kStageBytes;
       const uint32_t rowbase = (uint32_t)tid * W;
       // the row into registers, then the stage goes back to the producer
@@ -425,17 +424,22 @@ cudaError_t dispatch_tma(const LeafArgs& a, const CUtensorMap& m, uint32_t n_ful
 }  // namespace
 
 namespace {
+// A fixed table (no heap allocation, so that launch sites reached from the
+// allocation-free entry point allocate nothing either): one entry per kernel
+// instantiation that reads the input, well below the capacity.
+constexpr int kMaxInputKernels = 256;
 std::mutex g_input_mu;
-std::vector<std::pair<const void*, int>> g_input_kernels;
+std::pair<const void*, int> g_input_kernels[kMaxInputKernels];
+int g_input_count = 0;
 }  // namespace
 void register_input_kernel(const void* func, int kind) {
   std::lock_guard<std::mutex> lk(g_input_mu);
-  g_input_kernels.emplace_back(func, kind);
+  if (g_input_count < kMaxInputKernels) g_input_kernels[g_input_count++] = {func, kind};
 }
 int input_kernel_kind(const void* func) {
   std::lock_guard<std::mutex> lk(g_input_mu);
-  for (auto& e : g_input_kernels)
-    if (e.first == func) return e.second;
+  for (int i = 0; i < g_input_count; i++)
+    if (g_input_kernels[i].first == func) return g_input_kernels[i].second;
   return INPUT_NONE;
 }
 

@@ -25,6 +25,11 @@ enum : uint32_t {
   DERR_SORTKEYS = 1u << 7,      // more distinct source checkpoints than the sort supports
 };
 
+// Raise bits in a device error word (a launch given none records nothing).
+__device__ __forceinline__ void raise_err(uint32_t* err, uint32_t bits) {
+  if (err) atomicOr(err, bits);
+}
+
 struct __align__(16) Digest { uint32_t w[4]; };
 
 __device__ __forceinline__ bool digest_eq(const Digest& a, const Digest& b) {
@@ -339,7 +344,7 @@ __device__ inline int map_claim(const DigestMap& m, const Digest& k, uint64_t* s
     if (key_eq(old, k)) { *slot = i; return INS_EXISTING; }
     i = (i + 1) & m.mask;
   }
-  atomicOr(err, DERR_MAP_FULL);
+  raise_err(err, DERR_MAP_FULL);
   return INS_FAILED;
 }
 

@@ -53,7 +53,14 @@ struct LeafArgs {
   int hash_kind = HASH_MURMUR3;
   int epi = EPI_HASH;
   int basic_first = 0;            // basic approach with current_id == 0: every chunk changed
+  // Fault injection for the failure-detection tests: the TMA producer issues
+  // no copy, so every consumer's bounded wait runs out after `spin_limit`
+  // polls and the launch ends with DERR_SPIN, no copy in flight.  0 in
+  // every normal launch.
+  uint32_t stall = 0;
+  uint32_t spin_limit = 0;        // 0: kMbarSpinLimit
 };
+
 
 // Cached TMA descriptor for one (buffer, length, chunk size).
 struct TmaCache {

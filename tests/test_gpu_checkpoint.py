@@ -155,3 +155,28 @@ def test_length_change_requires_baseline(cuda, mtc):
     with pytest.raises(mtc.MtcError) as e:
         gpu.checkpoint(cuda.zeros(1 << 15, dtype=cuda.uint8, device="cuda"), False)
     assert e.value.code == 1
+
+
+def test_same_id_many_equal_chunks(cuda, mtc, oracle):
+    # Header overload (the id is not advanced): a run of 2^20 chunks rewritten
+    # to one content whose digest already has an entry of this id.  Every one
+    # of them lowers that entry's node at once; the lowest chunk must win, as
+    # the reference's atomic_min gives (src/tree_approach.cpp:337-339), and
+    # the rest become shifted duplicates.
+    cs, nbytes = 64, 1 << 27
+    rng = np.random.default_rng(23)
+    s0 = rng.integers(0, 256, nbytes, dtype=np.uint8)
+    s0[-(1 << 22):] = 0
+    s1 = s0.copy()
+    s1[(1 << 20):(1 << 20) + (1 << 26)] = 0
+    s2 = s1.copy()
+    s2[:1 << 16] = 0
+    s2[1 << 26:(1 << 26) + 4096] = rng.integers(0, 256, 4096, dtype=np.uint8)
+    for approach in (4, 5):
+        ref = oracle.Deduplicator(approach, cs)
+        gpu = mtc.Deduplicator(cs, approach=approach)
+        for i, s in enumerate((s0, s1, s2)):
+            want = ref.checkpoint(s, i == 0, increment=False)
+            got = gpu.checkpoint(cuda.from_numpy(s).cuda(), i == 0, advance=False)
+            assert got == want, (approach, i)
+        gpu.close()
