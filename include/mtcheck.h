@@ -93,6 +93,14 @@ int mtc_checkpoint_header(mtc_dedup_t* h, mtc_header_t* header, const void* dev_
                           int make_baseline, uint64_t* diff_len);
 /* checkpoint(uint8_t*, size_t, HostMirror&, bool), :93-96 (advances current_id) */
 int mtc_checkpoint(mtc_dedup_t* h, const void* dev_data, uint64_t len, int make_baseline, uint64_t* diff_len);
+/* Fault injection for failure-detection tests (no reference counterpart):
+ * the next `checkpoints` checkpoints of the handle run with the copy producer
+ * of the chunk-hashing kernel silent, so the kernel's bounded waits run out
+ * (after about a millisecond) and the call returns MTC_ETIMEOUT; the GPU
+ * context stays usable.  After any MTC_ETIMEOUT from a checkpoint the
+ * handle's digest state may be partly updated, so its next checkpoint is
+ * taken as a baseline (as if make_baseline were set). */
+int mtc_inject_stall(mtc_dedup_t* h, uint32_t checkpoints);
 /* current_id += 1: what the reference's convenience overloads do after
  * checkpoint(header_t&, ...) (src/tree_approach.cpp:1723, :1747, :1775) */
 int mtc_advance(mtc_dedup_t* h);
@@ -148,24 +156,34 @@ int mtc_digest_host(int hash, const void* host_data, uint64_t len, uint8_t out[1
 /* its printable form: "XXXXXXXX XXXXXXXX XXXXXXXX XXXXXXXX " (37 bytes incl. NUL) */
 int mtc_digest_hex(const uint8_t digest[16], char out[37]);
 
-/* Checkpoint for callers that cannot allocate memory -- code running inside an
- * allocator or an out-of-memory handler, a signal or crash handler that saves
- * state on the way down, or a runtime whose pool owns all GPU memory.  No
- * counterpart in the reference; it produces the same bytes as the basic
- * approach (MTC_BASIC) without a handle and without allocating anything:
- *   dev_digests  caller-owned, 16 bytes per chunk; the previous checkpoint's
- *                chunk digests on entry (zeros before the first), the current
- *                ones on return
+/* Checkpoint for callers that cannot allocate memory.  No counterpart in
+ * the reference.  It serves code that must not or cannot allocate: an
+ * out-of-memory handler saving state when no memory is left to ask for, a
+ * signal or crash handler taking a last checkpoint without entering an
+ * allocator that may be locked or corrupt, and a runtime or custom allocator
+ * whose pool owns the whole GPU (a cudaMalloc there would recurse into it).
+ * It produces the same bytes as the basic approach (MTC_BASIC) without a
+ * handle, calls no cudaMalloc, cudaFree or other allocating routine, and
+ * takes no host heap memory of its own:
+ *   dev_digests  caller-owned, 16-byte aligned, 16 bytes per chunk; the
+ *                previous checkpoint's chunk digests on entry (any value
+ *                before the first), the current ones on return
  *   first        nonzero for the first checkpoint (every chunk is saved)
  *   dev_diff     caller-owned device buffer, 4-byte aligned, capacity at least
  *                32 + chunks * (4 + chunk_size); receives the .basic checkpoint
  *                (header with ref_id/chkpt_id as given, changed chunk ids in
  *                ascending order, their data)
- * At most 4194304 chunks (MTC_ENOTSUP beyond).  Its scratch is a fixed 4 MiB
- * device array that every GPU loading the library holds until exit; the first
- * call on a device looks up that array's address, so make that first call
- * before any stream capture.  Calls share the array: calls that overlap on the
- * GPU race and must be serialised by the caller. */
+ * At most 4194304 chunks per call (MTC_ENOTSUP beyond).  Its scratch is a
+ * fixed device array of about 4 MiB in the library, which every GPU that
+ * loads the library holds until the process exits.  The first call on each
+ * device does the set-up: it looks up that array's device address (and the
+ * CUDA driver loads the kernels it uses), so make that first call early, while
+ * memory is still available, and before any stream capture.  The call
+ * synchronises its stream (it reads the count of changed chunks back), so it
+ * must not be made while a capture is active on that stream.  Calls share
+ * the array and each keeps the last call's contents: calls that overlap on
+ * the GPU (other streams or threads) race and must be serialised by the
+ * caller.  A bounded device wait that runs out gives MTC_ETIMEOUT. */
 int mtc_basic_checkpoint_noalloc(int hash, const void* dev_data, uint64_t len, uint32_t chunk_size,
                                  void* dev_digests, uint32_t ref_id, uint32_t chkpt_id, int first, void* dev_diff,
                                  uint64_t diff_capacity, uint64_t* diff_len, void* cuda_stream);

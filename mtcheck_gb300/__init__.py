@@ -99,6 +99,7 @@ SIGNATURES = {
     "mtc_checkpoint_header": (_I, [_VP, ctypes.POINTER(Header), _VP, _U64, _I, ctypes.POINTER(_U64)]),
     "mtc_checkpoint": (_I, [_VP, _VP, _U64, _I, ctypes.POINTER(_U64)]),
     "mtc_advance": (_I, [_VP]),
+    "mtc_inject_stall": (_I, [_VP, _U32]),
     "mtc_diff_copy": (_I, [_VP, _VP, _U64]),
     "mtc_diff_device": (_I, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(_U64)]),
     "mtc_checkpoint_alloc": (_I, [_VP, _VP, _U64, _I, ctypes.POINTER(_VP), ctypes.POINTER(_U64)]),
@@ -280,6 +281,11 @@ class Deduplicator:
         ptrs = (_VP * len(dev_chkpts))(*[int(p) for p, _ in dev_chkpts])
         lens = (_U64 * len(dev_chkpts))(*[int(l) for _, l in dev_chkpts])
         _check(load().mtc_restart_device(self.h, ptr, n, ptrs, lens, len(dev_chkpts), chkpt_id))
+
+    def inject_stall(self, checkpoints=1):
+        """Fault injection for tests: the next checkpoints' hashing kernel
+        times out on the device (MTC_ETIMEOUT); the one after is a baseline."""
+        _check(load().mtc_inject_stall(self.h, checkpoints))
 
     def release_restart_buffers(self):
         """Free the restart tables kept between restarts (reallocated by the next one)."""

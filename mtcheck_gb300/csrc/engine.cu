@@ -28,6 +28,9 @@ static __global__ void params_in_kernel(StepParams p, StepParams* dev, uint32_t*
   }
 }
 
+// Polls of an injected stall's bounded waits (about a millisecond).
+constexpr uint32_t kInjectedSpinLimit = 1u << 14;
+
 static uint64_t next_pow2(uint64_t v) {
   uint64_t c = 1;
   while (c < v) c <<= 1;
@@ -245,6 +248,10 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
   la.dup_list = fo_list_.p;
   la.dup_count = changed_count_.p + 3;
   la.dup_cap = (uint32_t)fo_list_.n;
+  if (stall_now_) {
+    la.stall = 1;
+    la.spin_limit = kInjectedSpinLimit;
+  }
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_TRY(mark(4));
@@ -296,6 +303,10 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
   la.dup_list = fo_list_.p;  // free until the chunk compaction
   la.dup_count = changed_count_.p + 3;
   la.dup_cap = (uint32_t)fo_list_.n;
+  if (stall_now_) {
+    la.stall = 1;
+    la.spin_limit = kInjectedSpinLimit;
+  }
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
   MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_TRY(mark(4));
@@ -308,6 +319,7 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
 int Engine::prepare(const uint8_t* data, uint64_t len, bool make_baseline, uint32_t id_headroom) {
   if (!data || len == 0) return fail(ST_EINVAL, "empty buffer");
   if (spilled_) return fail(ST_EINVAL, "state spilled to host: restore it first");
+  if (need_baseline_) make_baseline = true;  // the last checkpoint timed out on the device
   const uint64_t n64 = (len + cs_ - 1) / cs_;
   if (n64 >= (1ull << 31)) return fail(ST_ENOTSUP, "more than 2^31 chunks");
   const uint32_t N = (uint32_t)n64;
@@ -556,9 +568,13 @@ int Engine::checkpoint(const uint8_t* data, uint64_t len, bool make_baseline, He
   if (rc) return rc;
   if ((rc = order_inputs()) != ST_OK) return rc;
   if (mode_ != MODE_FULL) stage_params();
-  // a step that allocates (a first checkpoint or a new baseline) runs eagerly
-  if (own_graph_ && mode_ != MODE_FULL && !fresh_) rc = replay_own(data, len);
+  stall_now_ = stall_left_ > 0 && mode_ != MODE_FULL;
+  if (stall_now_) stall_left_--;
+  // a step that allocates (a first checkpoint or a new baseline) runs eagerly,
+  // and so does an injected stall (never part of a captured sequence)
+  if (own_graph_ && mode_ != MODE_FULL && !fresh_ && !stall_now_) rc = replay_own(data, len);
   else rc = enqueue(data, len, true);
+  stall_now_ = false;
   if (rc) return rc;
   MTC_CUDA(cudaStreamSynchronize(stream_));
   release_retired();
@@ -599,11 +615,17 @@ int Engine::complete(uint64_t len, HeaderHost* header) {
     const float leaf = event_ms(ev_[1], ev_[4]), rest = event_ms(ev_[4], ev_[2]);
     phase_times[0] = leaf * 1e-3; phase_times[1] = rest * 1e-3; phase_times[2] = ms[2] * 1e-3;
   }
-  if (last_device_error & DERR_SPIN) return fail(ST_ETIMEOUT, "bounded device wait expired");
+  if (last_device_error & DERR_SPIN) {
+    // some chunks' digests may already be stored: the next checkpoint starts
+    // from scratch as a baseline
+    need_baseline_ = true;
+    return fail(ST_ETIMEOUT, "bounded device wait expired (the next checkpoint is taken as a baseline)");
+  }
   if (last_device_error & (DERR_MAP_FULL | DERR_CAPACITY)) return fail(ST_ENOMEM, "device table or staging buffer full");
   if (last_device_error & DERR_MISSING) return fail(ST_EINTERNAL, "root digest missing from the map");
   if (last_device_error & DERR_SORTKEYS) return fail(ST_ENOTSUP, "more than 1024 distinct source checkpoints in one diff");
   if (!L.ok) return fail(ST_EINTERNAL, "diff layout failed");
+  if (fresh_) need_baseline_ = false;
   diff_len_ = L.diff_len;
   diff_pad_ = L.pad;
   num_first_ocur = L.F;

@@ -189,6 +189,13 @@ class Engine {
   void set_order_after_legacy(bool on) { order_after_legacy_ = on; }
   int order_inputs();
   uint32_t launches() const { return launches_; }
+  // Fault injection for tests: the next n checkpoints run eagerly with the
+  // chunk-hashing kernel's copy producer silent, so its bounded waits run
+  // out and the checkpoint fails with ST_ETIMEOUT.
+  void inject_stall(uint32_t n) { stall_left_ = n; }
+  // After a device timeout the digest state may be partly updated: the next
+  // checkpoint is taken as a baseline.
+  bool needs_baseline() const { return need_baseline_; }
 
  private:
   int fail(int code, const std::string& msg);
@@ -244,6 +251,8 @@ class Engine {
   int mark(int i);
   void drop_own_graph();
   bool stream_work_ = false;
+  uint32_t stall_left_ = 0;
+  bool stall_now_ = false, need_baseline_ = false;
   uint32_t epoch_ = 0;
   uint64_t map_cap_ = 0;
   uint32_t map_size_host_ = 0;
