@@ -1280,7 +1280,7 @@ cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M,
   if (ntiles == 0) ntiles = 1;
   const uint32_t nd = 2 * num_sms();
   root_count_kernel<<<ntiles + nd, kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay, nd);
-  if (ntiles <= kReduceTiles) {
+  if (ntiles <= reduce_tile_limit()) {
     root_emit_kernel<true><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
     note_launch(2);
     return cudaGetLastError();

@@ -1,6 +1,7 @@
 // mtc_scan.cuh -- deterministic block/grid scans used by the compaction,
 // gather and restart kernels.  Results never depend on scheduling order.
 #pragma once
+#include <cstdlib>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -111,6 +112,17 @@ __global__ void scan_emit_kernel(Val val, Emit emit, const uint32_t* n_ptr, uint
 // block sums the sums of the tiles before it; the block holding element n-1
 // (block 0 when n is 0) writes the grand total.
 constexpr uint32_t kReduceTiles = 2048;
+// The largest grid the two-launch forms serve: kReduceTiles, or less under the
+// test hook MTCHECK_REDUCE_TILES, which sends small inputs down the
+// three-launch path that otherwise only inputs of more than 2^23 elements take.
+inline uint32_t reduce_tile_limit() {
+  const char* e = std::getenv("MTCHECK_REDUCE_TILES");
+  if (e && *e) {
+    const unsigned long v = std::strtoul(e, nullptr, 10);
+    if (v < kReduceTiles) return (uint32_t)v;
+  }
+  return kReduceTiles;
+}
 template <class Val, class Emit>
 __global__ void scan_emit_reduce_kernel(Val val, Emit emit, const uint32_t* n_ptr, uint64_t n_const,
                                         const uint64_t* tile_sums, uint64_t* total) {
@@ -150,7 +162,7 @@ inline cudaError_t grid_scan(Val val, Emit emit, const uint32_t* n_dev, uint64_t
   uint32_t ntiles = (uint32_t)((max_n + kScanTile - 1) / kScanTile);
   if (ntiles == 0) ntiles = 1;
   scan_tile_sums_kernel<<<ntiles, kScanThreads, 0, s>>>(val, n_dev, max_n, scratch);
-  if (ntiles <= kReduceTiles) {
+  if (ntiles <= reduce_tile_limit()) {
     scan_emit_reduce_kernel<<<ntiles, kScanThreads, 0, s>>>(val, emit, n_dev, max_n, scratch, total);
     note_launch(2);
     return cudaGetLastError();

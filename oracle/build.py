@@ -2,7 +2,8 @@
 
 * ``oracle/_build/liboracle.so``: the C restatement in ``mtc_oracle.c``.
 * ``oracle/_ref/libref_hash.so``: the reference's own digest headers compiled
-  from where they lie (``/root/reference/include``) against the macro stub in
+  from where they lie (``$MTCHECK_REFERENCE/include``, by default
+  /root/reference/include) against the macro stub in
   ``oracle/ref_stub``.  Built only where the reference is mounted; the files
   travel with the repository snapshot but ``.so`` files are rebuilt per host.
 """
@@ -11,7 +12,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+# where the reference sources are mounted (only in the development container)
+REFERENCE = os.environ.get("MTCHECK_REFERENCE", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_hash.so")
 

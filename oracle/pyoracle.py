@@ -4,6 +4,7 @@ Test infrastructure: imported only by ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline leg of ``bench.py``.  The product library never loads it.
 """
 import ctypes
+import struct
 import os
 
 import numpy as np
@@ -90,7 +91,13 @@ class Deduplicator:
                                   ctypes.byref(p), ctypes.byref(n))
         if rc != 0:
             raise RuntimeError(f"oracle checkpoint failed: {rc}")
-        out = ctypes.string_at(p.value, n.value)
+        if n.value < (1 << 31):
+            out = ctypes.string_at(p.value, n.value)
+        else:  # string_at takes a C int size
+            a = np.empty(n.value, dtype=np.uint8)
+            ctypes.memmove(a.ctypes.data, p.value, n.value)
+            out = a.tobytes()
+            del a
         lib().orc_free(p)
         return out
 
@@ -113,3 +120,54 @@ def restart(approach, diffs, chkpt_id, out):
     lens = (ctypes.c_uint64 * len(bufs))(*[b.size for b in bufs])
     rc = lib().orc_restart(approach, ptrs, lens, len(bufs), chkpt_id, out.ctypes.data, out.size)
     return rc
+
+
+# ---------------------------------------------------------------------------
+# CSV logs of one checkpoint, restated from the reference's writers: the
+# values of every column except the timers.
+# ---------------------------------------------------------------------------
+LOG_NAMES = {FULL: "Full", BASIC: "Basic", LIST: "List", TREE: "Tree", TREE_LOW_OFFSET_REF: "Tree",
+             TREE_LOW_OFFSET: "Tree"}
+
+
+def metadata_breakdown(diff, num_chkpts):
+    """write_metadata_breakdown (src/utils.cpp:38-124): header bytes, distinct
+    metadata bytes, repeat-map bytes, then one column per checkpoint (the
+    bytes of shifted-duplicate entries taken from it, by repeat-map row)."""
+    ref_id, chkpt_id, _datalen, _cs, nfo, nprior, nshift = struct.unpack_from("<IIQIIII", diff, 0)
+    cols = [32, nfo * 4]
+    if ref_id != chkpt_id:                                      # :98-116
+        cols.append(8 * nprior)
+        for i in range(num_chkpts):
+            if i < nprior:
+                off = 32 + nfo * 4 + i * 8
+                num = struct.unpack_from("<I", diff, off + 4)[0]
+                cols.append(num * 8)
+            else:
+                cols.append(0)
+    else:                                                       # :117-123
+        cols.append(0)
+        cols.append(nshift * 8)
+        cols.extend([0] * max(0, num_chkpts - 1))
+    return cols
+
+
+def log_rows(approach, chunk_size, current_id, baseline_id, data_len, datasizes, diff):
+    """The rows that write_chkpt_log appends for checkpoint `current_id`
+    (src/tree_approach.cpp:1854-1896, src/list_approach.cpp:1014-1052,
+    src/basic_approach.cpp:632-673, src/full_approach.cpp:187-234), with the
+    timer columns left out: (.csv row without its four timers, .size.csv row,
+    .timing.csv row without its timers)."""
+    name = LOG_NAMES[approach]
+    d, m = datasizes
+    csv = [name, current_id, chunk_size, data_len, d + m, d, m]
+    timing = [name, current_id, chunk_size]
+    if approach == FULL:
+        size = [name, current_id, chunk_size, d, 0, 0, 0, 0] + [0] * current_id
+        timing += ["0.0", "0.0"]
+        return csv, size, timing
+    # the basic approach passes current_id - baseline_id + 1 checkpoints
+    # (src/basic_approach.cpp:672), the others current_id
+    n = current_id - baseline_id + 1 if approach == BASIC else current_id
+    size = [name, current_id, chunk_size, d, m] + metadata_breakdown(diff, n)
+    return csv, size, timing

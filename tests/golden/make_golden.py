@@ -9,7 +9,13 @@
   computed by the reference's own hash headers (include/kokkos_murmur3.hpp,
   include/kokkos_md5.hpp) compiled by ``oracle/build.py`` into oracle/_ref.
 
-Run from the repository root, where /root/reference is mounted:
+* ``long_hash_vectors.json``: whole-buffer digests of inputs longer than
+  INT_MAX bytes (a fixed arithmetic byte pattern, ``long_pattern``), where the
+  reference's MD5 takes its 128-byte-piece branch
+  (include/kokkos_md5.hpp:293-301), computed by the same compiled headers.
+
+Run from the repository root where the reference sources are mounted
+(``MTCHECK_REFERENCE``, default /root/reference):
     python tests/golden/make_golden.py
 """
 import ctypes
@@ -22,7 +28,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-REF = "/root/reference"
+REF = os.environ.get("MTCHECK_REFERENCE", "/root/reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 # lengths: every tail length, block boundaries, and the chunk sizes in use
@@ -68,9 +74,41 @@ def hash_vectors():
     return vecs
 
 
+# lengths above INT_MAX: len % 128 = 77 (a short last piece) and 0 (an
+# empty last piece)
+LONG_LENGTHS = [(1 << 31) + 77, (1 << 31) + 128]
+
+
+def long_pattern(n, block=64 << 20):
+    """n bytes: byte i = ((i * 2654435761) mod 2^32) >> 24."""
+    out = np.empty(n, dtype=np.uint8)
+    for s in range(0, n, block):
+        x = np.arange(s, min(n, s + block), dtype=np.uint32)
+        out[s:s + x.size] = ((x * np.uint32(2654435761)) >> np.uint32(24)).astype(np.uint8)
+    return out
+
+
+def long_vectors():
+    from oracle import build
+    lib = ctypes.CDLL(build.build_ref())
+    vecs = []
+    for n in LONG_LENGTHS:
+        data = long_pattern(n)
+        ent = {"len": n}
+        for name, fn in (("murmur3", lib.ref_murmur3_hash), ("md5", lib.ref_md5_hash)):
+            out = (ctypes.c_uint8 * 16)()
+            fn(ctypes.c_void_p(data.ctypes.data), ctypes.c_uint64(n), out)
+            ent[name] = bytes(out).hex()
+        vecs.append(ent)
+    return vecs
+
+
 if __name__ == "__main__":
     with open(os.path.join(OUT, "tree_kat.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": kat_cases()}, f, indent=1)
     with open(os.path.join(OUT, "hash_vectors.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "seed": HASH_SEED, "vectors": hash_vectors()}, f)
+    with open(os.path.join(OUT, "long_hash_vectors.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "pattern": "long_pattern",
+                   "vectors": long_vectors()}, f, indent=1)
     print("wrote", os.listdir(OUT))

@@ -50,3 +50,24 @@ def test_oracle_matches_compiled_reference(oracle):
             out = (ctypes.c_uint8 * 16)()
             fn(d.ctypes.data, n, out)
             assert oracle.digest(d, kind) == bytes(out)
+
+
+def test_whole_buffer_digest_above_int_max(mtc, oracle):
+    # calculate_digest_host over more than INT_MAX bytes: the reference's MD5
+    # then feeds 128-byte pieces and cuts the last one to len % 128 bytes
+    # (include/kokkos_md5.hpp:293-301).  The golden digests come from the
+    # reference's own headers; the library's host digest (the restart check)
+    # and the oracle must reproduce them.
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(GOLDEN),
+                                                                              "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    vecs = json.load(open(os.path.join(os.path.dirname(GOLDEN), "long_hash_vectors.json")))["vectors"]
+    assert [v["len"] for v in vecs] == mg.LONG_LENGTHS
+    for v in vecs:
+        data = mg.long_pattern(v["len"])
+        assert mtc.digest_host(data, mtc.MD5).hex() == v["md5"], v["len"]
+        assert oracle.digest(data, oracle.MD5).hex() == v["md5"], v["len"]
+        assert mtc.digest_host(data, mtc.MURMUR3).hex() == v["murmur3"], v["len"]
+        del data
