@@ -63,8 +63,11 @@ struct RArgs {
   uint64_t* srcp;                // per chunk: source address (TMA restore path)
   uint32_t* nbv;                 // per chunk: bytes to copy, 0 for none
   uint32_t* fo_at;  // main checkpoint: lowest FO entry per node (tree) or chunk (list)
-  uint64_t *dm_tab, *rm_tab;     // [step][key] cells, tag | (2^32-1 - entry index)
-  uint32_t *dm_mask, *rm_mask;   // [key][step / 32] bits: the step's map holds the key
+  uint32_t* dm_off;              // [step][key] position of the key's chunk in the step's data (valid
+                                 // where the step's distinct-map bit is set)
+  uint64_t* rm_tab;              // [step][key] repeat-map cells, tag | (2^32-1 - entry index)
+  uint32_t* sbm;                 // [KW][32 W steps][dm, rm] bitmaps: the step's map holds the key
+  uint32_t KW;                   // 32-key words per bitmap
   uint64_t* dm_excl;            // per chain FO entry: item prefix of the distinct-map table
   uint4* fo_rng;                // chain FO entries: leaf key ranges {lo0, n0, lo1, n1}
   uint64_t *tot;                // [0] dm items, [2] main FO chunks, [3] main shift chunks, [4] [3] + rm items
@@ -290,11 +293,13 @@ __device__ __forceinline__ uint32_t warp_upper_entry(const uint64_t* excl, uint3
 // searches in global memory) are staged in shared memory, and every item
 // finds its entry by a binary search there.
 constexpr uint32_t kExpandTile = 2048;
+template <uint32_t TILE = kExpandTile>
 struct ExpandTile {
-  uint64_t ex[kExpandTile + 1];
+  uint64_t ex[TILE + 1];
   uint32_t e0, e1;
 };
-__device__ __forceinline__ void expand_stage(ExpandTile& T, const uint64_t* excl, uint32_t n, uint64_t t0,
+template <uint32_t TILE>
+__device__ __forceinline__ void expand_stage(ExpandTile<TILE>& T, const uint64_t* excl, uint32_t n, uint64_t t0,
                                              uint64_t t1) {
   const uint32_t warp = threadIdx.x >> 5;
   if (warp < 2) {
@@ -303,15 +308,16 @@ __device__ __forceinline__ void expand_stage(ExpandTile& T, const uint64_t* excl
   }
   __syncthreads();
   const uint32_t cnt = T.e1 - T.e0 + 1;
-  if (cnt <= kExpandTile + 1)
+  if (cnt <= TILE + 1)
     for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) T.ex[i] = excl[T.e0 + i];
   __syncthreads();
 }
 // entry owning `item` and the item's position within it
-__device__ __forceinline__ uint32_t expand_entry(const ExpandTile& T, const uint64_t* excl, uint32_t n,
+template <uint32_t TILE>
+__device__ __forceinline__ uint32_t expand_entry(const ExpandTile<TILE>& T, const uint64_t* excl, uint32_t n,
                                                  uint64_t item, uint64_t* j) {
   const uint32_t cnt = T.e1 - T.e0 + 1;
-  if (cnt > kExpandTile + 1) {
+  if (cnt > TILE + 1) {
     const uint32_t k = upper_entry(excl, n, item);
     *j = item - excl[k];
     return k;
@@ -326,10 +332,11 @@ __device__ __forceinline__ uint32_t expand_entry(const ExpandTile& T, const uint
 }
 
 // Tiles of two item lists taken in one grid: list 0's tiles first.
+template <uint32_t TILE = kExpandTile>
 struct TwoLists {
   uint64_t tot0, tot1, nt0, nt1;
   __device__ __forceinline__ TwoLists(uint64_t a0, uint64_t a1)
-      : tot0(a0), tot1(a1), nt0((a0 + kExpandTile - 1) / kExpandTile), nt1((a1 + kExpandTile - 1) / kExpandTile) {}
+      : tot0(a0), tot1(a1), nt0((a0 + TILE - 1) / TILE), nt1((a1 + TILE - 1) / TILE) {}
   __device__ __forceinline__ uint64_t tiles() const { return nt0 + nt1; }
 };
 
@@ -338,8 +345,8 @@ struct TwoLists {
 // the FO regions (prefix fo_excl, total tot[2]) and the shift regions (prefix
 // sh_excl, total tot[3]) in one launch
 __global__ void __launch_bounds__(256) main_cover_kernel(RArgs a) {
-  __shared__ ExpandTile T;
-  const TwoLists L(a.tot[2], a.tot[3]);
+  __shared__ ExpandTile<> T;
+  const TwoLists<> L(a.tot[2], a.tot[3]);
   const bool tree = a.approach == APPROACH_TREE;
   for (uint64_t tile = blockIdx.x; tile < L.tiles(); tile += gridDim.x) {
     const bool sh = tile >= L.nt0;
@@ -416,11 +423,16 @@ __global__ void chain_ranges_kernel(RArgs a, uint32_t n) {
   }
 }
 
+// Chain table items are segments of up to kSegKeys consecutive keys of one
+// entry, each handled by one thread.
+constexpr uint32_t kSegKeys = 32;
+__device__ __forceinline__ uint32_t segs_of(uint32_t keys) { return (keys + kSegKeys - 1) / kSegKeys; }
+
 struct ChainDmCount {
   RArgs a;
   __device__ __forceinline__ uint64_t operator()(uint64_t k) const {
     const uint4 r = a.fo_rng[a.fo_cb + k];
-    return (uint64_t)r.y + r.w;
+    return (uint64_t)segs_of(r.y) + segs_of(r.w);
   }
 };
 struct ChainRmCount {
@@ -432,7 +444,7 @@ struct ChainRmCount {
     // repeat_map keys: the root (src/tree_approach.cpp:1069) and the leaf
     // range of num_leaf_descendents(node) from leftmost_leaf(node) (:1073-1078);
     // only keys in [N-1, M] can be looked up by a leaf
-    uint64_t c = num_leaf_descendents(node, a.M);
+    uint64_t c = segs_of(num_leaf_descendents(node, a.M));
     if (node >= a.N - 1 && node <= a.M) c += 1;
     return c;
   }
@@ -459,87 +471,309 @@ struct StoreShiftExcl {
 
 __device__ __forceinline__ uint32_t key_of_leaf(const RArgs& a, uint32_t x) { return x - (a.N - 1); }
 
-// Every (step, key) cell that a chain step's distinct map (FO entries) or
-// repeat map (shift entries) holds, both item lists in one launch.  A cell
-// keeps the entry that the reference inserts first (the lowest entry index;
-// shift entries as 2h for the root key, 2h+1 for the leaf keys) through an
-// atomicMax of tag | (2^32-1 - index): `tag` is this restart's epoch in the
-// high word, so a cell written by an earlier restart loses to any write of
-// this one and needs no clearing pass.  The key's mask bit for the step is
-// set beside it (masks are cleared for every restart).
+// The three entry scans of a restart in one pair of launches, each segment
+// starting on a tile boundary and scanned on its own:
+//   0: region length of every FO entry (FoLen) -> fo_excl
+//   1: table segments of every chain FO entry, with its leaf ranges
+//      (ChainDmCount, chain_ranges_kernel; the ranges are kept by the first
+//      launch for the second) -> dm_excl, fo_rng, total tot[0]
+//   2: items of every shift entry (ShiftItems) -> sh_excl, tot[3], total tot[4]
+// Used when every segment fits the two-launch form (at most kReduceTiles
+// tiles); otherwise the three scans run separately.
+struct EntryScans {
+  RArgs a;
+  uint64_t n[3];
+  uint32_t first[4];  // first tile of each segment; first[3] = all tiles
+};
+__device__ __forceinline__ uint4 chain_ranges_of(const RArgs& a, uint32_t g) {
+  uint4 r = make_uint4(0, 0, 0, 0);
+  if (a.approach == APPROACH_TREE) {
+    uint32_t lo[2], hi[2];
+    const int nr = fo_leaf_ranges(a.fo_node[g], a.N, a.M, lo, hi);
+    if (nr > 0) { r.x = lo[0]; r.y = hi[0] - lo[0] + 1; }
+    if (nr > 1) { r.z = lo[1]; r.w = hi[1] - lo[1] + 1; }
+  } else {
+    r.x = a.fo_node[g];
+    r.y = 1;
+  }
+  return r;
+}
+// `ranges`: compute a chain entry's leaf ranges and keep them (first pass),
+// or read the kept ones (second pass)
+__device__ __forceinline__ uint64_t entry_scan_val(const EntryScans& e, int k, uint64_t i, bool ranges) {
+  if (k == 0) return FoLen{e.a.fo_node, e.a.M, e.a.approach == APPROACH_TREE ? 1 : 0}(i);
+  if (k == 1) {
+    const uint32_t g = e.a.fo_cb + (uint32_t)i;
+    uint4 r;
+    if (ranges) {
+      r = chain_ranges_of(e.a, g);
+      e.a.fo_rng[g] = r;
+    } else {
+      r = e.a.fo_rng[g];
+    }
+    return (uint64_t)segs_of(r.y) + segs_of(r.w);
+  }
+  return ShiftItems{e.a}(i);
+}
+__device__ __forceinline__ int entry_scan_seg(const EntryScans& e, uint32_t b) {
+  return b < e.first[1] ? 0 : b < e.first[2] ? 1 : 2;
+}
+__global__ void entry_scan_sums_kernel(EntryScans e, uint64_t* tile_sums) {
+  __shared__ uint64_t sh[33];
+  const int k = entry_scan_seg(e, blockIdx.x);
+  const uint64_t base = (uint64_t)(blockIdx.x - e.first[k]) * kScanTile;
+  uint64_t sum = 0;
+  for (int q = 0; q < kScanPerThread; q++) {
+    const uint64_t i = base + (uint64_t)q * kScanThreads + threadIdx.x;
+    if (i < e.n[k]) sum += entry_scan_val(e, k, i, true);
+  }
+  uint64_t total;
+  block_excl_scan(sum, sh, &total);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+__global__ void entry_scan_emit_kernel(EntryScans e, const uint64_t* tile_sums) {
+  __shared__ uint64_t sh[33];
+  const int k = entry_scan_seg(e, blockIdx.x);
+  uint64_t part = 0;
+  for (uint32_t q = e.first[k] + threadIdx.x; q < blockIdx.x; q += blockDim.x) part += tile_sums[q];
+  uint64_t off;
+  block_excl_scan(part, sh, &off);
+  const uint64_t base = (uint64_t)(blockIdx.x - e.first[k]) * kScanTile;
+  uint64_t v[kScanPerThread];
+  uint64_t sum = 0;
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; q++) {
+    const uint64_t i = base + (uint64_t)threadIdx.x * kScanPerThread + q;
+    v[q] = i < e.n[k] ? entry_scan_val(e, k, i, false) : 0;
+    sum += v[q];
+  }
+  uint64_t tile_total;
+  uint64_t ex = block_excl_scan(sum, sh, &tile_total) + off;
+  if (threadIdx.x == 0 && blockIdx.x + 1 == e.first[k + 1]) {
+    if (k == 1) e.a.tot[0] = off + tile_total;
+    if (k == 2) e.a.tot[4] = off + tile_total;
+  }
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; q++) {
+    const uint64_t i = base + (uint64_t)threadIdx.x * kScanPerThread + q;
+    if (i < e.n[k]) {
+      if (k == 0) {
+        e.a.fo_excl[i] = ex;
+      } else if (k == 1) {
+        e.a.dm_excl[i] = ex;
+      } else {
+        StoreShiftExcl{e.a}(i, ex, v[q]);
+      }
+    }
+    ex += v[q];
+  }
+}
+
+// Every (step, key) that a chain step's distinct map (FO entries) or repeat
+// map (shift entries) holds, both entry lists in one launch, each entry cut
+// into segments of up to kSegKeys consecutive keys (one thread each):
+//   * distinct map: the key's position in the step's data section, by a plain
+//     store: the FO entries of one diff are disjoint subtrees (or distinct
+//     chunks), so no two segments of a step share a key;
+//   * repeat map: the entry that the reference inserts first (the lowest
+//     entry index; shift entries as 2h for the root key, 2h+1 for the leaf
+//     keys) through an atomicMax of tag | (2^32-1 - index): the arithmetic
+//     of num_leaf_descendents lets ranges of one step overlap when the leaf
+//     count is not a power of two.  `tag` is this restart's epoch in the
+//     high word, so a cell written by an earlier restart loses to any write
+//     of this one and needs no clearing pass;
+//   * per 32-key word, bitmaps of the steps' maps that hold each key
+//     ([word][step][dm, rm], cleared for every restart): one or two atomicOr
+//     per segment.
+// A malformed chain whose FO entries of one step overlap gets one of them
+// for the shared keys (the reference keeps the first).
+__device__ __forceinline__ void seg_bits(const RArgs& a, uint32_t s, int d, uint32_t k0, uint32_t lo, uint32_t hi) {
+  uint32_t* base = a.sbm + (uint64_t)s * 2 + d;
+  const uint64_t stride = (uint64_t)a.W * 64;  // words per 32-key word row
+  if (lo) atomicOr(base + (uint64_t)(k0 >> 5) * stride, lo);
+  if (hi) atomicOr(base + (uint64_t)((k0 >> 5) + 1) * stride, hi);
+}
+constexpr uint32_t kChainTile = 256;
 __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a) {
-  __shared__ ExpandTile T;
+  // tiles of one segment per thread: many small tiles keep every SM busy
+  // (the per-segment work is a chain of dependent loads)
+  __shared__ ExpandTile<kChainTile> T;
   if (a.nsteps == 0) return;
-  const uint64_t rbase = a.tot[3];  // repeat-map items are numbered from here
-  const TwoLists L(a.tot[0], a.tot[4] - rbase);
+  const uint64_t rbase = a.tot[3];  // repeat-map segments are numbered from here
+  const TwoLists<kChainTile> L(a.tot[0], a.tot[4] - rbase);
   const bool tree = a.approach == APPROACH_TREE;
+  const uint32_t leaf0 = a.N - 1;
   for (uint64_t tile = blockIdx.x; tile < L.tiles(); tile += gridDim.x) {
     const bool rm = tile >= L.nt0;
     const uint64_t total = rm ? L.tot1 : L.tot0, base = rm ? rbase : 0;
-    const uint64_t t0 = (rm ? tile - L.nt0 : tile) * kExpandTile;
-    const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
+    const uint64_t t0 = (rm ? tile - L.nt0 : tile) * kChainTile;
+    const uint64_t t1 = t0 + kChainTile < total ? t0 + kChainTile : total;
     const uint64_t* excl = rm ? a.sh_excl + a.sh_cb : a.dm_excl;
     const uint32_t n = rm ? a.nsh - a.sh_cb : a.nfo - a.fo_cb;
     expand_stage(T, excl, n, base + t0, base + t1);
-    for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-      uint64_t j;
-      const uint32_t k = expand_entry(T, excl, n, base + t, &j);
-      uint32_t key, s, idx;
-      if (!rm) {
+    const uint32_t lane = threadIdx.x & 31;
+    // whole warps step together (the fast path below is a warp operation)
+    for (uint64_t tw = t0 + (threadIdx.x & ~31u); tw < t1; tw += blockDim.x) {
+      const uint64_t t = tw + lane;
+      const bool in = t < t1;
+      uint32_t k = 0, j = 0;
+      if (in) {
+        uint64_t j64;
+        k = expand_entry(T, excl, n, base + t, &j64);
+        j = (uint32_t)j64;
+      }
+      uint32_t lo = 0, hi = 0, k0 = 0;
+      if (!rm && tree) {
+        // a distinct-map segment: leaves x0 .. x0 + cnt - 1 of entry g
         const uint32_t g = a.fo_cb + k;
-        s = a.fo_seg[g] - 1;
-        idx = g;
-        const uint4 r = a.fo_rng[g];
-        if (tree) {
-          const uint32_t x = j < r.y ? r.x + (uint32_t)j : r.z + (uint32_t)(j - r.y);
-          key = key_of_leaf(a, x);
-        } else {
-          key = r.x;
-          if (key >= a.N) continue;
+        uint32_t s = 0, x0 = 0, cnt = 0, pos0 = 0;
+        if (in) {
+          s = a.fo_seg[g] - 1;
+          const uint4 r = a.fo_rng[g];
+          const uint32_t n0 = segs_of(r.y);
+          x0 = j < n0 ? r.x + j * kSegKeys : r.z + (j - n0) * kSegKeys;
+          const uint32_t left = j < n0 ? r.y - j * kSegKeys : r.w - (j - n0) * kSegKeys;
+          cnt = left < kSegKeys ? left : kSegKeys;
+          // position of leaf x in the step's data: fo_clen + x - leftmost leaf
+          pos0 = a.fo_clen[g] + x0 - leftmost_leaf(a.fo_node[g], a.M);
         }
+        k0 = x0 - leaf0;
+        // 32 full, 32-key aligned, consecutive segments of one entry (the
+        // large regions): the warp writes them together, coalesced, and sets
+        // whole bitmap words
+        const uint32_t g0 = __shfl_sync(0xffffffffu, g, 0), k00 = __shfl_sync(0xffffffffu, k0, 0);
+        const bool uni = __all_sync(0xffffffffu, in && cnt == kSegKeys && (k0 & 31) == 0 && g == g0 &&
+                                                   k0 == k00 + kSegKeys * lane);
+        if (uni) {
+          const uint32_t p00 = __shfl_sync(0xffffffffu, pos0, 0);
+          uint32_t* cell = a.dm_off + (uint64_t)s * a.K + k00;
+#pragma unroll 4
+          for (uint32_t q = 0; q < kSegKeys; q++) cell[q * 32 + lane] = p00 + q * 32 + lane;
+          atomicOr(a.sbm + (uint64_t)((k00 >> 5) + lane) * a.W * 64 + (uint64_t)s * 2, ~0u);
+          continue;
+        }
+        if (!in) continue;
+        uint32_t* cell = a.dm_off + (uint64_t)s * a.K;
+        for (uint32_t q = 0; q < cnt; q++) cell[k0 + q] = pos0 + q;
+        const uint64_t m = (cnt == 32 ? ~0ull >> 32 : ((1ull << cnt) - 1)) << (k0 & 31);
+        seg_bits(a, s, 0, k0, (uint32_t)m, (uint32_t)(m >> 32));
+        continue;
+      }
+      if (!in) continue;
+      if (!rm) {
+        // list / basic: one chunk per entry
+        const uint32_t g = a.fo_cb + k;
+        const uint32_t s = a.fo_seg[g] - 1;
+        const uint4 r = a.fo_rng[g];
+        if (r.x >= a.N) continue;
+        k0 = r.x;
+        a.dm_off[(uint64_t)s * a.K + k0] = a.fo_clen[g];
+        lo = 1u << (k0 & 31);
+        seg_bits(a, s, 0, k0, lo, hi);
       } else {
         const uint32_t h = a.sh_cb + k;
-        s = a.sh_seg[h] - 1;
-        if (tree) {
+        const uint32_t s = a.sh_seg[h] - 1;
+        unsigned long long* cell = reinterpret_cast<unsigned long long*>(a.rm_tab + (uint64_t)s * a.K);
+        if (!tree) {
+          k0 = a.sh_node[h];
+          if (k0 >= a.N) continue;
+          atomicMax(cell + k0, a.tag | (0xffffffffull - 2ull * h));
+          lo = 1u << (k0 & 31);
+        } else {
           const uint32_t node = a.sh_node[h];
           const uint32_t len = num_leaf_descendents(node, a.M);
-          if (j < len) {
-            const uint32_t x = leftmost_leaf(node, a.M) + (uint32_t)j;
-            if (x < a.N - 1 || x > a.M) continue;
-            key = key_of_leaf(a, x);
-            idx = 2 * h + 1;
+          const uint32_t nseg = segs_of(len);
+          uint32_t x0, cnt;
+          unsigned long long v;
+          if (j < nseg) {
+            x0 = leftmost_leaf(node, a.M) + j * kSegKeys;
+            cnt = len - j * kSegKeys < kSegKeys ? len - j * kSegKeys : kSegKeys;
+            v = a.tag | (0xffffffffull - (2ull * h + 1));
           } else {
-            key = key_of_leaf(a, node);
-            idx = 2 * h;
+            x0 = node;
+            cnt = 1;
+            v = a.tag | (0xffffffffull - 2ull * h);
           }
-        } else {
-          key = a.sh_node[h];
-          if (key >= a.N) continue;
-          idx = 2 * h;
+          // keys of the segment in [N-1, M]; they span at most two words
+          uint32_t a0 = x0 > leaf0 ? x0 : leaf0;
+          uint64_t a1 = (uint64_t)x0 + cnt;  // exclusive
+          if (a1 > (uint64_t)a.M + 1) a1 = (uint64_t)a.M + 1;
+          if ((uint64_t)a0 >= a1) continue;
+          k0 = x0 >= leaf0 ? x0 - leaf0 : 0;
+          for (uint32_t x = a0; x < (uint32_t)a1; x++) {
+            const uint32_t key = x - leaf0;
+            atomicMax(cell + key, v);
+            if ((key >> 5) == (k0 >> 5)) lo |= 1u << (key & 31);
+            else hi |= 1u << (key & 31);
+          }
         }
+        seg_bits(a, s, 1, k0, lo, hi);
       }
-      unsigned long long* cell =
-          reinterpret_cast<unsigned long long*>((rm ? a.rm_tab : a.dm_tab) + (uint64_t)s * a.K + key);
-      atomicMax(cell, a.tag | (0xffffffffull - idx));
-      atomicOr((rm ? a.rm_mask : a.dm_mask) + (uint64_t)key * a.W + (s >> 5), 1u << (s & 31));
     }
     __syncthreads();
   }
 }
 
-// entry index stored in a chain table cell
+// 32 x 32 bit transpose across a warp: lane i holds row i on entry, column
+// `lane` on return (bit i of the result = bit `lane` of row i).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int r = 0; r < 5; r++) {
+    const uint32_t jj = 16u >> r, m = masks[r];
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, jj);
+    x = (lane & jj) ? ((x & ~m) | ((y >> jj) & m)) : ((x & m) | ((y << jj) & ~m));
+  }
+  return x;
+}
+
+// Masks of the warp's own 32 keys for the first 32 steps, by one coalesced
+// load and a transpose; lane l gets key 32w + l (the chunk's own key).
+struct OwnMasks {
+  uint32_t key;  // the key they belong to
+  uint2 m;       // {dm, rm} bits of steps 0..31
+};
+
+// The {dm, rm} bits of `key` at step s (one word pair of its 32-key row).
+__device__ __forceinline__ uint32_t key_bits(const RArgs& a, uint32_t key, uint32_t s) {
+  const uint2 v = reinterpret_cast<const uint2*>(a.sbm)[((uint64_t)(key >> 5) * a.W * 32) + s];
+  const uint32_t b = key & 31;
+  return ((v.x >> b) & 1u) | (((v.y >> b) & 1u) << 1);
+}
+
+// The first step at or after s whose distinct (bit 0) or repeat (bit 1) map
+// holds `key`: from the warp's own masks, or by probing the key's row step by
+// step (a key reached through a shifted duplicate).  nsteps when none.
+__device__ __forceinline__ uint32_t next_step(const RArgs& a, const OwnMasks& own, uint32_t key, uint32_t s,
+                                              bool* in_dm) {
+  if (key == own.key && a.nsteps <= 32) {
+    const uint32_t m = (own.m.x | own.m.y) & (s < 32 ? ~0u << s : 0u);
+    if (!m) return a.nsteps;
+    const uint32_t f = __ffs(m) - 1;
+    *in_dm = (own.m.x >> f) & 1u;
+    return f;
+  }
+  for (; s < a.nsteps; s++) {
+    const uint32_t b = key_bits(a, key, s);
+    if (b) {
+      *in_dm = b & 1u;
+      return s;
+    }
+  }
+  return a.nsteps;
+}
+
+// entry index stored in a repeat-map cell
 __device__ __forceinline__ uint32_t cell_index(uint64_t v) { return 0xffffffffu - (uint32_t)v; }
 
-// offset of leaf/chunk x in step s's data through its distinct map (the
-// caller has seen the step's mask bit for x), or kNone
-__device__ __forceinline__ uint64_t chain_dm_offset(const RArgs& a, uint32_t s, uint32_t x, uint32_t key) {
-  const uint32_t g = cell_index(a.dm_tab[(uint64_t)s * a.K + key]);
-  // list and basic: one chunk per entry, fo_clen = its position in the data
-  if (a.approach != APPROACH_TREE) return (uint64_t)a.fo_clen[g] * a.cs;
-  return (uint64_t)(uint32_t)(a.fo_clen[g] + x - leftmost_leaf(a.fo_node[g], a.M)) * a.cs;
+// offset of leaf/chunk x (key `key`) in step s's data through its distinct
+// map (the caller has seen the step's mask bit for the key)
+__device__ __forceinline__ uint64_t chain_dm_offset(const RArgs& a, uint32_t s, uint32_t key) {
+  return (uint64_t)a.dm_off[(uint64_t)s * a.K + key] * a.cs;
 }
 __device__ __forceinline__ bool dm_has(const RArgs& a, uint32_t s, uint32_t key) {
-  return (a.dm_mask[(uint64_t)key * a.W + (s >> 5)] >> (s & 31)) & 1u;
+  return key_bits(a, key, s) & 1u;
 }
 
 // 4. where chunk c's bytes come from: node_list and the first copy source
@@ -547,7 +781,8 @@ __device__ __forceinline__ bool dm_has(const RArgs& a, uint32_t s, uint32_t key)
 //    down the chain (src/tree_approach.cpp:1083-1118,
 //    src/list_approach.cpp:520-567, src/basic_approach.cpp:293-312).
 //    seg 0 is the main diff; off = kNone: the reference writes nothing.
-__device__ __forceinline__ void resolve_chunk(const RArgs& a, uint64_t c, uint32_t& seg, uint64_t& off) {
+__device__ __forceinline__ void resolve_chunk(const RArgs& a, const OwnMasks& own, uint64_t c, uint32_t& seg,
+                                              uint64_t& off) {
   const uint32_t cur = a.cur_main;
   const bool tree = a.approach == APPROACH_TREE;
   const uint64_t nr0 = a.nl_rank[c], cr0 = a.cp_rank[c];
@@ -600,24 +835,13 @@ __device__ __forceinline__ void resolve_chunk(const RArgs& a, uint64_t c, uint32
       key = x;
     }
     // next step at or below t that mentions this key
-    uint32_t s = id0 - t, found = 0xffffffffu;
     bool in_dm = false;
-    for (uint32_t w = s >> 5; w < a.W; w++) {
-      const uint32_t dmw = a.dm_mask[(uint64_t)key * a.W + w], rmw = a.rm_mask[(uint64_t)key * a.W + w];
-      uint32_t m = dmw | rmw;
-      if (w == (s >> 5)) m &= ~0u << (s & 31);
-      if (m) {
-        const uint32_t b = __ffs(m) - 1;
-        found = w * 32 + b;
-        in_dm = (dmw >> b) & 1u;
-        break;
-      }
-    }
+    const uint32_t found = next_step(a, own, key, id0 - t, &in_dm);
     if (found >= a.nsteps) break;  // never mentioned again: left as is
-    s = found;
+    const uint32_t s = found;
     const uint32_t ts = id0 - s;
     if (in_dm) {
-      const uint64_t o = chain_dm_offset(a, s, x, key);
+      const uint64_t o = chain_dm_offset(a, s, key);
       if (o < (1ull << kOffBits)) { seg = 1 + s; off = o; }
       break;
     }
@@ -639,7 +863,7 @@ __device__ __forceinline__ void resolve_chunk(const RArgs& a, uint64_t c, uint32
         pkey = pnode;
       }
       if (ok && dm_has(a, s, pkey)) {
-        const uint64_t o2 = chain_dm_offset(a, s, pnode, pkey);
+        const uint64_t o2 = chain_dm_offset(a, s, pkey);
         if (o2 < (1ull << kOffBits)) { seg = 1 + s; off = o2; }
       }
       break;
@@ -742,13 +966,14 @@ __device__ __forceinline__ void copy_tile(const RArgs& a, uint64_t c0, const uin
 
 // Where chunk c of a tile comes from: a source address and byte count (0:
 // the chunk is not written).
-__device__ __forceinline__ void chunk_source(const RArgs& a, uint64_t c, const uint8_t*& src, uint32_t& nb) {
+__device__ __forceinline__ void chunk_source(const RArgs& a, const OwnMasks& own, uint64_t c, const uint8_t*& src,
+                                             uint32_t& nb) {
   src = nullptr;
   nb = 0;
   if (c >= a.N) return;
   uint32_t seg;
   uint64_t off;
-  resolve_chunk(a, c, seg, off);
+  resolve_chunk(a, own, c, seg, off);
   if (off == kNone) return;
   const DiffInfo& d = a.di[seg];
   const uint64_t o = d.data_off + off;
@@ -764,13 +989,29 @@ __device__ __forceinline__ void chunk_source(const RArgs& a, uint64_t c, const u
 // 4. Every chunk's source address and byte count, in a pass of its own: the
 // walks' dependent loads want all the warps an SM can hold, the copy wants
 // bytes in flight per warp.
-__global__ void __launch_bounds__(256, 8) resolve_kernel(RArgs a) {
-  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.N; c += (uint64_t)gridDim.x * blockDim.x) {
-    const uint8_t* src;
-    uint32_t nb;
-    chunk_source(a, c, src, nb);
-    a.srcp[c] = reinterpret_cast<uint64_t>(src);
-    a.nbv[c] = nb;
+// Whole warps take 32 consecutive chunks at a time: the warp's own keys'
+// step masks come from one coalesced load and a transpose per 32 steps.
+__global__ void __launch_bounds__(256, 6) resolve_kernel(RArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint2* bm = reinterpret_cast<const uint2*>(a.sbm);
+  for (uint64_t cw = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); cw < a.N; cw += stride) {
+    const uint64_t c = cw + lane;
+    OwnMasks own;
+    own.key = (uint32_t)c;  // chunk c's own key (tree: leaf N-1+c, list: chunk c)
+    own.m = make_uint2(0, 0);
+    if (a.nsteps) {
+      const uint32_t st = lane;
+      const uint2 v = st < a.nsteps ? bm[(cw >> 5) * a.W * 32 + st] : make_uint2(0, 0);
+      own.m = make_uint2(warp_transpose32(v.x), warp_transpose32(v.y));
+    }
+    if (c < a.N) {
+      const uint8_t* src;
+      uint32_t nb;
+      chunk_source(a, own, c, src, nb);
+      a.srcp[c] = reinterpret_cast<uint64_t>(src);
+      a.nbv[c] = nb;
+    }
   }
 }
 
@@ -804,14 +1045,13 @@ inline uint32_t gsz(uint64_t n, int threads = 256, int per_sm = 8) {
 // Restart scratch owned by the engine between calls.
 struct RestartScratch {
   DevBuf<DiffInfo> di;
-  DevBuf<uint32_t> fo_node, fo_seg, fo_clen, sh_node, sh_prev, sh_tree, sh_seg, rrs, fo_at, dm_mask, rm_mask;
-  DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl_rank, cp_rank, dm_excl, tot, scan, scan_total, dm_tab, rm_tab,
-      srcp;
+  DevBuf<uint32_t> fo_node, fo_seg, fo_clen, sh_node, sh_prev, sh_tree, sh_seg, rrs, fo_at, dm_off, sbm;
+  DevBuf<uint64_t> fo_excl, sh_off, sh_excl, nl_rank, cp_rank, dm_excl, tot, scan, scan_total, rm_tab, srcp;
   DevBuf<uint32_t> nbv;
   DevBuf<uint4> fo_rng;
-  // epochs: chain table cells and the main scatter ranks hold the epoch of
-  // the restart that wrote them; the four buffers are zeroed when one of them
-  // is (re)allocated or the epoch reaches 2^30
+  // epochs: repeat-map cells and the main scatter ranks hold the epoch of
+  // the restart that wrote them; the three buffers are zeroed when one of
+  // them is (re)allocated or the epoch reaches 2^30
   uint32_t epoch = 0;
   const void* seen[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -869,10 +1109,10 @@ uint64_t Engine::restart_scratch_bytes() const {
   const RestartScratch& R = *rs_;
   uint64_t b = sizeof(DiffInfo) * R.di.n + sizeof(uint4) * R.fo_rng.n;
   for (const auto* x : {&R.fo_node, &R.fo_seg, &R.fo_clen, &R.sh_node, &R.sh_prev, &R.sh_tree, &R.sh_seg, &R.rrs,
-                        &R.fo_at, &R.dm_mask, &R.rm_mask, &R.nbv})
+                        &R.fo_at, &R.dm_off, &R.sbm, &R.nbv})
     b += sizeof(uint32_t) * x->n;
   for (const auto* x : {&R.fo_excl, &R.sh_off, &R.sh_excl, &R.nl_rank, &R.cp_rank, &R.dm_excl, &R.tot, &R.scan,
-                        &R.scan_total, &R.dm_tab, &R.rm_tab, &R.srcp})
+                        &R.scan_total, &R.rm_tab, &R.srcp})
     b += sizeof(uint64_t) * x->n;
   return b;
 }
@@ -881,10 +1121,10 @@ static void set_scratch_pool(RestartScratch* r, cudaMemPool_t pool) {
   r->di.pool = pool;
   r->fo_rng.pool = pool;
   for (auto* b : {&r->fo_node, &r->fo_seg, &r->fo_clen, &r->sh_node, &r->sh_prev, &r->sh_tree, &r->sh_seg, &r->rrs,
-                  &r->fo_at, &r->dm_mask, &r->rm_mask})
+                  &r->fo_at, &r->dm_off, &r->sbm})
     b->pool = pool;
   for (auto* b : {&r->fo_excl, &r->sh_off, &r->sh_excl, &r->nl_rank, &r->cp_rank, &r->dm_excl, &r->tot,
-                  &r->scan, &r->scan_total, &r->dm_tab, &r->rm_tab, &r->srcp})
+                  &r->scan, &r->scan_total, &r->rm_tab, &r->srcp})
     b->pool = pool;
   r->nbv.pool = pool;
 }
@@ -1011,25 +1251,24 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(R.fo_at.ensure((size_t)M + 2, s));
   MTC_CUDA_R(R.dm_excl.ensure(nfo + 1, s));
   MTC_CUDA_R(R.tot.ensure(5, s));
-  MTC_CUDA_R(R.dm_tab.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
+  const uint32_t KW = (K + 31) / 32;
+  MTC_CUDA_R(R.dm_off.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
   MTC_CUDA_R(R.rm_tab.ensure((size_t)std::max<uint32_t>(nsteps, 1) * K, s));
-  if (R.dm_tab.p != R.seen[0] || R.rm_tab.p != R.seen[1] || R.nl_rank.p != R.seen[2] || R.cp_rank.p != R.seen[3] ||
+  MTC_CUDA_R(R.sbm.ensure((size_t)KW * W * 32 * 2, s));
+  if (R.rm_tab.p != R.seen[1] || R.nl_rank.p != R.seen[2] || R.cp_rank.p != R.seen[3] ||
       R.epoch >= (1u << 30) - 1) {
-    MTC_CUDA_R(cudaMemsetAsync(R.dm_tab.p, 0, sizeof(uint64_t) * R.dm_tab.n, s));
     MTC_CUDA_R(cudaMemsetAsync(R.rm_tab.p, 0, sizeof(uint64_t) * R.rm_tab.n, s));
     MTC_CUDA_R(cudaMemsetAsync(R.nl_rank.p, 0, sizeof(uint64_t) * R.nl_rank.n, s));
     MTC_CUDA_R(cudaMemsetAsync(R.cp_rank.p, 0, sizeof(uint64_t) * R.cp_rank.n, s));
-    R.seen[0] = R.dm_tab.p;
     R.seen[1] = R.rm_tab.p;
     R.seen[2] = R.nl_rank.p;
     R.seen[3] = R.cp_rank.p;
     R.epoch = 0;
   }
   R.epoch++;
-  MTC_CUDA_R(R.dm_mask.ensure((size_t)K * W, s));
-  MTC_CUDA_R(R.rm_mask.ensure((size_t)K * W, s));
   const uint64_t scan_n = std::max<uint64_t>(nfo, nsh) + 1;
-  MTC_CUDA_R(R.scan.ensure(scan_n / kScanTile + 2, s));
+  // tile sums: one scan at a time, or the three entry scans side by side
+  MTC_CUDA_R(R.scan.ensure(3 * (scan_n / kScanTile + 2), s));
   MTC_CUDA_R(R.scan_total.ensure(1, s));
   MTC_CUDA_R(err_.ensure(1, s));
   MTC_CUDA_R(cudaMemsetAsync(err_.p, 0, sizeof(uint32_t), s));
@@ -1052,7 +1291,7 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   a.nl_rank = R.nl_rank.p; a.cp_rank = R.cp_rank.p;
   a.srcp = R.srcp.p; a.nbv = R.nbv.p;
   a.fo_at = R.fo_at.p;
-  a.dm_tab = R.dm_tab.p; a.rm_tab = R.rm_tab.p; a.dm_mask = R.dm_mask.p; a.rm_mask = R.rm_mask.p;
+  a.dm_off = R.dm_off.p; a.rm_tab = R.rm_tab.p; a.sbm = R.sbm.p; a.KW = KW;
   a.dm_excl = R.dm_excl.p; a.tot = R.tot.p;
   a.fo_rng = R.fo_rng.p;
   a.out = dev_out; a.err = err_.p;
@@ -1064,11 +1303,33 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   rrs_kernel<<<gsz(di.size(), 1, 4), 256, 0, s>>>(a);
   note_launch();
   if (nsh) { shift_tree_kernel<<<gsz(nsh), 256, 0, s>>>(a); note_launch(); }
-  // chunk_len of every FO entry within its own diff; the main checkpoint's
-  // FO items (tot[2])
+  const uint32_t nfo_chain = nsteps ? nfo - a.fo_cb : 0;
+  const uint64_t tiles[3] = {(nfo + kScanTile - 1) / kScanTile, (nfo_chain + kScanTile - 1) / kScanTile,
+                             (nsh + kScanTile - 1) / kScanTile};
+  const bool fused = tiles[0] <= reduce_tile_limit() && tiles[1] <= reduce_tile_limit() &&
+                     tiles[2] <= reduce_tile_limit() && tiles[0] + tiles[1] + tiles[2] > 0;
+  if (fused) {
+    // the three entry scans in one pair of launches
+    EntryScans e{a, {nfo, nfo_chain, nsh}, {0, (uint32_t)tiles[0], (uint32_t)(tiles[0] + tiles[1]),
+                                            (uint32_t)(tiles[0] + tiles[1] + tiles[2])}};
+    entry_scan_sums_kernel<<<e.first[3], kScanThreads, 0, s>>>(e, R.scan.p);
+    entry_scan_emit_kernel<<<e.first[3], kScanThreads, 0, s>>>(e, R.scan.p);
+    note_launch(2);
+  } else {
+    // chunk_len of every FO entry within its own diff
+    if (nfo) MTC_CUDA_R(grid_scan(FoLen{R.fo_node.p, M, tree ? 1 : 0}, StoreExcl{R.fo_excl.p}, nullptr, nfo,
+                                  R.scan.p, R.scan_total.p, s));
+    // items of the main shift regions and of the chain's repeat maps
+    if (nsh) MTC_CUDA_R(grid_scan(ShiftItems{a}, StoreShiftExcl{a}, nullptr, nsh, R.scan.p, R.tot.p + 4, s));
+    if (nfo_chain) {
+      chain_ranges_kernel<<<gsz(nfo_chain), 256, 0, s>>>(a, nfo_chain);
+      note_launch();
+      MTC_CUDA_R(grid_scan(ChainDmCount{a}, StoreExcl{R.dm_excl.p}, nullptr, nfo_chain, R.scan.p, R.tot.p + 0, s));
+    }
+  }
+  // chunk_len relative to each FO entry's own diff; the main checkpoint's FO
+  // items (tot[2])
   if (nfo) {
-    MTC_CUDA_R(grid_scan(FoLen{R.fo_node.p, M, tree ? 1 : 0}, StoreExcl{R.fo_excl.p}, nullptr, nfo, R.scan.p,
-                         R.scan_total.p, s));
     clen_kernel<<<gsz(nfo), 256, 0, s>>>(a);
     note_launch();
   }
@@ -1079,22 +1340,13 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     main_shift_kernel<<<gsz(di[0].S), 256, 0, s>>>(a);
     note_launch();
   }
-  // items of the main shift regions and of the chain's repeat maps
-  if (nsh) MTC_CUDA_R(grid_scan(ShiftItems{a}, StoreShiftExcl{a}, nullptr, nsh, R.scan.p, R.tot.p + 4, s));
   if (di[0].F || di[0].S) {
     main_cover_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
     note_launch();
   }
   // chain
   if (nsteps) {
-    MTC_CUDA_R(cudaMemsetAsync(R.dm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
-    MTC_CUDA_R(cudaMemsetAsync(R.rm_mask.p, 0, sizeof(uint32_t) * (size_t)K * W, s));
-    const uint32_t nfo_chain = nfo - a.fo_cb;
-    if (nfo_chain) {
-      chain_ranges_kernel<<<gsz(nfo_chain), 256, 0, s>>>(a, nfo_chain);
-      note_launch();
-      MTC_CUDA_R(grid_scan(ChainDmCount{a}, StoreExcl{R.dm_excl.p}, nullptr, nfo_chain, R.scan.p, R.tot.p + 0, s));
-    }
+    MTC_CUDA_R(cudaMemsetAsync(R.sbm.p, 0, sizeof(uint32_t) * (size_t)KW * W * 32 * 2, s));
     chain_tables_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
     note_launch();
   }
