@@ -22,6 +22,7 @@ static __global__ void set_word_kernel(uint32_t* p, uint32_t v) { *p = v; }
 // memory behind it on the link.  A replayed graph gets each step's values
 // by an update of this node (Engine::replay_own).
 static __global__ void params_in_kernel(StepParams p, StepParams* dev, uint32_t* err) {
+  pdl_enter();
   if (threadIdx.x == 0) {
     *dev = p;
     *err = 0;
@@ -365,7 +366,7 @@ int Engine::enqueue(const uint8_t* data, uint64_t len, bool timed) {
   if (params_by_value_) {
     static const bool reg = (register_input_kernel(reinterpret_cast<const void*>(params_in_kernel), INPUT_PARAMS), true);
     (void)reg;
-    params_in_kernel<<<1, 32, 0, stream_>>>(*sp_host_, sp_.p, err_.p);
+    launch_k(params_in_kernel, 1, 32, 0, stream_, *sp_host_, sp_.p, err_.p);
     note_launch();
     MTC_CUDA(cudaGetLastError());
   } else {

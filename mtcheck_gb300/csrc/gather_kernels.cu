@@ -164,6 +164,7 @@ __device__ __forceinline__ int resolve_pass(const ForestArgs& a, int pass) {
 // levels below it.
 __global__ void __launch_bounds__(256) forest_span_kernel(ForestArgs a, int pass, int baseline, uint32_t N,
                                                           uint32_t d_top, uint32_t d_bot) {
+  pdl_enter();
   __shared__ uint8_t lab[2][2 << (kSpanLevels - 1)];
   pass = resolve_pass(a, pass);
   if (pass < 0) return;
@@ -332,6 +333,7 @@ __device__ __forceinline__ void upper_levels(const ForestArgs& a, int pass, uint
 // stored: the tree keeps every digest for the next checkpoint).
 template <int HK>
 __global__ void __launch_bounds__(256) forest_span9_warp_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
+  pdl_enter();
   __shared__ uint8_t top8[8];
   __shared__ Digest topdg[8];
   __shared__ uint32_t ids[(1u << kSpanLevels) - 1];  // one per interior node: never overflows
@@ -482,6 +484,7 @@ __device__ __forceinline__ uint8_t thread_levels_bytewise(const ForestArgs& a, i
 // unrolled levels keep the kernel small enough for the instruction cache.
 template <int HK>
 __global__ void __launch_bounds__(256) forest_bottom12_kernel(ForestArgs a, int pass, uint32_t N, uint32_t d_top) {
+  pdl_enter();
   __shared__ uint8_t top8[8];
   __shared__ Digest topdg[8];
   __shared__ uint32_t ids[kBottomSink];
@@ -584,6 +587,7 @@ __device__ __forceinline__ bool forest_fused(const ForestArgs& a) { return a.fus
 // digests up.  A fused pass looks nothing up that these inserts could add,
 // so its inserts wait for the root count (root_count_kernel's extra blocks).
 __global__ void forest_insert_kernel(ForestArgs a) {
+  pdl_enter();
   if (forest_fused(a)) return;
   drain_inserts(a, 0, gridDim.x);
 }
@@ -652,6 +656,7 @@ __device__ __forceinline__ void root_prologue(const uint8_t* labels, uint32_t N,
 __global__ void __launch_bounds__(kScanThreads) root_count_kernel(ForestArgs a, uint32_t N, uint64_t n,
                                                                   uint64_t* tile_sums, uint32_t* fo_list,
                                                                   Layout* lay, uint32_t nd) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   if (blockIdx.x < nd) {
     if (forest_fused(a)) drain_inserts(a, 0, nd);
@@ -673,6 +678,7 @@ __global__ void __launch_bounds__(kScanThreads) root_count_kernel(ForestArgs a, 
 template <bool kReduce>
 __global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, uint64_t n, const uint64_t* tile_off,
                                                                  uint32_t* fo_list, uint32_t* sh_list, Layout* lay) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   uint64_t off = 0;
   if (kReduce) {
@@ -713,6 +719,7 @@ __global__ void __launch_bounds__(kScanThreads) root_emit_kernel(ForestArgs a, u
 }
 
 __global__ void root_epilogue_kernel(const uint64_t* total, Layout* lay) {
+  pdl_enter();
   lay->F = lay->root_fo + (uint32_t)(*total);
   lay->S = (uint32_t)(*total >> 32);
 }
@@ -760,6 +767,7 @@ struct FoEmit {
 // kFoTile) over a persistent grid: the tile count follows F on the device.
 constexpr uint32_t kFoTile = kScanThreads;
 __global__ void __launch_bounds__(kScanThreads) fo_tile_sums_kernel(GatherArgs g) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   const uint32_t F = g.lay->F;
   const uint32_t nt = (F + kFoTile - 1) / kFoTile;
@@ -771,6 +779,7 @@ __global__ void __launch_bounds__(kScanThreads) fo_tile_sums_kernel(GatherArgs g
   }
 }
 __global__ void __launch_bounds__(kScanThreads) fo_emit_kernel(GatherArgs g) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   const uint32_t F = g.lay->F;
   const uint32_t nt = (F + kFoTile - 1) / kFoTile;
@@ -809,6 +818,7 @@ __device__ __forceinline__ void shift_prep(const GatherArgs& g) {
 
 // Both root lists' lookups in one launch.
 __global__ void roots_prep_kernel(GatherArgs g) {
+  pdl_enter();
   shift_prep(g);
   fo_prep(g);
 }
@@ -818,6 +828,7 @@ __global__ void roots_prep_kernel(GatherArgs g) {
 // First, the tile sums of the region-size scan become tile offsets in place,
 // and their total gives the region count and the data chunk count.
 __global__ void layout_kernel(GatherArgs g) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   Layout* lay = g.lay;
   {
@@ -968,6 +979,7 @@ __global__ void layout_kernel(GatherArgs g) {
 // Stable counting sort of the shift entries by representative key.
 // Tile t counts its keys; matrix[key * T + t] (key-major).
 __global__ void sort_count_kernel(GatherArgs g) {
+  pdl_enter();
   extern __shared__ uint32_t cnt[];
   const uint32_t K = g.lay->nkeys, S = g.lay->S, T = g.lay->sort_tiles;
   if (K > kSortFastKeys) return;
@@ -1007,6 +1019,7 @@ struct MatEmit {
 // base (key-major scan of sort_mat) give each entry its position.
 constexpr int kSortWarps = 8;
 __global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g) {
+  pdl_enter();
   __shared__ uint32_t keys[kSortTile];
   __shared__ uint32_t lrank[kSortTile];
   extern __shared__ uint32_t cnt[];  // [kSortWarps][K]
@@ -1087,6 +1100,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(GatherArgs g) {
 // Each block owns a contiguous range of units, so a thread locates its region
 // once by binary search and then walks forward.
 __global__ void copy_kernel(GatherArgs g) {
+  pdl_enter();
   if (!g.lay->ok) return;
   const uint32_t R = g.lay->num_distinct;
   const uint64_t nslots = g.lay->chunk_counter;
@@ -1141,6 +1155,7 @@ __global__ void copy_kernel(GatherArgs g) {
 // Byte-granular gather for chunk sizes that are not multiples of 16 or
 // buffers that are not 16-byte aligned.
 __global__ void copy_bytes_kernel(GatherArgs g) {
+  pdl_enter();
   if (!g.lay->ok) return;
   const uint32_t R = g.lay->num_distinct;
   const uint64_t nslots = g.lay->chunk_counter;
@@ -1181,6 +1196,7 @@ struct ChunkEmit {
   }
 };
 __global__ void chunk_totals_kernel(const uint64_t* total, Layout* lay) {
+  pdl_enter();
   lay->root_fo = 0;
   lay->F = (uint32_t)(*total);
   lay->S = (uint32_t)(*total >> 32);
@@ -1248,8 +1264,8 @@ cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t 
     const uint32_t top = dmax - (kBottomLevels - 1);
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
-    if (a.hash_kind == HASH_MD5) forest_bottom12_kernel<HASH_MD5><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
-    else forest_bottom12_kernel<HASH_MURMUR3><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+    if (a.hash_kind == HASH_MD5) launch_k(forest_bottom12_kernel<HASH_MD5>, (uint32_t)count, 256, 0, s, a, pass, N, top);
+    else launch_k(forest_bottom12_kernel<HASH_MURMUR3>, (uint32_t)count, 256, 0, s, a, pass, N, top);
     note_launch();
     bot = (int)top - 1;
   }
@@ -1258,15 +1274,15 @@ cudaError_t launch_forest(const ForestArgs& a, int pass, int baseline, uint32_t 
     const uint64_t first = (1ull << top) - 1;
     const uint64_t count = std::min<uint64_t>(1ull << top, (uint64_t)N - 1 - first);
     if (!dup_baseline && (uint32_t)bot - top == kSpanLevels - 1)
-      if (a.hash_kind == HASH_MD5) forest_span9_warp_kernel<HASH_MD5><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
-      else forest_span9_warp_kernel<HASH_MURMUR3><<<(uint32_t)count, 256, 0, s>>>(a, pass, N, top);
+      if (a.hash_kind == HASH_MD5) launch_k(forest_span9_warp_kernel<HASH_MD5>, (uint32_t)count, 256, 0, s, a, pass, N, top);
+      else launch_k(forest_span9_warp_kernel<HASH_MURMUR3>, (uint32_t)count, 256, 0, s, a, pass, N, top);
     else
-      forest_span_kernel<<<(uint32_t)count, 256, 0, s>>>(a, pass, baseline, N, top, (uint32_t)bot);
+      launch_k(forest_span_kernel, (uint32_t)count, 256, 0, s, a, pass, baseline, N, top, (uint32_t)bot);
     note_launch();
     if (top == 0) break;
   }
   if (pass == 0) {
-    forest_insert_kernel<<<grid_for(N, 256), 256, 0, s>>>(a);
+    launch_k(forest_insert_kernel, grid_for(N, 256), 256, 0, s, a);
     note_launch();
   }
   return cudaGetLastError();
@@ -1279,15 +1295,15 @@ cudaError_t launch_root_compaction(const ForestArgs& fa, uint32_t N, uint32_t M,
   uint32_t ntiles = (uint32_t)((n + kRootTile - 1) / kRootTile);
   if (ntiles == 0) ntiles = 1;
   const uint32_t nd = 2 * num_sms();
-  root_count_kernel<<<ntiles + nd, kScanThreads, 0, s>>>(fa, N, n, scan_scratch, fo_list, lay, nd);
+  launch_k(root_count_kernel, ntiles + nd, kScanThreads, 0, s, fa, N, n, scan_scratch, fo_list, lay, nd);
   if (ntiles <= reduce_tile_limit()) {
-    root_emit_kernel<true><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
+    launch_k(root_emit_kernel<true>, ntiles, kScanThreads, 0, s, fa, n, scan_scratch, fo_list, sh_list, lay);
     note_launch(2);
     return cudaGetLastError();
   }
-  scan_tile_offsets_kernel<<<1, 1024, 0, s>>>(scan_scratch, ntiles, scan_total);
-  root_emit_kernel<false><<<ntiles, kScanThreads, 0, s>>>(fa, n, scan_scratch, fo_list, sh_list, lay);
-  root_epilogue_kernel<<<1, 1, 0, s>>>(scan_total, lay);
+  launch_k(scan_tile_offsets_kernel, 1, 1024, 0, s, scan_scratch, ntiles, scan_total);
+  launch_k(root_emit_kernel<false>, ntiles, kScanThreads, 0, s, fa, n, scan_scratch, fo_list, sh_list, lay);
+  launch_k(root_epilogue_kernel, 1, 1, 0, s, scan_total, lay);
   note_launch(4);
   return cudaGetLastError();
 }
@@ -1298,7 +1314,7 @@ cudaError_t launch_chunk_compaction(const uint8_t* labels, uint32_t n_chunks, in
   cudaError_t e = grid_scan(ChunkVal{labels, basic}, ChunkEmit{fo_list, sh_list}, nullptr, n_chunks, scan_scratch,
                             scan_total, s);
   if (e != cudaSuccess) return e;
-  chunk_totals_kernel<<<1, 1, 0, s>>>(scan_total, lay);
+  launch_k(chunk_totals_kernel, 1, 1, 0, s, scan_total, lay);
   note_launch();
   return cudaGetLastError();
 }
@@ -1311,12 +1327,12 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
   // FO emit (metadata + regions), sort, copy.
   cudaMemsetAsync(g.hist, 0, sizeof(uint32_t) * (size_t)g.k_cap, s);
   const uint32_t gs = grid_for(max_entries, 256);
-  roots_prep_kernel<<<gs, 256, 0, s>>>(g);
+  launch_k(roots_prep_kernel, gs, 256, 0, s, g);
   // region totals first (phase 1+2 of the scan), then layout, then emit
   const uint32_t gfo = (uint32_t)std::min<uint64_t>((max_entries + kFoTile - 1) / kFoTile + 1, 4ull * num_sms());
-  fo_tile_sums_kernel<<<gfo, kScanThreads, 0, s>>>(g);
-  layout_kernel<<<1, 1024, 0, s>>>(g);
-  fo_emit_kernel<<<gfo, kScanThreads, 0, s>>>(g);
+  launch_k(fo_tile_sums_kernel, gfo, kScanThreads, 0, s, g);
+  launch_k(layout_kernel, 1, 1024, 0, s, g);
+  launch_k(fo_emit_kernel, gfo, kScanThreads, 0, s, g);
   note_launch(4);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (g.approach != APPROACH_BASIC) {
@@ -1333,19 +1349,19 @@ cudaError_t launch_assemble(const GatherArgs& g, uint64_t max_entries, cudaStrea
     }
     // tiles of the actual shift entries, read on the device: small grids
     const uint32_t gsort = std::min<uint32_t>(T, 2 * num_sms());
-    sort_count_kernel<<<gsort, 256, smem_cnt, s>>>(g);
+    launch_k(sort_count_kernel, gsort, 256, smem_cnt, s, g);
     e = grid_scan(MatVal{g.sort_mat}, MatEmit{g.sort_mat}, &g.lay->sort_n, (uint64_t)K * T, g.scan_scratch2,
                   g.scan_total2, s);
     if (e != cudaSuccess) return e;
-    sort_scatter_kernel<<<gsort, 256, smem_sc, s>>>(g);
+    launch_k(sort_scatter_kernel, gsort, 256, smem_sc, s, g);
     note_launch(2);
   }
   const bool vec = (g.cs % 16 == 0) && ((reinterpret_cast<uintptr_t>(g.data) & 15) == 0);
   static const bool reg = (register_input_kernel(reinterpret_cast<const void*>(copy_kernel), INPUT_GATHER),
                            register_input_kernel(reinterpret_cast<const void*>(copy_bytes_kernel), INPUT_GATHER), true);
   (void)reg;
-  if (vec) copy_kernel<<<num_sms() * 8, 256, 0, s>>>(g);
-  else copy_bytes_kernel<<<num_sms() * 8, 256, 0, s>>>(g);
+  if (vec) launch_k(copy_kernel, num_sms() * 8, 256, 0, s, g);
+  else launch_k(copy_bytes_kernel, num_sms() * 8, 256, 0, s, g);
   note_launch();
   return cudaGetLastError();
 }

@@ -14,6 +14,7 @@
 //   list  -- src/list_approach.cpp:38-61
 //   basic -- src/basic_approach.cpp:25-46
 #include <cstdio>
+#include <cstdlib>
 #include <atomic>
 #include <mutex>
 #include <utility>
@@ -103,6 +104,7 @@ __device__ __forceinline__ void note_dup(const LeafArgs& a, uint32_t note) {
 // entry waits for nothing after its claim.
 template <int EPI>
 __global__ void leaf_insert_kernel(LeafArgs a) {
+  pdl_enter();
   const uint32_t n = *a.changed_count;
   const uint32_t cur = a.sp->cur, epoch = a.sp->epoch;
   uint32_t created = 0;
@@ -155,6 +157,7 @@ __device__ __forceinline__ void demote_chunk(const LeafArgs& a, uint32_t c, cons
   }
 }
 __global__ void leaf_demote_kernel(LeafArgs a) {
+  pdl_enter();
   const uint32_t n = min(*a.dup_count, a.dup_cap);
   const uint32_t cur = a.sp->cur;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -178,6 +181,7 @@ __device__ __forceinline__ bool needs_old(const LeafArgs& a) {
 template <int HK, int EPI, int W, int kRows>
 __global__ void __launch_bounds__(kRows + 32, 2) leaf_tma_kernel(const __grid_constant__ CUtensorMap tmap, LeafArgs a,
                                                               uint32_t n_full) {
+  pdl_enter();
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr uint32_t kStageBytes = kRows * W;
@@ -290,6 +294,7 @@ __global__ void __launch_bounds__(kRows + 32, 2) leaf_tma_kernel(const __grid_co
 // ---------------------------------------------------------------------------
 template <int EPI>
 __global__ void leaf_direct_kernel(LeafArgs a, uint32_t c0, uint32_t c1) {
+  pdl_enter();
   for (uint64_t c = c0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < c1; c += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t off = c * (uint64_t)a.cs;
     uint64_t nb = a.cs;
@@ -363,7 +368,7 @@ cudaError_t launch_tma_t(const LeafArgs& a, const CUtensorMap& m, uint32_t n_ful
   if (per_sm > fit) per_sm = fit > 0 ? fit : 1;
   uint32_t grid = (uint32_t)(num_sms() * per_sm);
   if (grid > ntiles) grid = ntiles;
-  k<<<grid, R + 32, smem, s>>>(m, a, n_full);
+  launch_k(k, grid, R + 32, smem, s, m, a, n_full);
   note_launch();
   return cudaGetLastError();
 }
@@ -399,7 +404,7 @@ cudaError_t launch_direct(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStrea
   static const bool reg =
       (register_input_kernel(reinterpret_cast<const void*>(leaf_direct_kernel<EPI>), INPUT_LEAF_DIRECT), true);
   (void)reg;
-  leaf_direct_kernel<EPI><<<grid, 128, 0, s>>>(a, c0, c1);
+  launch_k(leaf_direct_kernel<EPI>, grid, 128, 0, s, a, c0, c1);
   note_launch();
   return cudaGetLastError();
 }
@@ -443,6 +448,19 @@ int input_kernel_kind(const void* func) {
   return INPUT_NONE;
 }
 
+namespace {
+thread_local int t_pdl_suppress = 0;
+}  // namespace
+PdlSuppress::PdlSuppress() { t_pdl_suppress++; }
+PdlSuppress::~PdlSuppress() { t_pdl_suppress--; }
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("MTCHECK_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on && t_pdl_suppress == 0;
+}
+
 static std::atomic<uint64_t> g_launches{0};
 void note_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
@@ -484,9 +502,9 @@ cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, co
 
 cudaError_t launch_leaf_inserts(const LeafArgs& a, cudaStream_t s) {
   const uint32_t grid = (uint32_t)num_sms() * 8;
-  if (a.epi == EPI_TREE) leaf_insert_kernel<EPI_TREE><<<grid, 256, 0, s>>>(a);
-  else leaf_insert_kernel<EPI_LIST><<<grid, 256, 0, s>>>(a);
-  leaf_demote_kernel<<<grid, 256, 0, s>>>(a);
+  if (a.epi == EPI_TREE) launch_k(leaf_insert_kernel<EPI_TREE>, grid, 256, 0, s, a);
+  else launch_k(leaf_insert_kernel<EPI_LIST>, grid, 256, 0, s, a);
+  launch_k(leaf_demote_kernel, grid, 256, 0, s, a);
   note_launch(2);
   return cudaGetLastError();
 }

@@ -25,6 +25,17 @@ enum : uint32_t {
   DERR_SORTKEYS = 1u << 7,      // more distinct source checkpoints than the sort supports
 };
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may be scheduled while its predecessor on the stream is
+// finishing.  Every kernel of the checkpoint sequence starts here: it waits
+// for the predecessor grid's completion and memory (a no-op without such a
+// dependency) before touching anything, then lets its own successor be
+// scheduled.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Raise bits in a device error word (a launch given none records nothing).
 __device__ __forceinline__ void raise_err(uint32_t* err, uint32_t bits) {
   if (err) atomicOr(err, bits);

@@ -101,6 +101,31 @@ cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, co
 cudaError_t launch_leaf_inserts(const LeafArgs& a, cudaStream_t s);
 
 int num_sms();
+
+// Kernel launch with programmatic stream serialization (see pdl_enter): the
+// kernel may be scheduled while its predecessor finishes, hiding the launch
+// gap between the dependent kernels of a checkpoint.  Off when MTCHECK_PDL=0,
+// and while a thread holds a PdlSuppress (captures that become child graphs).
+bool pdl_enabled();
+struct PdlSuppress {
+  PdlSuppress();
+  ~PdlSuppress();
+};
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                            Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 // Running count of kernel launches issued by the library (all handles).
 void note_launch(uint32_t n = 1);
 uint64_t launch_count();

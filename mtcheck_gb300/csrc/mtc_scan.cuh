@@ -51,6 +51,7 @@ __device__ __forceinline__ uint64_t block_excl_scan(uint64_t v, uint64_t* sh, ui
 // counts (the grid covers `max_n`).
 template <class Val>
 __global__ void scan_tile_sums_kernel(Val val, const uint32_t* n_ptr, uint64_t n_const, uint64_t* tile_sums) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   const uint64_t n = n_ptr ? *n_ptr : n_const;
   const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
@@ -68,6 +69,7 @@ __global__ void scan_tile_sums_kernel(Val val, const uint32_t* n_ptr, uint64_t n
 
 // single block: exclusive scan of tile sums in place; grand total to *total
 static __global__ void scan_tile_offsets_kernel(uint64_t* tile_sums, uint32_t ntiles, uint64_t* total) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   uint64_t carry = 0;
   for (uint32_t b = 0; b < ntiles; b += blockDim.x) {
@@ -86,6 +88,7 @@ static __global__ void scan_tile_offsets_kernel(uint64_t* tile_sums, uint32_t nt
 // consumer sees a stable order.
 template <class Val, class Emit>
 __global__ void scan_emit_kernel(Val val, Emit emit, const uint32_t* n_ptr, uint64_t n_const, const uint64_t* tile_offsets) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   const uint64_t n = n_ptr ? *n_ptr : n_const;
   const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
@@ -126,6 +129,7 @@ inline uint32_t reduce_tile_limit() {
 template <class Val, class Emit>
 __global__ void scan_emit_reduce_kernel(Val val, Emit emit, const uint32_t* n_ptr, uint64_t n_const,
                                         const uint64_t* tile_sums, uint64_t* total) {
+  pdl_enter();
   __shared__ uint64_t sh[33];
   const uint64_t n = n_ptr ? *n_ptr : n_const;
   const uint64_t last_tile = n ? (n - 1) / kScanTile : 0;
@@ -161,14 +165,16 @@ inline cudaError_t grid_scan(Val val, Emit emit, const uint32_t* n_dev, uint64_t
                              uint64_t* total, cudaStream_t s) {
   uint32_t ntiles = (uint32_t)((max_n + kScanTile - 1) / kScanTile);
   if (ntiles == 0) ntiles = 1;
-  scan_tile_sums_kernel<<<ntiles, kScanThreads, 0, s>>>(val, n_dev, max_n, scratch);
+  launch_k(scan_tile_sums_kernel<Val>, ntiles, kScanThreads, 0, s, val, n_dev, max_n, scratch);
   if (ntiles <= reduce_tile_limit()) {
-    scan_emit_reduce_kernel<<<ntiles, kScanThreads, 0, s>>>(val, emit, n_dev, max_n, scratch, total);
+    launch_k(scan_emit_reduce_kernel<Val, Emit>, ntiles, kScanThreads, 0, s, val, emit, n_dev, max_n,
+             (const uint64_t*)scratch, total);
     note_launch(2);
     return cudaGetLastError();
   }
-  scan_tile_offsets_kernel<<<1, 1024, 0, s>>>(scratch, ntiles, total);
-  scan_emit_kernel<<<ntiles, kScanThreads, 0, s>>>(val, emit, n_dev, max_n, scratch);
+  launch_k(scan_tile_offsets_kernel, 1, 1024, 0, s, scratch, ntiles, total);
+  launch_k(scan_emit_kernel<Val, Emit>, ntiles, kScanThreads, 0, s, val, emit, n_dev, max_n,
+           (const uint64_t*)scratch);
   note_launch(3);
   return cudaGetLastError();
 }
