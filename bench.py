@@ -49,6 +49,8 @@ def parse():
                    help="update series: the 4 GiB one (sparse chunks, runs, shifted copies, a zero range) or the "
                         "64 MiB one (20%% duplicated chunks at first, then 1%% rewritten per step in runs of 1-32)")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-sections", action="store_true",
+                   help="skip the MD5 and the 64 MiB / 128 B sections")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-restart", action="store_true")
     p.add_argument("--restart-gib", type=float, default=1.0)
@@ -65,11 +67,13 @@ def parse():
     p.add_argument("--only-restart", action="store_true")
     p.add_argument("--serve-procs", type=int, default=256)
     p.add_argument("--serve-rate", type=float, default=2000.0)
-    p.add_argument("--serve-seconds", type=float, default=4.0)
+    p.add_argument("--serve-seconds", type=float, default=8.0)
     p.add_argument("--serve-budget-gb", type=float, default=120.0)
     p.add_argument("--serve-inflight", type=int, default=64)
     p.add_argument("--serve-verify-procs", type=int, default=4)
     p.add_argument("--serve-pinned-gb", type=float, default=32.0)
+    p.add_argument("--serve-sat-requests", type=int, default=3000,
+                   help="requests of the capacity run (all arriving at once), also run one call at a time")
     return p.parse_args()
 
 
@@ -224,6 +228,15 @@ def restart_bench(torch, mc, dev, a, kind, approach=None):
     dev_t = statistics.median(dev_times)
     call_t = statistics.median(times)
     chain_bytes = sum(t.numel() for t in chain_dev)
+    # B_restart = D (written) + the chain bytes read: every chunk's data once
+    # (D) and the metadata of every checkpoint of the chain (headers, region
+    # lists, repeat tables, shift entries)
+    import struct
+    meta = 0
+    for h in chain_host:
+        _r, _c, _dl, _cs, nfo, nprior, nshift = struct.unpack_from("<IIQIIII", h[:32].numpy().tobytes(), 0)
+        meta += 32 + 4 * nfo + (0 if approach == mc.BASIC else 8 * nprior + 8 * nshift)
+    b_restart = 2 * nbytes + meta
     # chain in pinned host memory: H2D inside the call (mtc_restart)
     host_list = [h.numpy().tobytes() for h in chain_host]
     e2e_t = []
@@ -242,6 +255,8 @@ def restart_bench(torch, mc, dev, a, kind, approach=None):
     return {"workload": "restart of checkpoint %d of a %s chain, %.3g GiB buffer, %d B chunks, 4 GiB update "
                         "pattern" % (rid, name, a.restart_gib, a.restart_chunk),
             "value": round(nbytes / dev_t / 1e9, 3), "unit": "GB/s", "ms": round(dev_t * 1e3, 3),
+            "roofline_frac": round(b_restart / dev_t / 1e9 / load_peaks()[0], 4),
+            "b_restart_bytes": int(b_restart),
             "call_ms": round(call_t * 1e3, 3),
             "chain_bytes": int(chain_bytes), "verified_byte_identical": ok,
             "restart_digest": dig.strip(), "digest_matches_original": dig_ok,
@@ -249,6 +264,82 @@ def restart_bench(torch, mc, dev, a, kind, approach=None):
             "host_chain_ms": round(statistics.median(e2e_t) * 1e3, 3),
             "note": "value: device time with the chain resident in HBM; call_ms adds the host side of the call; "
                     "host_chain_value: chain in pageable host memory, copied to HBM inside the call"}
+
+
+def series_bench(torch, mc, dev, states, cs, kind, W, flush=None):
+    """Incremental checkpoints of resident device states through one handle:
+    states[0] is the baseline, the next W are warm-up, the rest are timed.
+    With `flush`, each step is timed alone after a write of `flush` (larger
+    than L2); without it, the whole loop between two events.  Returns the
+    device seconds per step and the per-step counters."""
+    d = mc.TreeDeduplicator(cs, kind)
+    d.checkpoint_device(states[0], True)
+    for s in states[1:1 + W]:
+        d.checkpoint_device(s, False)
+    timed = states[1 + W:]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in timed]
+    leaf, sdata, smeta = [], [], []
+    torch.cuda.synchronize()
+    for i, s in enumerate(timed):
+        if flush is not None:
+            flush.zero_()
+        if flush is not None or i == 0:
+            evs[i][0].record()
+        d.checkpoint_device(s, False)
+        if flush is not None or i == len(timed) - 1:
+            evs[i][1].record()
+        info = d.info()
+        leaf.append(info.phase_times[0])
+        sdata.append(info.data_size)
+        smeta.append(info.metadata_size)
+    torch.cuda.synchronize()
+    if flush is not None:
+        t = sum(e0.elapsed_time(e1) for e0, e1 in evs) / 1e3 / len(timed)
+    else:
+        t = evs[0][0].elapsed_time(evs[-1][1]) / 1e3 / len(timed)
+    d.close()
+    return t, sum(leaf) / len(leaf), sum(sdata) / len(sdata), sum(smeta) / len(smeta)
+
+
+def small_series_section(torch, mc, dev, peak):
+    """The 64 MiB / 128 B series (tree, Murmur3, 10 checkpoints: a baseline and
+    9 incremental ones, each timed alone after a 256 MiB write that flushes
+    L2), run once untimed and once timed on the same states."""
+    nbytes, cs = 64 << 20, 128
+    N = nbytes // cs
+    states = make_states(torch, nbytes, cs, 10, seed=64, device=dev, pattern="64mib")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    series_bench(torch, mc, dev, states, cs, mc.MURMUR3, 0, flush)
+    t, leaf, sd, sm = series_bench(torch, mc, dev, states, cs, mc.MURMUR3, 0, flush)
+    b = nbytes + 32 * N + 2 * sd + sm
+    del states, flush
+    return {"workload": "tree dedup, Murmur3, 64 MiB buffer, 128 B chunks, 10 checkpoints of the 64 MiB update "
+                        "pattern (9 incremental timed, L2 flushed before each)",
+            "value": round(nbytes / t / 1e9, 3), "unit": "GB/s", "ms": round(t * 1e3, 4),
+            "leaf_ms": round(leaf * 1e3, 4),
+            "roofline_frac": round(b / t / 1e9 / peak, 4),
+            "note": "roofline_frac: B_dedup = D + 32 N + 2 S_data + S_meta per device-timed checkpoint over the "
+                    "measured HBM copy bandwidth"}
+
+
+def md5_section(torch, mc, dev, states, cs, W, peak):
+    """The same 4 GiB states checkpointed with MD5 chunk digests."""
+    nbytes = states[0].numel()
+    N = (nbytes + cs - 1) // cs
+    t, leaf, sd, sm = series_bench(torch, mc, dev, states, cs, mc.MD5, W)
+    return {"workload": "tree dedup, MD5, %.3g GiB buffer, %d B chunks, incremental checkpoints of the 4 GiB update "
+                        "pattern" % (nbytes / GIB, cs),
+            "value": round(nbytes / t / 1e9, 3), "unit": "GB/s", "ms": round(t * 1e3, 4),
+            "leaf_ms": round(leaf * 1e3, 4),
+            "leaf_hbm_frac": round(N * (cs + 32) / leaf / 1e9 / peak, 4),
+            "leaf_alu_pipe_frac_ncu": MD5_ALU_PIPE,
+            "note": "MD5 is bound by the integer ALU pipe; leaf_alu_pipe_frac_ncu is the ALU pipe's share of peak "
+                    "in the committed ncu capture of this kernel (profiles/leaf_tma_kernel_md5_512B.md)"}
+
+
+# ALU pipe utilisation of leaf_tma_kernel<MD5> at 512 B chunks, from the
+# committed ncu capture (sm__inst_executed_pipe_alu over its peak)
+MD5_ALU_PIPE = 0.797
 
 
 def cpu_sample(kind, cs, pattern="4gib", nbytes=GIB):
@@ -509,65 +600,126 @@ def serve_bench(torch, mc, dev, a):
         c = srv.poll(100)
         assert len(c) == 1 and c[0]["status"] == 0, c
         pending_checks.append((p, 1, _digest2(mc, kind, outs[0][:nb])))
-    # the request stream
+    rst_ok, rst_checked = True, 0
+
+    def stream(arr, is_rst, who):
+        """Requests arriving at offsets `arr` (ms); returns the latencies,
+        (arrival offset, latency) pairs, bytes served and the wall time from
+        the first arrival to the last completion."""
+        n_req = len(arr)
+        queues = [deque() for _ in range(P)]
+        busy = [None] * P
+        ready = set()
+        lat = {"checkpoint": [], "restart": []}
+        lat_t = []
+        nbytes_done = 0
+        t0 = mc.now_ms() + 20.0
+        i = 0
+        t_last = t0
+        outstanding = 0
+        while i < n_req or outstanding or ready:
+            now = mc.now_ms()
+            while i < n_req and t0 + arr[i] <= now:
+                p = int(who[i])
+                queues[p].append((t0 + arr[i], bool(is_rst[i])))
+                if busy[p] is None:
+                    ready.add(p)
+                i += 1
+            for p in list(ready):
+                arrival, r = queues[p][0]
+                if r:
+                    if not free_outs:
+                        continue
+                    slot = free_outs.pop()
+                    target = int(rng.integers(0, step[p]))
+                    n = mix[p]["nbytes"]
+                    srv.submit_restart(pids[p], target, outs[slot][:n])
+                    busy[p] = ("restart", arrival, target, slot)
+                else:
+                    plans[p].apply(bufs[p], step[p])
+                    srv.submit_checkpoint(pids[p], bufs[p])
+                    busy[p] = ("checkpoint", arrival, step[p], None)
+                    step[p] += 1
+                queues[p].popleft()
+                ready.discard(p)
+                outstanding += 1
+            done = srv.poll(0.0 if (ready or (i < n_req and t0 + arr[i] <= mc.now_ms() + 0.05)) else 0.2)
+            for c in done:
+                p = c["pid"]  # this server's process ids are 0..P-1 in order
+                what, arrival, target, slot = busy[p]
+                assert c["status"] == 0, c
+                lat[what].append(c["t_done_ms"] - arrival)
+                lat_t.append((arrival - t0, c["t_done_ms"] - arrival))
+                nbytes_done += mix[p]["nbytes"]
+                t_last = max(t_last, c["t_done_ms"])
+                if what == "restart":
+                    pending_checks.append((p, target, _digest2(mc, kind, outs[slot][:mix[p]["nbytes"]])))
+                    free_outs.append(slot)
+                busy[p] = None
+                outstanding -= 1
+                if queues[p]:
+                    ready.add(p)
+        return lat, lat_t, nbytes_done, (t_last - t0) / 1e3
+
+    # the request stream: Poisson arrivals at the configured rate
     n_req = int(a.serve_rate * a.serve_seconds)
     arr = np.cumsum(rng.exponential(1.0 / a.serve_rate, n_req)) * 1e3
-    is_rst = rng.random(n_req) < 0.05
-    who = rng.integers(0, P, n_req)
-    queues = [deque() for _ in range(P)]
-    busy = [None] * P
-    ready = set()
-    lat = {"checkpoint": [], "restart": []}
-    lat_t = []                      # (arrival offset, latency) in ms
-    nbytes_done = 0
-    rst_ok, rst_checked = True, 0
-    t0 = mc.now_ms() + 20.0
-    i = 0
-    t_last = t0
-    outstanding = 0
-    while i < n_req or outstanding or ready:
-        now = mc.now_ms()
-        while i < n_req and t0 + arr[i] <= now:
-            p = int(who[i])
-            queues[p].append((t0 + arr[i], bool(is_rst[i])))
-            if busy[p] is None:
-                ready.add(p)
-            i += 1
-        for p in list(ready):
-            arrival, r = queues[p][0]
-            if r:
-                if not free_outs:
-                    continue
-                slot = free_outs.pop()
-                target = int(rng.integers(0, step[p]))
-                n = mix[p]["nbytes"]
-                srv.submit_restart(pids[p], target, outs[slot][:n])
-                busy[p] = ("restart", arrival, target, slot)
-            else:
-                plans[p].apply(bufs[p], step[p])
-                srv.submit_checkpoint(pids[p], bufs[p])
-                busy[p] = ("checkpoint", arrival, step[p], None)
-                step[p] += 1
-            queues[p].popleft()
-            ready.discard(p)
-            outstanding += 1
-        done = srv.poll(0.0 if (ready or (i < n_req and t0 + arr[i] <= mc.now_ms() + 0.05)) else 0.2)
-        for c in done:
-            p = c["pid"]  # this server's process ids are 0..P-1 in order
-            what, arrival, target, slot = busy[p]
-            assert c["status"] == 0, c
-            lat[what].append(c["t_done_ms"] - arrival)
-            lat_t.append((arrival - t0, c["t_done_ms"] - arrival))
-            nbytes_done += mix[p]["nbytes"]
-            t_last = max(t_last, c["t_done_ms"])
-            if what == "restart":
-                pending_checks.append((p, target, _digest2(mc, kind, outs[slot][:mix[p]["nbytes"]])))
-                free_outs.append(slot)
-            busy[p] = None
-            outstanding -= 1
-            if queues[p]:
-                ready.add(p)
-    wall = (t_last - t0) / 1e3
+    lat, lat_t, nbytes_done, wall = stream(arr, rng.random(n_req) < 0.05, rng.integers(0, P, n_req))
+    st_stream = srv.stats()
+    # capacity: the same kind of requests all arriving at once (each process
+    # still has one request on the server at a time)
+    n_sat = a.serve_sat_requests
+    sat_rst = rng.random(n_sat) < 0.05
+    sat_who = rng.integers(0, P, n_sat)
+    lat_s, _, bytes_s, wall_s = stream(np.zeros(n_sat), sat_rst, sat_who)
+    sat_lat = lat_s["checkpoint"] + lat_s["restart"]
+    # the one-buffer-per-call path on the same requests: one lone handle per
+    # process (a baseline of the process's current state first, untimed),
+    # every request a synchronous call in arrival order, each new checkpoint
+    # kept in HBM for the restarts as the server keeps its chains
+    pc_bufs = [b.clone() for b in bufs]
+    lones = [mc.TreeDeduplicator(m["chunk_size"], kind) for m in mix]
+    pc_chain = [[] for _ in range(P)]
+
+    def keep_diff(p):
+        ptr, ln = lones[p].diff_device()
+        pc_chain[p].append(torch.as_tensor(_DevView(ptr, ln), device=dev).clone())
+
+    for p in range(P):
+        lones[p].checkpoint_device(pc_bufs[p], True)
+        keep_diff(p)
+    pc_step = list(step)
+    rng_pc = np.random.default_rng(12)
+    torch.cuda.synchronize()
+    t_pc = time.perf_counter()
+    for r, p in zip(sat_rst, sat_who):
+        p = int(p)
+        if r:
+            target = int(rng_pc.integers(0, len(pc_chain[p])))
+            lones[p].restart_device(outs[0][:mix[p]["nbytes"]],
+                                    [(x.data_ptr(), x.numel()) for x in pc_chain[p]], target)
+        else:
+            plans[p].apply(pc_bufs[p], pc_step[p])
+            pc_step[p] += 1
+            lones[p].checkpoint_device(pc_bufs[p], False)
+            keep_diff(p)
+    torch.cuda.synchronize()
+    wall_pc = time.perf_counter() - t_pc
+    for d in lones:
+        d.close()
+    del lones, pc_bufs, pc_chain
+    torch.cuda.empty_cache()
+    saturation = {
+        "requests": n_sat, "restarts": int(sat_rst.sum()),
+        "served_rate": round(n_sat / wall_s, 1), "served_gbs": round(bytes_s / wall_s / 1e9, 3),
+        "per_call_rate": round(n_sat / wall_pc, 1),
+        "speedup_vs_per_call": round(wall_pc / wall_s, 3),
+        "served_latency_ms": {"p50": round(float(np.percentile(sat_lat, 50)), 3),
+                              "p99": round(float(np.percentile(sat_lat, 99)), 3)},
+        "note": "all requests arrive at once; served: the request server (continuous admission, overlapped on "
+                "the device); per_call: one synchronous call per request through one lone handle per process, "
+                "starting from a baseline of the same states, each checkpoint kept in HBM",
+    }
     st = srv.stats()
     # every restart against the state it restores: replay each process's
     # updates (deterministic per seed and step) into a scratch buffer
@@ -624,6 +776,7 @@ def serve_bench(torch, mc, dev, a):
                        "restart_p50": pct(lat["restart"], 50), "restart_p99": pct(lat["restart"], 99),
                        "after_first_second_p50": pct(late, 50), "after_first_second_p99": pct(late, 99),
                        "p99_per_second": [pct(per_s[k], 99) for k in sorted(per_s)]},
+        "saturation": saturation,
         "restarts_verified": rst_checked, "restarts_identical": rst_ok,
         "alone_vs_mix": {"processes": len(sample), "checkpoints": alone_checked, "identical": alone_ok},
         "baseline_s": round(base_s, 2),
@@ -631,9 +784,44 @@ def serve_bench(torch, mc, dev, a):
         "server": {k: st[k] for k in ("inflight_peak", "graph_captures", "graph_replays", "spilled_diffs",
                                       "spilled_states", "restored_states", "staged_diffs", "hbm_peak",
                                       "deferred_admissions", "failed", "worker_ms")},
+        "server_after_stream": {k: st_stream[k] for k in ("spilled_diffs", "spilled_states", "restored_states",
+                                                          "staged_diffs", "hbm_peak")},
         "note": "value: bytes of all completed requests (checkpointed and restarted buffers) / time from the first "
                 "arrival to the last completion; latency: arrival to completion (diff archived in HBM, or "
                 "restarted buffer written)",
+    }
+
+
+def summary_of(line):
+    """The headline figures of every section in one small object, printed
+    last on the line."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict) or d.get(k) is None:
+                return None
+            d = d[k]
+        return d
+    return {
+        "dedup_4gib_512b_murmur3_gbs": line["value"],
+        "dedup_checkpoint_roofline_frac": g(line, "config", "checkpoint_roofline_frac"),
+        "leaf_kernel_roofline_frac": g(line, "roofline", "frac"),
+        "e2e_gbs": g(line, "e2e", "value"),
+        "dedup_4gib_512b_md5_gbs": g(line, "md5", "value"),
+        "md5_leaf_alu_pipe_frac": g(line, "md5", "leaf_alu_pipe_frac_ncu"),
+        "dedup_64mib_128b_gbs": g(line, "series_64mib", "value"),
+        "dedup_64mib_128b_ms": g(line, "series_64mib", "ms"),
+        "dedup_64mib_128b_roofline_frac": g(line, "series_64mib", "roofline_frac"),
+        "restart_1gib_256b_gbs": g(line, "restart", "value"),
+        "restart_roofline_frac": g(line, "restart", "roofline_frac"),
+        "restart_host_chain_gbs": g(line, "restart", "host_chain_value"),
+        "restart_verified": g(line, "restart", "verified_byte_identical"),
+        "batched_speedup_job": g(line, "batched", "speedup"),
+        "batched_speedup_incremental": g(line, "batched", "speedup_incremental"),
+        "batched_identical": g(line, "batched", "identical_to_per_call"),
+        "served_gbs": g(line, "served", "value"),
+        "served_p50_ms": g(line, "served", "latency_ms", "p50"),
+        "served_p99_ms": g(line, "served", "latency_ms", "p99"),
+        "served_capacity_vs_per_call": g(line, "served", "saturation", "speedup_vs_per_call"),
     }
 
 
@@ -820,6 +1008,9 @@ def main():
                "step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]}
         del host, pinned_out, out_view, bufs
 
+    md5 = small = None
+    if rank == 0 and not a.no_sections:
+        md5 = md5_section(torch, mc, dev, states[:1 + W + K], cs, W, peak)
     rst = None
     if not a.no_restart and rank == 0:
         del states
@@ -833,6 +1024,11 @@ def main():
                                                                  "digest_matches_original", "host_chain_value",
                                                                  "chain_bytes")}
             torch.cuda.empty_cache()
+
+    if rank == 0 and not a.no_sections:
+        torch.cuda.empty_cache()
+        small = small_series_section(torch, mc, dev, peak)
+        torch.cuda.empty_cache()
 
     bat = None
     if not a.no_batch and rank == 0:
@@ -880,12 +1076,15 @@ def main():
                          else "fallback 6.8 TB/s"},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "md5": md5,
+            "series_64mib": small,
             "restart": rst,
             "batched": bat,
             "served": srvd,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }
+        line["summary"] = summary_of(line)
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
