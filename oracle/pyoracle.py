@@ -56,6 +56,65 @@ def ref_lib():
     return _ref
 
 
+_refd = None
+
+
+def ref_dedup_lib():
+    """The reference's own deduplicators compiled on this host, or None."""
+    global _refd
+    if _refd is None:
+        path = _build.build_ref_dedup()
+        if path is None:
+            return None
+        L = ctypes.CDLL(path)
+        L.refd_create.restype = ctypes.c_void_p
+        L.refd_create.argtypes = [ctypes.c_int, ctypes.c_uint32]
+        L.refd_destroy.argtypes = [ctypes.c_void_p]
+        L.refd_checkpoint.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
+        L.refd_free.argtypes = [ctypes.c_void_p]
+        L.refd_restart.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p),
+                                   ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p,
+                                   ctypes.c_uint64]
+        _refd = L
+    return _refd
+
+
+class RefDeduplicator:
+    """A deduplicator of the reference's own code (Murmur3, the reference's
+    hash()): BASIC, LIST or TREE."""
+
+    def __init__(self, approach, chunk_size):
+        self.h = ref_dedup_lib().refd_create(approach, chunk_size)
+        if not self.h:
+            raise ValueError("approach not available in the reference build")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref_dedup_lib().refd_destroy(self.h)
+            self.h = None
+
+    def checkpoint(self, data, make_baseline):
+        a = _buf(data)
+        p, n = ctypes.c_void_p(), ctypes.c_uint64()
+        ref_dedup_lib().refd_checkpoint(self.h, a.ctypes.data, a.size, int(make_baseline), ctypes.byref(p),
+                                        ctypes.byref(n))
+        out = ctypes.string_at(p.value, n.value)
+        ref_dedup_lib().refd_free(p)
+        return out
+
+
+def ref_restart(approach, chunk_size, diffs, chkpt_id, out):
+    """The reference's restart_chkpt of checkpoint ``chkpt_id`` into ``out``
+    (in place).  Its tree restart reads out of bounds for chunk counts that
+    are not powers of two: callers keep to power-of-two tree chains."""
+    bufs = [np.frombuffer(d, dtype=np.uint8) for d in diffs]
+    ptrs = (ctypes.c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+    lens = (ctypes.c_uint64 * len(bufs))(*[b.size for b in bufs])
+    return ref_dedup_lib().refd_restart(approach, chunk_size, ptrs, lens, len(bufs), chkpt_id, out.ctypes.data,
+                                        out.size)
+
+
 def _buf(data):
     a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray)) else data,
                              dtype=np.uint8)

@@ -9,6 +9,9 @@
   computed by the reference's own hash headers (include/kokkos_murmur3.hpp,
   include/kokkos_md5.hpp) compiled by ``oracle/build.py`` into oracle/_ref.
 
+* ``reference_series.npz``: a seeded series (inputs) checkpointed by the
+  reference's own basic, list and tree deduplicators, compiled by
+  ``oracle/build.py`` against the serial Kokkos stand-in (``<approach>_diff<i>``).
 * ``long_hash_vectors.json``: whole-buffer digests of inputs longer than
   INT_MAX bytes (a fixed arithmetic byte pattern, ``long_pattern``), where the
   reference's MD5 takes its 128-byte-piece branch
@@ -103,6 +106,25 @@ def long_vectors():
     return vecs
 
 
+# series checkpointed by the reference's own code (oracle/_ref/libref_dedup.so)
+# for the GPU tests: inputs, diffs per approach, restarted states
+REF_SERIES = {"nbytes": 32 * 1024 + 77, "chunk_size": 64, "steps": 4, "seed": 1234}
+
+
+def reference_series():
+    from oracle import pyoracle
+    from mtcheck_gb300 import workloads
+    n, cs, steps = REF_SERIES["nbytes"], REF_SERIES["chunk_size"], REF_SERIES["steps"]
+    z = (n // 4, n // 4 + n // 8)
+    states = [s.copy() for s in workloads.pattern2(n, cs, steps, seed=REF_SERIES["seed"], zero_range=z)]
+    out = {"state%d" % i: s for i, s in enumerate(states)}
+    for approach, name in ((2, "basic"), (3, "list"), (4, "tree")):
+        r = pyoracle.RefDeduplicator(approach, cs)
+        for i, s in enumerate(states):
+            out["%s_diff%d" % (name, i)] = np.frombuffer(r.checkpoint(s, i == 0), np.uint8).copy()
+    return out
+
+
 if __name__ == "__main__":
     with open(os.path.join(OUT, "tree_kat.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": kat_cases()}, f, indent=1)
@@ -111,4 +133,5 @@ if __name__ == "__main__":
     with open(os.path.join(OUT, "long_hash_vectors.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "pattern": "long_pattern",
                    "vectors": long_vectors()}, f, indent=1)
+    np.savez_compressed(os.path.join(OUT, "reference_series.npz"), **reference_series())
     print("wrote", os.listdir(OUT))
