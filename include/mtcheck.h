@@ -208,7 +208,9 @@ typedef struct mtc_batch_info {
   double host_ms[5];       /* its parts: prepare (allocation, validation), graph
                               capture, issue, wait for the join, completion */
   int32_t last_used_graph;
-  int32_t reserved;
+  uint32_t batched_leaf_members; /* members whose leaves ran in the one persistent
+                                    launch of the last graph step (its work queue
+                                    holds their (member, tile) items) */
 } mtc_batch_info_t;
 int mtc_batch_create(uint32_t n, const int* approaches, const int* hashes, const uint32_t* chunk_sizes,
                      mtc_batch_t** out);
@@ -308,6 +310,10 @@ typedef struct mtc_tune {
   int32_t eager;        /* 1: issue every launch of a checkpoint from the host instead of
                            replaying the captured sequence (single-handle calls) */
   double max_load;      /* digest-map load factor bound, (0.1, 0.95] */
+  int32_t threads_per_chunk; /* 1 (0 taken as 1): one thread per chunk; 32: one warp
+                                per chunk (chunks of at most 4096 bytes; the warp loads
+                                the chunk, one lane hashes it: the digests are serial) */
+  int32_t reserved;
 } mtc_tune_t;
 int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t);
 int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* out);

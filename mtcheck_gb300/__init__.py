@@ -54,16 +54,17 @@ class BatchInfo(ctypes.Structure):
                 ("kernels_per_step", ctypes.c_uint64), ("last_device_ms", ctypes.c_double),
                 ("last_call_ms", ctypes.c_double), ("host_ms", ctypes.c_double * 5),
                 ("last_used_graph", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("batched_leaf_members", ctypes.c_uint32)]
 
 
 class Tune(ctypes.Structure):
     _fields_ = [("rows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("direct", ctypes.c_int32),
-                ("eager", ctypes.c_int32), ("max_load", ctypes.c_double)]
+                ("eager", ctypes.c_int32), ("max_load", ctypes.c_double), ("threads_per_chunk", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
     def as_dict(self):
         return {"rows": self.rows, "ctas_per_sm": self.ctas_per_sm, "direct": self.direct,
-                "eager": self.eager, "max_load": self.max_load}
+                "eager": self.eager, "max_load": self.max_load, "threads_per_chunk": self.threads_per_chunk}
 
 
 class ServerOptions(ctypes.Structure):
@@ -316,12 +317,13 @@ class Deduplicator:
         _check(load().mtc_write_restart_log(self.h, select_chkpt, logname.encode()))
 
     # -- tuning ------------------------------------------------------------
-    def set_tuning(self, rows=None, ctas_per_sm=None, direct=None, max_load=None, eager=None):
+    def set_tuning(self, rows=None, ctas_per_sm=None, direct=None, max_load=None, eager=None,
+                   threads_per_chunk=None):
         """Set the given fields of the launch tuning; the others keep their values."""
         cur = self.tuning()
         pick = lambda v, k: cur[k] if v is None else v
         t = Tune(pick(rows, "rows"), pick(ctas_per_sm, "ctas_per_sm"), pick(direct, "direct"), pick(eager, "eager"),
-                 pick(max_load, "max_load"))
+                 pick(max_load, "max_load"), pick(threads_per_chunk, "threads_per_chunk"), 0)
         _check(load().mtc_set_tuning(self.h, ctypes.byref(t)))
 
     def tuning(self):

@@ -1,4 +1,6 @@
 // batch.cu -- Batch (many engines, one CUDA graph per step) and the autotuner.
+#include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <map>
 #include <mutex>
@@ -15,7 +17,34 @@ double now_ms() {
 }
 }  // namespace
 
+namespace {
+// MTCHECK_BATCH_LEAF / MTCHECK_BATCH_POOL = 0 or 1 override the defaults
+bool env_flag(const char* name, bool dflt) {
+  const char* e = std::getenv(name);
+  if (!e || !*e) return dflt;
+  return e[0] != '0';
+}
+}  // namespace
+
 Batch::Batch() {
+  leaf_batching_ = env_flag("MTCHECK_BATCH_LEAF", leaf_batching_);
+  // every member allocates from one stream-ordered pool that keeps what is
+  // freed: a batch of many small members otherwise spends its first step in
+  // thousands of cudaMalloc calls
+  const bool use_pool = env_flag("MTCHECK_BATCH_POOL", true);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  if (use_pool && cudaMemPoolCreate(&pool_, &props) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep);
+  } else {
+    pool_ = nullptr;
+    cudaGetLastError();
+  }
   cudaStreamCreateWithFlags(&origin_, cudaStreamNonBlocking);
   cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&in_, cudaEventDisableTiming);
@@ -28,7 +57,12 @@ Batch::~Batch() {
   for (auto s : streams_) cudaStreamSynchronize(s);
   drop_graph();
   for (auto* e : engs_) delete e;
+  for (auto s : streams_) cudaStreamSynchronize(s);
   for (auto s : streams_) cudaStreamDestroy(s);
+  if (pool_) cudaMemPoolDestroy(pool_);
+  if (members_dev_) cudaFree(members_dev_);
+  if (items_dev_) cudaFree(items_dev_);
+  if (head_dev_) cudaFree(head_dev_);
   for (auto e : joins_) cudaEventDestroy(e);
   if (fork_) cudaEventDestroy(fork_);
   if (in_) cudaEventDestroy(in_);
@@ -47,14 +81,18 @@ void Batch::drop_parent() {
   if (parent_) cudaGraphDestroy(parent_);
   parent_exec_ = nullptr;
   parent_ = nullptr;
-  child_nodes_.clear();
 }
 
 void Batch::drop_graph() {
   drop_parent();
-  for (auto& g : graphs_)
+  for (auto& g : pre_)
     if (g) cudaGraphDestroy(g);
-  graphs_.assign(engs_.size(), nullptr);
+  for (auto& g : post_)
+    if (g) cudaGraphDestroy(g);
+  pre_.assign(engs_.size(), nullptr);
+  post_.assign(engs_.size(), nullptr);
+  in_kernel_.assign(engs_.size(), 0);
+  recs_.assign(engs_.size(), MemberLeaf{});
   sigs_.assign(engs_.size(), 0);
   nodes_.assign(engs_.size(), 0);
   kernels_.assign(engs_.size(), 0);
@@ -72,6 +110,7 @@ int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
   e->set_stream(s);
   e->set_order_after_legacy(true);
   e->set_params_from_host(true);  // the batch's graph replays the member's sequence as captured
+  if (pool_) e->set_pool(pool_);
   engs_.push_back(e);
   streams_.push_back(s);
   joins_.push_back(j);
@@ -86,36 +125,135 @@ int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
                                        std::string(#call) + ": " + cudaGetErrorString(e_));          \
   } while (0)
 
+// The member's sequence reaches its leaf pass while being captured: when
+// its leaves can go through the batched launch, keep its record, close the
+// capture there (the part before the leaves) and open the part after it,
+// which starts with the partial last chunk, if any, hashed on its own.
+int Batch::on_leaves(Engine* e, const LeafArgs& la, cudaStream_t s) {
+  MemberLeaf rec;
+  if (!leaf_batching_ || !batch_leaf_member(&rec, la)) {
+    const cudaError_t ce = e->launch_own_leaves(la, s);
+    return ce == cudaSuccess ? ST_OK : ST_ECUDA;
+  }
+  cudaGraph_t g = nullptr;
+  if (cudaStreamEndCapture(s, &g) != cudaSuccess) return ST_ECUDA;
+  pre_[cur_] = g;
+  recs_[cur_] = rec;
+  in_kernel_[cur_] = 1;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return ST_ECUDA;
+  if (la.n_chunks > rec.n_full && launch_leaf_range(la, rec.n_full, la.n_chunks, s) != cudaSuccess) return ST_ECUDA;
+  return ST_OK;
+}
+
 int Batch::capture_member(size_t i, const uint8_t* data, uint64_t len) {
-  if (graphs_[i]) cudaGraphDestroy(graphs_[i]);
-  graphs_[i] = nullptr;
+  for (cudaGraph_t* g : {&pre_[i], &post_[i]}) {
+    if (*g) cudaGraphDestroy(*g);
+    *g = nullptr;
+  }
+  in_kernel_[i] = 0;
   const uint64_t l0 = launch_count();
+  // the member's graphs become child nodes of the step's graph: captured
+  // with plain stream order (no programmatic dependencies)
+  PdlSuppress no_pdl;
+  cur_ = i;
+  engs_[i]->set_leaf_hook(this);
   MTC_BCUDA(cudaStreamBeginCapture(streams_[i], cudaStreamCaptureModeRelaxed));
   int rc = engs_[i]->enqueue(data, len, false);
+  engs_[i]->set_leaf_hook(nullptr);
   cudaGraph_t g = nullptr;
   cudaError_t ee = cudaStreamEndCapture(streams_[i], &g);
   if (rc != ST_OK || ee != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
+    for (cudaGraph_t* p : {&pre_[i], &post_[i]}) {
+      if (*p) cudaGraphDestroy(*p);
+      *p = nullptr;
+    }
+    in_kernel_[i] = 0;
     if (rc != ST_OK) return fail(rc, "member " + std::to_string(i) + ": " + engs_[i]->last_error);
     return fail(ST_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
   }
-  size_t n = 0;
-  cudaGraphGetNodes(g, nullptr, &n);
-  graphs_[i] = g;
-  nodes_[i] = n;
+  (in_kernel_[i] ? post_[i] : pre_[i]) = g;
+  size_t n = 0, n2 = 0;
+  cudaGraphGetNodes(pre_[i], nullptr, &n);
+  if (post_[i]) cudaGraphGetNodes(post_[i], nullptr, &n2);
+  nodes_[i] = n + n2;
   kernels_[i] = launch_count() - l0;
   sigs_[i] = engs_[i]->signature(data, len);
   stats_.captures++;
   return ST_OK;
 }
 
+// The step's graph: the work queue's head is reset and every member's part
+// before its leaves runs; then one persistent launch hashes the leaves of
+// every member whose record was kept (items (member, tile), largest tiles
+// first); then each such member's part after its leaves.
 int Batch::build_parent() {
   drop_parent();
+  std::vector<uint32_t> order;
+  for (uint32_t i = 0; i < engs_.size(); i++)
+    if (in_kernel_[i]) order.push_back(i);
+  // per-tile cost: bytes per tile, MD5 about twice Murmur3's work per byte
+  auto cost = [&](uint32_t i) {
+    return (uint64_t)recs_[i].la.cs * (recs_[i].la.hash_kind == HASH_MD5 ? 2 : 1);
+  };
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return cost(x) > cost(y); });
+  std::vector<uint2> items;
+  for (uint32_t i : order) {
+    const uint32_t tiles = (recs_[i].n_full + kBatchRows - 1) / kBatchRows;
+    for (uint32_t t = 0; t < tiles; t++) items.push_back(make_uint2(i, t));
+  }
+  if (!order.empty()) {
+    if (members_cap_ < engs_.size()) {
+      if (members_dev_) cudaFree(members_dev_);
+      members_dev_ = nullptr;
+      MTC_BCUDA(cudaMalloc(&members_dev_, sizeof(MemberLeaf) * engs_.size()));
+      members_cap_ = engs_.size();
+    }
+    if (items_cap_ < items.size()) {
+      if (items_dev_) cudaFree(items_dev_);
+      items_dev_ = nullptr;
+      MTC_BCUDA(cudaMalloc(&items_dev_, sizeof(uint2) * items.size()));
+      items_cap_ = items.size();
+    }
+    if (!head_dev_) MTC_BCUDA(cudaMalloc(&head_dev_, 256));
+    MTC_BCUDA(cudaMemcpy(members_dev_, recs_.data(), sizeof(MemberLeaf) * engs_.size(), cudaMemcpyHostToDevice));
+    MTC_BCUDA(cudaMemcpy(items_dev_, items.data(), sizeof(uint2) * items.size(), cudaMemcpyHostToDevice));
+  }
+  leaf_params_ = BatchLeafParams{members_dev_, items_dev_, (uint32_t)items.size(), 0, head_dev_};
+  stats_.batched_leaf_items = items.size();
+  stats_.batched_leaf_members = (uint32_t)order.size();
+
   MTC_BCUDA(cudaGraphCreate(&parent_, 0));
-  child_nodes_.assign(engs_.size(), nullptr);
-  for (size_t i = 0; i < engs_.size(); i++)
-    MTC_BCUDA(cudaGraphAddChildGraphNode(&child_nodes_[i], parent_, nullptr, 0, graphs_[i]));
+  std::vector<cudaGraphNode_t> before;  // what the batched launch waits for
+  if (!order.empty()) {
+    cudaMemsetParams mp{};
+    mp.dst = head_dev_;
+    mp.value = 0;
+    mp.elementSize = 4;
+    mp.width = 1;
+    mp.height = 1;
+    cudaGraphNode_t reset = nullptr;
+    MTC_BCUDA(cudaGraphAddMemsetNode(&reset, parent_, nullptr, 0, &mp));
+    before.push_back(reset);
+  }
+  for (size_t i = 0; i < engs_.size(); i++) {
+    cudaGraphNode_t a = nullptr;
+    MTC_BCUDA(cudaGraphAddChildGraphNode(&a, parent_, nullptr, 0, pre_[i]));
+    if (in_kernel_[i]) before.push_back(a);
+  }
+  if (!order.empty()) {
+    cudaKernelNodeParams kp{};
+    void* args[1];
+    MTC_BCUDA(batch_leaf_node_params(leaf_params_, &kp, args));
+    cudaGraphNode_t k = nullptr;
+    MTC_BCUDA(cudaGraphAddKernelNode(&k, parent_, before.data(), before.size(), &kp));
+    for (size_t i = 0; i < engs_.size(); i++) {
+      if (!in_kernel_[i]) continue;
+      cudaGraphNode_t b = nullptr;
+      MTC_BCUDA(cudaGraphAddChildGraphNode(&b, parent_, &k, 1, post_[i]));
+    }
+  }
   cudaError_t ie = cudaGraphInstantiate(&parent_exec_, parent_, 0);
   if (ie != cudaSuccess) {
     parent_exec_ = nullptr;
@@ -148,15 +286,11 @@ int Batch::checkpoint(const uint8_t* const* data, const uint64_t* lens, bool mak
     bool rebuild = !parent_exec_;
     for (size_t i = 0; i < engs_.size(); i++) {
       if (engs_[i]->take_stream_work()) join[i] = 1;
-      if (!graphs_[i] || sigs_[i] != engs_[i]->signature(data[i], lens[i])) {
+      if (!pre_[i] || sigs_[i] != engs_[i]->signature(data[i], lens[i])) {
         int rc = capture_member(i, data[i], lens[i]);
         if (rc) return rc;
         join[i] = 1;
-        // same launch sequence on moved buffers: update the member's node
-        if (!rebuild && cudaGraphExecChildGraphNodeSetParams(parent_exec_, child_nodes_[i], graphs_[i]) != cudaSuccess) {
-          cudaGetLastError();
-          rebuild = true;
-        }
+        rebuild = true;  // moved buffers: new records and graphs
       }
     }
     if (rebuild) {
@@ -183,6 +317,7 @@ int Batch::checkpoint(const uint8_t* const* data, const uint64_t* lens, bool mak
       nodes += nodes_[i];
       kernels += kernels_[i];
     }
+    if (stats_.batched_leaf_members) kernels += 1;  // the batched leaf launch
     MTC_BCUDA(cudaEventRecord(t0_, origin_));
     MTC_BCUDA(cudaGraphLaunch(parent_exec_, origin_));
   } else {
@@ -306,6 +441,9 @@ int autotune(int mode, int hash_kind, uint32_t chunk_size, uint64_t len, bool us
   for (int rows : {256, 128})
     for (int per_sm : {1, 2, 3, 4}) cands.push_back({LeafTune{rows, per_sm, 0}, 0.75});
   cands.push_back({LeafTune{256, 0, 1}, 0.75});
+  // a warp per chunk (large chunks only: below 1 KiB a warp would spend its
+  // loads on a few hundred bytes)
+  if (chunk_size >= 1024 && chunk_size <= 4096) cands.push_back({LeafTune{256, 0, 1, 32}, 0.75});
   if (has_map)
     for (double l : loads_tree)
       if (l != 0.75) cands.push_back({LeafTune{256, 0, 0}, l});

@@ -31,6 +31,8 @@ struct BatchStats {
   uint64_t steps = 0;
   uint64_t captures = 0;
   uint64_t graph_nodes = 0;       // nodes of all members' graphs
+  uint64_t batched_leaf_items = 0;  // work items of the batched leaf launch (0: none)
+  uint32_t batched_leaf_members = 0;
   uint64_t kernels_per_step = 0;  // kernel launches issued (eager) or held in the graphs
   double last_device_ms = 0;      // fork to join of the last step, CUDA events on the origin stream
   double last_call_ms = 0;        // host wall time of the last checkpoint() call
@@ -38,7 +40,7 @@ struct BatchStats {
   int last_used_graph = 0;
 };
 
-class Batch {
+class Batch : public Engine::LeafHook {
  public:
   Batch();
   ~Batch();
@@ -51,8 +53,13 @@ class Batch {
   int checkpoint(const uint8_t* const* data, const uint64_t* lens, bool make_baseline, uint64_t* diff_lens);
   void set_use_graph(bool g) { use_graph_ = g; }
   void set_id_headroom(uint32_t h) { headroom_ = h ? h : 1; }
+  // off: every member launches its own leaf kernels in its graph (no
+  // batched leaf launch)
+  void set_leaf_batching(bool on) { leaf_batching_ = on; }
   const BatchStats& stats() const { return stats_; }
   std::string last_error;
+  // Engine::LeafHook: a member's captured sequence reaches its leaf pass
+  int on_leaves(Engine* e, const LeafArgs& la, cudaStream_t s) override;
 
  private:
   int fail(int code, const std::string& msg);
@@ -65,13 +72,25 @@ class Batch {
   std::vector<cudaStream_t> streams_;
   std::vector<cudaEvent_t> joins_;
   cudaStream_t origin_ = nullptr;
+  cudaMemPool_t pool_ = nullptr;  // stream-ordered allocations of every member
   cudaEvent_t fork_ = nullptr, in_ = nullptr, t0_ = nullptr, t1_ = nullptr;
-  std::vector<cudaGraph_t> graphs_;  // each member's captured sequence
+  // each member's captured sequence, cut at its leaf pass when the batched
+  // leaf launch takes it over: pre_ (up to the leaves) and post_ (after);
+  // otherwise the whole sequence in pre_
+  std::vector<cudaGraph_t> pre_, post_;
+  std::vector<char> in_kernel_;      // the member's leaves run in the batched launch
+  std::vector<MemberLeaf> recs_;     // their records (host copy)
   std::vector<uint64_t> sigs_, nodes_, kernels_;
-  cudaGraph_t parent_ = nullptr;     // one child graph node per member
+  size_t cur_ = 0;                   // member being captured
+  // step graph: [head reset, members' pre_] -> batched leaf launch -> members' post_
+  cudaGraph_t parent_ = nullptr;
   cudaGraphExec_t parent_exec_ = nullptr;
-  std::vector<cudaGraphNode_t> child_nodes_;  // member i's node in parent_
-  bool use_graph_ = true;
+  MemberLeaf* members_dev_ = nullptr;
+  uint2* items_dev_ = nullptr;
+  uint32_t* head_dev_ = nullptr;
+  size_t members_cap_ = 0, items_cap_ = 0;
+  BatchLeafParams leaf_params_{};
+  bool use_graph_ = true, leaf_batching_ = false;
   uint32_t headroom_ = 64;
   BatchStats stats_;
 };

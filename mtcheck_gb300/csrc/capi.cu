@@ -409,6 +409,7 @@ int mtc_batch_get_info(const mtc_batch_t* b, mtc_batch_info_t* o) {
   o->last_call_ms = s.last_call_ms;
   for (int k = 0; k < 5; k++) o->host_ms[k] = s.host_ms[k];
   o->last_used_graph = s.last_used_graph;
+  o->batched_leaf_members = s.last_used_graph ? s.batched_leaf_members : 0;
   return MTC_OK;
 }
 
@@ -530,7 +531,10 @@ int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t) {
   if (t->rows != 128 && t->rows != 256) return ret(MTC_EINVAL, "rows must be 128 or 256");
   if (t->ctas_per_sm < 0 || t->ctas_per_sm > 8) return ret(MTC_EINVAL, "ctas_per_sm out of range");
   if (!(t->max_load > 0.1 && t->max_load <= 0.95)) return ret(MTC_EINVAL, "max_load outside (0.1, 0.95]");
-  h->eng->set_leaf_tune(mtc::LeafTune{t->rows, t->ctas_per_sm, t->direct ? 1 : 0});
+  if (t->threads_per_chunk != 0 && t->threads_per_chunk != 1 && t->threads_per_chunk != 32)
+    return ret(MTC_EINVAL, "threads_per_chunk must be 1 or 32");
+  h->eng->set_leaf_tune(mtc::LeafTune{t->rows, t->ctas_per_sm, t->direct ? 1 : 0,
+                                      t->threads_per_chunk == 32 ? 32 : 1});
   h->eng->set_max_load(t->max_load);
   h->eng->set_own_graph(t->eager == 0);
   return MTC_OK;
@@ -543,6 +547,7 @@ int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* o) {
   o->rows = t.rows;
   o->ctas_per_sm = t.ctas_per_sm;
   o->direct = t.direct;
+  o->threads_per_chunk = t.threads_per_chunk;
   o->eager = h->eng->own_graph() ? 0 : 1;
   o->max_load = h->eng->max_load();
   return MTC_OK;
@@ -562,6 +567,7 @@ int mtc_autotune(int approach, int hash, uint32_t chunk_size, uint64_t len, mtc_
   best->rows = r.leaf.rows;
   best->ctas_per_sm = r.leaf.ctas_per_sm;
   best->direct = r.leaf.direct;
+  best->threads_per_chunk = r.leaf.threads_per_chunk;
   best->max_load = r.max_load;
   if (best_ms) *best_ms = r.ms;
   if (default_ms) *default_ms = r.default_ms;

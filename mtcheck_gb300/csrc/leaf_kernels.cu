@@ -15,6 +15,7 @@
 //   basic -- src/basic_approach.cpp:25-46
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <atomic>
 #include <mutex>
 #include <utility>
@@ -306,6 +307,237 @@ __global__ void leaf_direct_kernel(LeafArgs a, uint32_t c0, uint32_t c1) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// One persistent launch for the leaf pass of many deduplicators (a batch).
+// A device work queue holds (member, tile) items; each CTA's producer lane
+// claims the next item with one atomicAdd and streams its boxes through the
+// same full/empty mbarrier pipeline as leaf_tma_kernel, announcing in a small
+// per-stage record which member, tile and column step each box belongs to.
+// Members differ in chunk size (box width 64 or 128 bytes), digest and
+// approach; every consumer thread owns one row of the current item and ends
+// with that member's epilogue.  Items are ordered largest first.  A producer
+// that finds the queue empty drains its copies, then sends one record
+// without data that stops the CTA's consumers.
+// ---------------------------------------------------------------------------
+struct BatchStageMeta {
+  uint32_t member, tile, xs, flags;  // flags: kMetaFirst | kMetaLast | kMetaDone
+};
+constexpr uint32_t kMetaFirst = 1, kMetaLast = 2, kMetaDone = 4;
+constexpr uint32_t kBatchStageBytes = kBatchRows * 128;
+
+__device__ __forceinline__ bool needs_old_rt(const LeafArgs& a) {
+  return a.epi != EPI_HASH && !(a.epi == EPI_BASIC && a.basic_first);
+}
+
+__global__ void __launch_bounds__(kBatchRows + 32, 3) batch_leaf_kernel(BatchLeafParams p) {
+  pdl_enter();
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kBatchStageBytes);
+  uint64_t* empty = full + kStages;
+  BatchStageMeta* meta = reinterpret_cast<BatchStageMeta*>(empty + kStages);
+  const int tid = threadIdx.x;
+  const uint32_t limit = p.spin_limit ? p.spin_limit : kMbarSpinLimit;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kBatchRows / 32);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  if (tid >= kBatchRows) {
+    if (tid == kBatchRows) {
+      uint32_t it = 0;
+      uint32_t* err = p.members[0].la.err;
+      bool ok = true;
+      while (ok) {
+        const uint32_t k = atomicAdd(p.head, 1u);
+        if (k >= p.nitems) break;
+        const uint2 item = p.items[k];
+        const uint32_t m = item.x, tile = item.y;
+        const uint32_t xsteps = p.members[m].xsteps, W = p.members[m].W;
+        err = p.members[m].la.err;
+        for (uint32_t xs = 0; xs < xsteps; xs++, it++) {
+          const uint32_t s = it % kStages, ph = (it / kStages) & 1;
+          if (!mbar_wait(&empty[s], ph ^ 1, limit)) {
+            raise_err(err, DERR_SPIN);
+            ok = false;
+            break;
+          }
+          meta[s] = BatchStageMeta{m, tile, xs, (xs == 0 ? kMetaFirst : 0u) | (xs + 1 == xsteps ? kMetaLast : 0u)};
+          mbar_arrive_expect_tx(&full[s], kBatchRows * W);
+          tma_load_2d(smem + s * kBatchStageBytes, &p.members[m].map, (int32_t)(xs * W), (int32_t)(tile * kBatchRows),
+                      &full[s]);
+        }
+      }
+      // drain: every issued box lands before the CTA exits (before the stop
+      // record, which reuses the slot of the oldest of them)
+      const uint32_t first = it > (uint32_t)kStages ? it - kStages : 0;
+      for (uint32_t j2 = first; j2 < it; j2++) mbar_wait(&full[j2 % kStages], (j2 / kStages) & 1, limit);
+      if (ok) {
+        // the stop record: no data, the arrive alone completes the phase
+        const uint32_t s = it % kStages, ph = (it / kStages) & 1;
+        if (mbar_wait(&empty[s], ph ^ 1, limit)) {
+          meta[s] = BatchStageMeta{0, 0, 0, kMetaDone};
+          mbar_arrive(&full[s]);
+        } else {
+          raise_err(err, DERR_SPIN);
+        }
+      }
+    }
+    return;
+  }
+
+  const uint32_t lane = tid & 31;
+  Murmur3State mm;
+  Md5State md;
+  mm.init();
+  md.init();
+  Digest old{{0, 0, 0, 0}};
+  uint32_t c = 0;
+  bool valid = false;
+  for (uint32_t it = 0;; it++) {
+    const uint32_t s = it % kStages, ph = (it / kStages) & 1;
+    if (!mbar_wait(&full[s], ph, limit)) {
+      raise_err(p.members[0].la.err, DERR_SPIN);
+      return;
+    }
+    const BatchStageMeta mt = meta[s];
+    if (mt.flags & kMetaDone) return;
+    const MemberLeaf& ml = p.members[mt.member];
+    const LeafArgs& a = ml.la;
+    const uint32_t W = ml.W;
+    const bool md5 = a.hash_kind == HASH_MD5;
+    if (mt.flags & kMetaFirst) {
+      c = mt.tile * kBatchRows + tid;
+      valid = c < ml.n_full;
+      old = Digest{{0, 0, 0, 0}};
+      if (valid && needs_old_rt(a)) old = ld_digest(a.prev + c);
+      mm.init();
+      md.init();
+    }
+    // the row into registers, then the stage goes back to the producer
+    const uint8_t* stage = smem + s * kBatchStageBytes;
+    uint4 row[8];
+    if (W == 128) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) row[q] = *reinterpret_cast<const uint4*>(stage + swz<128>((uint32_t)tid * 128 + q * 16));
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) row[q] = *reinterpret_cast<const uint4*>(stage + swz<64>((uint32_t)tid * 64 + q * 16));
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    const int nblk = W == 128 ? 2 : 1;
+    if (md5) {
+      uint32_t X[16];
+      for (int blk = 0; blk < nblk; blk++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const uint4 v = row[blk * 4 + q];
+          X[4 * q] = v.x; X[4 * q + 1] = v.y; X[4 * q + 2] = v.z; X[4 * q + 3] = v.w;
+        }
+        md.block(X);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (q < 4 * nblk) mm.block(row[q].x, row[q].y, row[q].z, row[q].w);
+    }
+    if (mt.flags & kMetaLast) {
+      Digest dg;
+      if (md5) {
+        uint32_t X[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) X[i] = 0;
+        dg = md.finish(X, 0, a.cs);
+      } else {
+        dg = mm.finish(a.cs);
+      }
+      switch (a.epi) {
+        case EPI_TREE: leaf_epilogue<EPI_TREE>(a, valid, c, dg, old); break;
+        case EPI_LIST: leaf_epilogue<EPI_LIST>(a, valid, c, dg, old); break;
+        case EPI_BASIC: leaf_epilogue<EPI_BASIC>(a, valid, c, dg, old); break;
+        default: leaf_epilogue<EPI_HASH>(a, valid, c, dg, old); break;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-per-chunk kernel: the lanes of a warp load one chunk together into
+// shared memory (coalesced 4-byte words), then lane 0 hashes it.  The digests
+// are serial chains (each 16-byte Murmur3 block and each 64-byte MD5 block
+// depends on the state left by the previous one), so the other lanes cannot
+// share the hashing; this shape exists for the autotuner to compare against
+// the thread-per-chunk pipelines.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kWarpChunkMax = 4096;
+template <int EPI>
+__global__ void leaf_warp_kernel(LeafArgs a, uint32_t c0, uint32_t c1) {
+  pdl_enter();
+  extern __shared__ uint32_t wsm[];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t stride_w = (a.cs + 64 + 3) / 4;  // words per warp buffer, zero padding included
+  uint32_t* buf = wsm + warp * stride_w;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const bool al4 = (reinterpret_cast<uintptr_t>(a.data) & 3) == 0 && (a.cs & 3) == 0;
+  for (uint64_t c = c0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < c1; c += nwarps) {
+    const uint64_t off = c * (uint64_t)a.cs;
+    const uint32_t nb = c == a.n_chunks - 1 ? (uint32_t)(a.len - off) : a.cs;
+    const uint32_t nw = (nb + 64 + 3) / 4;
+    for (uint32_t i = lane; i < nw; i += 32) {
+      uint32_t v = 0;
+      if (al4 && 4 * i + 4 <= nb) v = __ldg(reinterpret_cast<const uint32_t*>(a.data + off) + i);
+      else v = ld_word_any(a.data + off, 4 * (uint64_t)i, nb);
+      buf[i] = v;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      Digest old{{0, 0, 0, 0}};
+      if (needs_old<EPI>(a)) old = ld_digest(a.prev + c);
+      const Digest dg = hash_words(a.hash_kind, buf, nb);
+      leaf_epilogue<EPI>(a, true, (uint32_t)c, dg, old);
+    }
+    __syncwarp();
+  }
+}
+
+template <int EPI>
+cudaError_t launch_warp(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStream_t s) {
+  if (c1 <= c0) return cudaSuccess;
+  const uint32_t warps_per_block = 8;
+  const size_t smem = (size_t)warps_per_block * 4 * ((a.cs + 64 + 3) / 4);
+  static std::atomic<bool> attr_set{false};
+  if (!attr_set.load(std::memory_order_acquire)) {
+    cudaError_t e = cudaFuncSetAttribute(leaf_warp_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(warps_per_block * 4 * ((kWarpChunkMax + 64 + 3) / 4)));
+    if (e != cudaSuccess) return e;
+    attr_set.store(true, std::memory_order_release);
+  }
+  uint64_t grid = (c1 - c0 + warps_per_block - 1) / warps_per_block;
+  const uint64_t cap = (uint64_t)num_sms() * 8;
+  if (grid > cap) grid = cap;
+  static const bool reg =
+      (register_input_kernel(reinterpret_cast<const void*>(leaf_warp_kernel<EPI>), INPUT_LEAF_DIRECT), true);
+  (void)reg;
+  launch_k(leaf_warp_kernel<EPI>, (uint32_t)grid, warps_per_block * 32, smem, s, a, c0, c1);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t dispatch_warp(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStream_t s) {
+  switch (a.epi) {
+    case EPI_TREE: return launch_warp<EPI_TREE>(a, c0, c1, s);
+    case EPI_LIST: return launch_warp<EPI_LIST>(a, c0, c1, s);
+    case EPI_BASIC: return launch_warp<EPI_BASIC>(a, c0, c1, s);
+    default: return launch_warp<EPI_HASH>(a, c0, c1, s);
+  }
+}
+
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -491,6 +723,7 @@ cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, co
   const bool aligned = (reinterpret_cast<uintptr_t>(a.data) & 15) == 0;
   LeafTune t = tune;
   if (t.rows != 128) t.rows = 256;
+  if (t.threads_per_chunk == 32 && a.cs <= kWarpChunkMax) return dispatch_warp(a, 0, a.n_chunks, s);
   uint32_t done = 0;
   if (!t.direct && W && aligned && n_full > 0 && cache && make_tmap(cache, a.data, a.len, a.cs, W, t.rows, n_full)) {
     cudaError_t e = dispatch_tma(a, cache->map, n_full, W, t, s);
@@ -498,6 +731,54 @@ cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, co
     done = n_full;
   }
   return dispatch_direct(a, done, a.n_chunks, s);
+}
+
+bool batch_leaf_member(MemberLeaf* out, const LeafArgs& a) {
+  const int W = tma_width(a.cs);
+  const uint32_t n_full = (uint32_t)(a.len / a.cs);
+  if ((W != 64 && W != 128) || n_full == 0 || (reinterpret_cast<uintptr_t>(a.data) & 15) != 0) return false;
+  TmaCache cache;
+  if (!make_tmap(&cache, a.data, a.len, a.cs, W, kBatchRows, n_full)) return false;
+  std::memcpy(&out->map, &cache.map, sizeof(CUtensorMap));
+  out->la = a;
+  out->n_full = n_full;
+  out->W = (uint32_t)W;
+  out->xsteps = a.cs / (uint32_t)W;
+  out->pad = 0;
+  return true;
+}
+
+cudaError_t launch_leaf_range(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStream_t s) {
+  return dispatch_direct(a, c0, c1, s);
+}
+
+static size_t batch_leaf_smem() {
+  return 1024 + (size_t)kStages * kBatchStageBytes + 2 * kStages * sizeof(uint64_t) + kStages * sizeof(BatchStageMeta);
+}
+
+cudaError_t batch_leaf_node_params(const BatchLeafParams& p, cudaKernelNodeParams* kp, void** args) {
+  static std::atomic<bool> attr_set{false};
+  const size_t smem = batch_leaf_smem();
+  if (!attr_set.load(std::memory_order_acquire)) {
+    cudaError_t e = cudaFuncSetAttribute(batch_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set.store(true, std::memory_order_release);
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_leaf_kernel, kBatchRows + 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  if (per_sm > 3) per_sm = 3;
+  uint32_t grid = (uint32_t)(num_sms() * per_sm);
+  if (grid > p.nitems && p.nitems > 0) grid = p.nitems;
+  args[0] = const_cast<BatchLeafParams*>(&p);
+  kp->func = reinterpret_cast<void*>(batch_leaf_kernel);
+  kp->gridDim = dim3(grid);
+  kp->blockDim = dim3(kBatchRows + 32);
+  kp->sharedMemBytes = (unsigned)smem;
+  kp->kernelParams = args;
+  kp->extra = nullptr;
+  return cudaSuccess;
 }
 
 cudaError_t launch_leaf_inserts(const LeafArgs& a, cudaStream_t s) {

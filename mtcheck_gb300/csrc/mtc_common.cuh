@@ -233,6 +233,31 @@ __device__ inline Digest hash_bytes(int kind, const uint8_t* p, uint64_t len) {
   return s.finish(len);
 }
 
+// Digest of `len` bytes held in a 4-byte aligned buffer that is zero from
+// `len` up to the next 64-byte boundary (shared memory staging).
+__device__ inline Digest hash_words(int kind, const uint32_t* w, uint32_t len) {
+  if (kind == HASH_MD5) {
+    Md5State s; s.init();
+    uint32_t X[16];
+    uint32_t off = 0;
+    for (; off + 64 <= len; off += 64) {
+#pragma unroll
+      for (int i = 0; i < 16; i++) X[i] = w[off / 4 + i];
+      s.block(X);
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) X[i] = w[off / 4 + i];
+    return s.finish(X, len - off, len);
+  }
+  Murmur3State s; s.init();
+  uint32_t off = 0;
+  for (; off + 16 <= len; off += 16) s.block(w[off / 4], w[off / 4 + 1], w[off / 4 + 2], w[off / 4 + 3]);
+  const uint64_t t0 = ((uint64_t)w[off / 4 + 1] << 32) | w[off / 4];
+  const uint64_t t1 = ((uint64_t)w[off / 4 + 3] << 32) | w[off / 4 + 2];
+  s.tail(t0, t1, len - off);
+  return s.finish(len);
+}
+
 // ---------------------------------------------------------------------------
 // Merkle heap index arithmetic, include/kokkos_merkle_tree.hpp:102-142
 // (exact only for a power-of-two leaf count; restated as written).

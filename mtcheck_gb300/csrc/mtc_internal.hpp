@@ -79,10 +79,15 @@ struct TmaCache {
 //                  that fit in shared memory, at most 3)
 //   direct      -- 1: every thread loads its own chunk from global memory
 //                  instead of the TMA-staged shared-memory pipeline
+//   threads_per_chunk -- 1: one thread hashes one chunk (the pipelines
+//                  above); 32: one warp per chunk, its lanes loading the
+//                  chunk together into shared memory and one lane hashing it
+//                  (chunks of 1 to 4096 bytes)
 struct LeafTune {
   int rows = 256;
   int ctas_per_sm = 0;
   int direct = 0;
+  int threads_per_chunk = 1;
 };
 // Default shape per digest, measured at 4 GiB / 512 B: Murmur3 tiles of 128
 // rows, two CTAs per SM (0.652 ms against 0.691 for 256 rows); MD5, whose
@@ -95,12 +100,53 @@ inline LeafTune default_leaf_tune(int hash_kind) {
 // for chunk sizes that are a multiple of 128 bytes (or 16/32/64) on 16-byte
 // aligned buffers, and a thread-per-chunk kernel otherwise and for the tail.
 cudaError_t launch_leaves(const LeafArgs& a, TmaCache* cache, cudaStream_t s, const LeafTune& tune = LeafTune{});
+// The leaf pass of many deduplicators in one persistent launch (a batch):
+// one record per member (its TMA descriptor with boxes of kBatchRows rows,
+// its leaf arguments) and a work queue of (member, tile) items.
+constexpr int kBatchRows = 128;
+struct MemberLeaf {  // aligned as CUtensorMap
+  CUtensorMap map;
+  LeafArgs la;
+  uint32_t n_full, W, xsteps, pad;
+};
+static_assert(alignof(MemberLeaf) % 64 == 0, "a TMA descriptor in global memory is 64-byte aligned");
+struct BatchLeafParams {
+  const MemberLeaf* members;
+  const uint2* items;   // (member, tile), largest first
+  uint32_t nitems;
+  uint32_t spin_limit;  // 0: the default bound
+  uint32_t* head;       // next item to claim, zero before every launch
+};
+// Fills a member's record from its leaf arguments; false when the member's
+// leaves cannot go through the batched launch (chunk size other than 64 or a
+// multiple of 128 bytes, an input not 16-byte aligned, no full chunk).
+bool batch_leaf_member(MemberLeaf* out, const LeafArgs& a);
+// Kernel node parameters of the batched leaf launch (args: one slot).
+cudaError_t batch_leaf_node_params(const BatchLeafParams& p, cudaKernelNodeParams* kp, void** args);
+// The leaf kernel for chunks [c0, c1) only, one thread per chunk.
+cudaError_t launch_leaf_range(const LeafArgs& a, uint32_t c0, uint32_t c1, cudaStream_t s);
+
 // Tree / list: map inserts of the changed chunks collected by launch_leaves,
 // then the lowest-offset demotion (src/tree_approach.cpp:356-369; for the
 // list a changed chunk is a first occurrence only if it owns its digest).
 cudaError_t launch_leaf_inserts(const LeafArgs& a, cudaStream_t s);
 
 int num_sms();
+
+// Small device results to pinned host memory, written by a kernel through the
+// memory's device mapping instead of copied: copies of a few bytes would
+// queue on the copy engines behind large transfers of other streams (an
+// upload, another process's spill).  Up to three (src, dst, words) segments;
+// dst is the device alias of pinned memory (host_alias).
+struct Readback {
+  const uint32_t* src[3];
+  uint32_t* dst[3];
+  uint32_t words[3];
+};
+cudaError_t launch_readback(const Readback& r, cudaStream_t s);
+// The device address of pinned host memory (the same pointer under unified
+// addressing).
+void* host_alias(void* pinned);
 
 // Kernel launch with programmatic stream serialization (see pdl_enter): the
 // kernel may be scheduled while its predecessor finishes, hiding the launch

@@ -60,8 +60,12 @@ def member_diff(mtc, m):
     return host.tobytes()
 
 
-@pytest.mark.parametrize("use_graph", [True, False], ids=["graph", "eager"])
-def test_batch_equals_lone_handles(cuda, mtc, states, lone, use_graph):
+@pytest.mark.parametrize("use_graph,leaf_launch", [(True, False), (True, True), (False, False)],
+                         ids=["graph", "graph-one-leaf-launch", "eager"])
+def test_batch_equals_lone_handles(cuda, mtc, states, lone, use_graph, leaf_launch, monkeypatch):
+    # leaf_launch: every member's leaves in one persistent launch driven by a
+    # device work queue (MTCHECK_BATCH_LEAF=1) instead of a leaf kernel per member
+    monkeypatch.setenv("MTCHECK_BATCH_LEAF", "1" if leaf_launch else "0")
     b = mtc.Batch([m[:3] for m in MIX])
     b.set_options(use_graph=use_graph)
     bufs = [cuda.empty(m[3], dtype=cuda.uint8, device="cuda") for m in MIX]
@@ -71,6 +75,11 @@ def test_batch_equals_lone_handles(cuda, mtc, states, lone, use_graph):
         sizes = b.checkpoint(bufs, make_baseline=(step == 0))
         info = b.info()
         assert info.last_used_graph == (1 if (use_graph and step > 0) else 0)
+        # graph steps hash every member's leaves in one persistent launch
+        # driven by a device work queue (all members but the full approach,
+        # which has no leaves)
+        if info.last_used_graph:
+            assert info.batched_leaf_members == (sum(1 for m in MIX if m[0] != 1) if leaf_launch else 0)
         for i, m in enumerate(b.members):
             got = member_diff(mtc, m)
             assert sizes[i] == len(got)
@@ -154,7 +163,7 @@ def test_member_handles_are_owned(cuda, mtc):
 @pytest.mark.parametrize("tune", [
     dict(rows=128), dict(rows=256, ctas_per_sm=1), dict(rows=128, ctas_per_sm=4), dict(direct=1),
     dict(max_load=0.5), dict(max_load=0.9), dict(rows=128, ctas_per_sm=2, max_load=0.6), dict(eager=1),
-    dict(direct=1, eager=1),
+    dict(direct=1, eager=1), dict(threads_per_chunk=32), dict(threads_per_chunk=32, eager=1),
 ])
 def test_tuning_does_not_change_output(cuda, mtc, states, lone, tune):
     for i in (0, 1, 3, 4, 5, 6):
@@ -170,6 +179,23 @@ def test_autotune(cuda, mtc):
     t, best, dflt = mtc.autotune(4, 0, 512, 16 << 20)
     assert t["rows"] in (128, 256) and 0.1 < t["max_load"] <= 0.95
     assert 0 < best <= dflt
+    # 4096 B chunks: the warp-per-chunk shape is among the candidates
+    t, best, dflt = mtc.autotune(4, 1, 4096, 16 << 20)
+    assert t["threads_per_chunk"] in (1, 32) and 0 < best <= dflt
+
+
+@pytest.mark.parametrize("cs,nbytes", [(4096, (1 << 20) + 1000), (24, 64 * 1024 + 5), (1, 3000)])
+@pytest.mark.parametrize("kind", [0, 1], ids=["murmur3", "md5"])
+def test_warp_per_chunk_matches_oracle(cuda, mtc, oracle, cs, nbytes, kind):
+    # one warp per chunk (coalesced loads, one lane hashing) gives the oracle's bytes
+    seq = [s.copy() for s in workloads.pattern2(nbytes, cs, 4, seed=cs, zero_range=(nbytes // 4, nbytes // 2))]
+    for approach in (2, 3, 4):
+        ref = oracle.Deduplicator(approach, cs, kind)
+        d = mtc.Deduplicator(cs, kind, approach=approach)
+        d.set_tuning(threads_per_chunk=32)
+        for i, s in enumerate(seq):
+            assert d.checkpoint(cuda.from_numpy(s).cuda(), i == 0) == ref.checkpoint(s, i == 0), (approach, i)
+        d.close()
 
 
 def test_batch_autotune_keeps_output(cuda, mtc, states, lone):
