@@ -72,6 +72,8 @@ def parse():
     p.add_argument("--serve-inflight", type=int, default=64)
     p.add_argument("--serve-verify-procs", type=int, default=4)
     p.add_argument("--serve-pinned-gb", type=float, default=32.0)
+    p.add_argument("--serve-sat-procs", type=int, default=64,
+                   help="processes the capacity run draws its requests from (both arms)")
     p.add_argument("--serve-sat-requests", type=int, default=3000,
                    help="requests of the capacity run (all arriving at once), also run one call at a time")
     return p.parse_args()
@@ -669,23 +671,24 @@ def serve_bench(torch, mc, dev, a):
     # capacity: the same kind of requests all arriving at once (each process
     # still has one request on the server at a time)
     n_sat = a.serve_sat_requests
+    P_sat = min(P, a.serve_sat_procs)
     sat_rst = rng.random(n_sat) < 0.05
-    sat_who = rng.integers(0, P, n_sat)
+    sat_who = rng.integers(0, P_sat, n_sat)
     lat_s, _, bytes_s, wall_s = stream(np.zeros(n_sat), sat_rst, sat_who)
     sat_lat = lat_s["checkpoint"] + lat_s["restart"]
     # the one-buffer-per-call path on the same requests: one lone handle per
     # process (a baseline of the process's current state first, untimed),
     # every request a synchronous call in arrival order, each new checkpoint
     # kept in HBM for the restarts as the server keeps its chains
-    pc_bufs = [b.clone() for b in bufs]
-    lones = [mc.TreeDeduplicator(m["chunk_size"], kind) for m in mix]
-    pc_chain = [[] for _ in range(P)]
+    pc_bufs = [b.clone() for b in bufs[:P_sat]]
+    lones = [mc.TreeDeduplicator(m["chunk_size"], kind) for m in mix[:P_sat]]
+    pc_chain = [[] for _ in range(P_sat)]
 
     def keep_diff(p):
         ptr, ln = lones[p].diff_device()
         pc_chain[p].append(torch.as_tensor(_DevView(ptr, ln), device=dev).clone())
 
-    for p in range(P):
+    for p in range(P_sat):
         lones[p].checkpoint_device(pc_bufs[p], True)
         keep_diff(p)
     pc_step = list(step)
@@ -710,15 +713,16 @@ def serve_bench(torch, mc, dev, a):
     del lones, pc_bufs, pc_chain
     torch.cuda.empty_cache()
     saturation = {
-        "requests": n_sat, "restarts": int(sat_rst.sum()),
+        "requests": n_sat, "restarts": int(sat_rst.sum()), "processes": P_sat,
         "served_rate": round(n_sat / wall_s, 1), "served_gbs": round(bytes_s / wall_s / 1e9, 3),
         "per_call_rate": round(n_sat / wall_pc, 1),
         "speedup_vs_per_call": round(wall_pc / wall_s, 3),
         "served_latency_ms": {"p50": round(float(np.percentile(sat_lat, 50)), 3),
                               "p99": round(float(np.percentile(sat_lat, 99)), 3)},
-        "note": "all requests arrive at once; served: the request server (continuous admission, overlapped on "
-                "the device); per_call: one synchronous call per request through one lone handle per process, "
-                "starting from a baseline of the same states, each checkpoint kept in HBM",
+        "note": "all requests arrive at once, for the first `processes` processes; served: the request server "
+                "(continuous admission, overlapped on the device); per_call: one synchronous call per request "
+                "through one lone handle per process, starting from a baseline of the same states, each "
+                "checkpoint kept in HBM",
     }
     st = srv.stats()
     # every restart against the state it restores: replay each process's

@@ -120,7 +120,12 @@ int mtc_checkpoint_file(mtc_dedup_t* h, const void* dev_data, uint64_t len, cons
 
 /* restart(uint8_t*, size_t, std::vector<HostMirror>&, std::string&, uint32_t),
  * :142-146: rebuilds checkpoint `chkpt_id` of the chain `host_diffs[0..n)` into
- * the device buffer `dev_out` of `len` == header.datalen bytes */
+ * the device buffer `dev_out` of `len` == header.datalen bytes.  Where the GPU
+ * can read the host memory (pinned memory; pageable memory on a system with
+ * cudaDevAttrPageableMemoryAccess, such as Grace), the kernels read the chain
+ * in place; elsewhere, or with MTCHECK_RESTART_HOST=stage in the environment,
+ * the chain is first copied to device memory.  Returns when the restart is
+ * complete; the host buffers may be released then. */
 int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* host_diffs, const uint64_t* lens,
                 uint32_t n, uint32_t chkpt_id);
 /* same, with the chain already resident in device memory; the diffs must be

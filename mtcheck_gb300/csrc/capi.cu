@@ -186,13 +186,35 @@ int mtc_release_restart_buffers(mtc_dedup_t* h) {
   return MTC_OK;
 }
 
+namespace {
+// Can the restart kernels read this host memory in place?  Pinned memory
+// always can (through its device alias); ordinary pageable memory can on a
+// system whose GPU reads the host's page tables (NVLink-C2C with ATS on
+// Grace, cudaDevAttrPageableMemoryAccess).
+const uint8_t* device_view(const void* host) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+    return static_cast<const uint8_t*>(at.devicePointer);
+  cudaGetLastError();
+  static int pageable = -1;
+  if (pageable < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) v = 0;
+    pageable = v;
+  }
+  return pageable ? static_cast<const uint8_t*>(host) : nullptr;
+}
+bool restart_in_place() {
+  const char* e = std::getenv("MTCHECK_RESTART_HOST");
+  return !(e && std::strcmp(e, "stage") == 0);
+}
+}  // namespace
+
 int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* host_diffs, const uint64_t* lens,
                 uint32_t n, uint32_t chkpt_id) {
   if (!h || !dev_out || !host_diffs || !lens) return ret(MTC_EINVAL, "NULL argument");
   if (chkpt_id >= n) return ret(MTC_EINVAL, "checkpoint id outside the chain");
-  // the reference copies each diff of the chain to the device as it walks it
-  // (src/tree_approach.cpp:756, :962); here the whole used part of the chain
-  // is staged once
   std::vector<mtc::HeaderHost> hdrs(n);
   std::vector<const uint8_t*> ptrs(n, nullptr);
   std::vector<uint64_t> l(lens, lens + n);
@@ -201,6 +223,22 @@ int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* 
     if (h->eng->mode() != MTC_FULL && l[i] >= sizeof(mtc::HeaderHost)) std::memcpy(&hdrs[i], host_diffs[i], sizeof(mtc::HeaderHost));
     else std::memset(&hdrs[i], 0, sizeof(hdrs[i]));
     if (i <= chkpt_id) total += (l[i] + 255) & ~uint64_t(255);
+  }
+  // In place: the kernels read the chain where it lies in host memory, only
+  // the bytes the restart needs (the metadata and each restored chunk once)
+  // instead of a copy of the whole used chain; where the GPU cannot read the
+  // host memory, the chain is staged in device memory first.  The reference
+  // copies each diff to the device as it walks the chain
+  // (src/tree_approach.cpp:756, :962).
+  bool direct = restart_in_place() && h->eng->mode() != MTC_FULL;
+  for (uint32_t i = 0; direct && i <= chkpt_id; i++) {
+    ptrs[i] = device_view(host_diffs[i]);
+    if (!ptrs[i] && l[i]) direct = false;
+  }
+  if (direct) {
+    int rc = h->eng->restart(static_cast<uint8_t*>(dev_out), len, ptrs, l, hdrs, chkpt_id);
+    if (rc == MTC_OK) h->eng->restart_timers[0] = 0;  // no staging copy
+    return ret_eng(rc, h->eng);
   }
   uint8_t* dev = nullptr;
   if (cudaMalloc(&dev, total ? total : 1) != cudaSuccess) return ret(MTC_ENOMEM, "cannot stage the chain");

@@ -32,6 +32,28 @@ static __global__ void params_in_kernel(StepParams p, StepParams* dev, uint32_t*
 // Polls of an injected stall's bounded waits (about a millisecond).
 constexpr uint32_t kInjectedSpinLimit = 1u << 14;
 
+static __global__ void readback_kernel(Readback r) {
+  pdl_enter();
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    for (uint32_t i = threadIdx.x; i < r.words[k]; i += blockDim.x) r.dst[k][i] = r.src[k][i];
+}
+
+cudaError_t launch_readback(const Readback& r, cudaStream_t s) {
+  launch_k(readback_kernel, 1, 32, 0, s, r);
+  note_launch();
+  return cudaGetLastError();
+}
+
+void* host_alias(void* pinned) {
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, pinned, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return pinned;
+  }
+  return d;
+}
+
 static uint64_t next_pow2(uint64_t v) {
   uint64_t c = 1;
   while (c < v) c <<= 1;
@@ -254,7 +276,8 @@ int Engine::run_tree(const uint8_t* data, uint64_t len, bool baseline_path) {
     la.spin_limit = kInjectedSpinLimit;
   }
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
-  MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
+  if (leaf_hook_) MTC_TRY(leaf_hook_->on_leaves(this, la, stream_));
+  else MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_TRY(mark(4));
   MTC_CUDA(launch_leaf_inserts(la, stream_));
 
@@ -309,7 +332,8 @@ int Engine::run_list_basic(const uint8_t* data, uint64_t len) {
     la.spin_limit = kInjectedSpinLimit;
   }
   MTC_CUDA(cudaMemsetAsync(changed_count_.p, 0, 4 * sizeof(uint32_t), stream_));
-  MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
+  if (leaf_hook_) MTC_TRY(leaf_hook_->on_leaves(this, la, stream_));
+  else MTC_CUDA(launch_leaves(la, &tma_, stream_, leaf_tune_));
   if (timed_) MTC_TRY(mark(4));
   if (mode_ == MODE_LIST) MTC_CUDA(launch_leaf_inserts(la, stream_));
   MTC_CUDA(launch_chunk_compaction(labels_.p, N_, mode_ == MODE_BASIC ? 1 : 0, fo_list_.p, sh_list_.p, lay_.p, scan_.p,
@@ -381,10 +405,22 @@ int Engine::enqueue(const uint8_t* data, uint64_t len, bool timed) {
   if (timed) MTC_TRY(mark(2));
   MTC_CUDA(launch_assemble(gather_args(data, len), (uint64_t)N_ + 1, stream_));
   if (timed) MTC_TRY(mark(3));
-  // results by device-to-host copies: that direction has its own copy engine
-  MTC_CUDA(cudaMemcpyAsync(lay_host_, lay_.p, sizeof(Layout), cudaMemcpyDeviceToHost, stream_));
-  MTC_CUDA(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
-  if (map_size_.p) MTC_CUDA(cudaMemcpyAsync(err_host_ + 1, map_size_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+  // results (layout, error word, map size) written to pinned memory by a
+  // kernel, not queued on a copy engine behind other streams' transfers
+  static_assert(sizeof(Layout) % 4 == 0, "layout copied as words");
+  Readback rb{};
+  rb.src[0] = reinterpret_cast<const uint32_t*>(lay_.p);
+  rb.dst[0] = static_cast<uint32_t*>(host_alias(lay_host_));
+  rb.words[0] = sizeof(Layout) / 4;
+  rb.src[1] = err_.p;
+  rb.dst[1] = static_cast<uint32_t*>(host_alias(err_host_));
+  rb.words[1] = 1;
+  if (map_size_.p) {
+    rb.src[2] = map_size_.p;
+    rb.dst[2] = rb.dst[1] + 1;
+    rb.words[2] = 1;
+  }
+  MTC_CUDA(launch_readback(rb, stream_));
   return ST_OK;
 }
 
@@ -664,7 +700,8 @@ uint64_t Engine::shape_signature(const uint8_t* data, uint64_t len) const {
                         (uint64_t)rank_.p, (uint64_t)fo_val_.p, (uint64_t)sort_mat_.p, sort_mat_.n, (uint64_t)scan_.p,
                         (uint64_t)scan_total_.p, (uint64_t)scan2_.p, (uint64_t)scan_total2_.p, (uint64_t)stage_.p,
                         stage_.n, (uint64_t)lay_.p, (uint64_t)sp_.p, (uint64_t)baseline_path_, (uint64_t)mode_,
-                        (uint64_t)leaf_tune_.rows, (uint64_t)leaf_tune_.ctas_per_sm, (uint64_t)leaf_tune_.direct};
+                        (uint64_t)leaf_tune_.rows, (uint64_t)leaf_tune_.ctas_per_sm, (uint64_t)leaf_tune_.direct,
+                        (uint64_t)leaf_tune_.threads_per_chunk};
   uint64_t h = 1469598103934665603ull;
   for (uint64_t x : v) h = (h ^ x) * 1099511628211ull;
   return h;

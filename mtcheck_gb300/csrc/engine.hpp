@@ -189,6 +189,16 @@ class Engine {
   void set_order_after_legacy(bool on) { order_after_legacy_ = on; }
   int order_inputs();
   uint32_t launches() const { return launches_; }
+  // A batch takes over the leaf pass of its members' captured sequences:
+  // while a hook is set, the sequence calls it where it would launch the
+  // leaf kernels.
+  struct LeafHook {
+    virtual int on_leaves(Engine* e, const LeafArgs& la, cudaStream_t s) = 0;
+    virtual ~LeafHook() {}
+  };
+  void set_leaf_hook(LeafHook* h) { leaf_hook_ = h; }
+  // The engine's own leaf launch (its descriptor cache and launch shape).
+  cudaError_t launch_own_leaves(const LeafArgs& la, cudaStream_t s) { return launch_leaves(la, &tma_, s, leaf_tune_); }
   // Fault injection for tests: the next n checkpoints run eagerly with the
   // chunk-hashing kernel's copy producer silent, so its bounded waits run
   // out and the checkpoint fails with ST_ETIMEOUT.
@@ -251,6 +261,7 @@ class Engine {
   int mark(int i);
   void drop_own_graph();
   bool stream_work_ = false;
+  LeafHook* leaf_hook_ = nullptr;
   uint32_t stall_left_ = 0;
   bool stall_now_ = false, need_baseline_ = false;
   uint32_t epoch_ = 0;

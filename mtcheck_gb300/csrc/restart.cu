@@ -1355,7 +1355,11 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   restore_copy_kernel<<<num_sms() * 3, 256, 0, s>>>(a);
   note_launch(2);
   cudaEventRecord(e1, s);
-  MTC_CUDA_R(cudaMemcpyAsync(err_host_, err_.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  Readback rb{};
+  rb.src[0] = err_.p;
+  rb.dst[0] = static_cast<uint32_t*>(host_alias(err_host_));
+  rb.words[0] = 1;
+  MTC_CUDA_R(launch_readback(rb, s));
   return ST_OK;
 }
 
