@@ -72,6 +72,8 @@ def parse():
     p.add_argument("--serve-inflight", type=int, default=64)
     p.add_argument("--serve-verify-procs", type=int, default=4)
     p.add_argument("--serve-pinned-gb", type=float, default=32.0)
+    p.add_argument("--serve-trace", default=None,
+                   help="write one CSV row per request of the timed stream to this file")
     p.add_argument("--serve-sat-procs", type=int, default=64,
                    help="processes the capacity run draws its requests from (both arms)")
     p.add_argument("--serve-sat-requests", type=int, default=3000,
@@ -301,6 +303,44 @@ def series_bench(torch, mc, dev, states, cs, kind, W, flush=None):
         t = evs[0][0].elapsed_time(evs[-1][1]) / 1e3 / len(timed)
     d.close()
     return t, sum(leaf) / len(leaf), sum(sdata) / len(sdata), sum(smeta) / len(smeta)
+
+
+def link_section(torch, dev, nbytes=GIB, reps=3):
+    """The host link's ceiling: pinned 1 GiB copies host->device and
+    device->host, split over 1, 2 and 4 streams (best of `reps`), timed by
+    events on the current stream that every copy stream joins."""
+    host = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    devb = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    devb.copy_(host)  # first pass over the newly pinned pages
+    host.copy_(devb)
+    torch.cuda.synchronize()
+    streams = [torch.cuda.Stream(device=dev) for _ in range(4)]
+    out = {}
+    for name, to_dev in (("h2d_gbs", True), ("d2h_gbs", False)):
+        out[name] = {}
+        for ns in (1, 2, 4):
+            part = nbytes // ns
+            best = None
+            for _ in range(reps):
+                cur = torch.cuda.current_stream()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(cur)
+                for k in range(ns):
+                    streams[k].wait_event(e0)
+                    with torch.cuda.stream(streams[k]):
+                        if to_dev:
+                            devb[k * part:(k + 1) * part].copy_(host[k * part:(k + 1) * part], non_blocking=True)
+                        else:
+                            host[k * part:(k + 1) * part].copy_(devb[k * part:(k + 1) * part], non_blocking=True)
+                for k in range(ns):
+                    cur.wait_stream(streams[k])
+                e1.record(cur)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            out[name][str(ns)] = round(nbytes / (best * 1e-3) / 1e9, 1)
+    del host, devb
+    return out
 
 
 def small_series_section(torch, mc, dev, peak):
@@ -604,10 +644,12 @@ def serve_bench(torch, mc, dev, a):
         pending_checks.append((p, 1, _digest2(mc, kind, outs[0][:nb])))
     rst_ok, rst_checked = True, 0
 
-    def stream(arr, is_rst, who):
+    def stream(arr, is_rst, who, trace=None):
         """Requests arriving at offsets `arr` (ms); returns the latencies,
         (arrival offset, latency) pairs, bytes served and the wall time from
-        the first arrival to the last completion."""
+        the first arrival to the last completion.  `trace`, a list, receives
+        one row per request: arrival, submission, admission and completion
+        (ms from the start), kind, process, buffer bytes."""
         n_req = len(arr)
         queues = [deque() for _ in range(P)]
         busy = [None] * P
@@ -652,6 +694,10 @@ def serve_bench(torch, mc, dev, a):
                 assert c["status"] == 0, c
                 lat[what].append(c["t_done_ms"] - arrival)
                 lat_t.append((arrival - t0, c["t_done_ms"] - arrival))
+                if trace is not None:
+                    trace.append((round(arrival - t0, 3), round(c["t_submit_ms"] - t0, 3),
+                                  round(c["t_admit_ms"] - t0, 3), round(c["t_done_ms"] - t0, 3), what, p,
+                                  mix[p]["nbytes"]))
                 nbytes_done += mix[p]["nbytes"]
                 t_last = max(t_last, c["t_done_ms"])
                 if what == "restart":
@@ -666,8 +712,14 @@ def serve_bench(torch, mc, dev, a):
     # the request stream: Poisson arrivals at the configured rate
     n_req = int(a.serve_rate * a.serve_seconds)
     arr = np.cumsum(rng.exponential(1.0 / a.serve_rate, n_req)) * 1e3
-    lat, lat_t, nbytes_done, wall = stream(arr, rng.random(n_req) < 0.05, rng.integers(0, P, n_req))
+    trace = [] if a.serve_trace else None
+    lat, lat_t, nbytes_done, wall = stream(arr, rng.random(n_req) < 0.05, rng.integers(0, P, n_req), trace)
     st_stream = srv.stats()
+    if trace is not None:
+        with open(a.serve_trace, "w") as f:
+            f.write("arrival_ms,submit_ms,admit_ms,done_ms,kind,process,bytes\n")
+            for row in trace:
+                f.write(",".join(str(x) for x in row) + "\n")
     # capacity: the same kind of requests all arriving at once (each process
     # still has one request on the server at a time)
     n_sat = a.serve_sat_requests
@@ -786,10 +838,12 @@ def serve_bench(torch, mc, dev, a):
         "baseline_s": round(base_s, 2),
         "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
         "server": {k: st[k] for k in ("inflight_peak", "graph_captures", "graph_replays", "spilled_diffs",
-                                      "spilled_states", "restored_states", "staged_diffs", "hbm_peak",
-                                      "deferred_admissions", "failed", "worker_ms")},
-        "server_after_stream": {k: st_stream[k] for k in ("spilled_diffs", "spilled_states", "restored_states",
-                                                          "staged_diffs", "hbm_peak")},
+                                      "spilled_bytes", "spilled_states", "restored_states", "staged_diffs",
+                                      "hbm_peak", "pinned_reserved", "pinned_sync_grows", "deferred_admissions",
+                                      "failed", "worker_ms")},
+        "server_after_stream": {k: st_stream[k] for k in ("spilled_diffs", "spilled_bytes", "spilled_states",
+                                                          "restored_states", "staged_diffs", "hbm_peak",
+                                                          "deferred_admissions")},
         "note": "value: bytes of all completed requests (checkpointed and restarted buffers) / time from the first "
                 "arrival to the last completion; latency: arrival to completion (diff archived in HBM, or "
                 "restarted buffer written)",
@@ -810,6 +864,7 @@ def summary_of(line):
         "dedup_checkpoint_roofline_frac": g(line, "config", "checkpoint_roofline_frac"),
         "leaf_kernel_roofline_frac": g(line, "roofline", "frac"),
         "e2e_gbs": g(line, "e2e", "value"),
+        "e2e_frac_of_link": g(line, "e2e", "link_frac"),
         "dedup_4gib_512b_md5_gbs": g(line, "md5", "value"),
         "md5_leaf_alu_pipe_frac": g(line, "md5", "leaf_alu_pipe_frac_ncu"),
         "dedup_64mib_128b_gbs": g(line, "series_64mib", "value"),
@@ -1015,6 +1070,13 @@ def main():
     md5 = small = None
     if rank == 0 and not a.no_sections:
         md5 = md5_section(torch, mc, dev, states[:1 + W + K], cs, W, peak)
+    if rank == 0 and e2e is not None:
+        # the link bounds e2e: every input byte crosses it once
+        link = link_section(torch, dev)
+        h2d = max(link["h2d_gbs"].values())
+        e2e["link"] = dict(link, note="pinned 1 GiB copies split over 1, 2 and 4 streams; kernels reading pinned "
+                                      "or pageable host memory directly measured the same ceiling")
+        e2e["link_frac"] = round(e2e["value"] / h2d, 3)
     rst = None
     if not a.no_restart and rank == 0:
         del states

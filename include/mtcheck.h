@@ -258,7 +258,8 @@ typedef struct mtc_server_options {
                               while the worker captures one, no thread of the application
                               may synchronise the whole device (cudaDeviceSynchronize) */
   int32_t reserve_hbm;     /* take the whole budget from the device at creation */
-  uint64_t pinned_reserve; /* bytes of pinned host memory for spills, pinned at creation */
+  uint64_t pinned_reserve; /* bytes of pinned host memory for spills, pinned at creation;
+                              a helper thread then keeps an eighth of it pinned ahead of use */
 } mtc_server_options_t;
 #define MTC_REQ_CHECKPOINT 0
 #define MTC_REQ_RESTART 1
@@ -278,7 +279,7 @@ typedef struct mtc_server_stats {
   uint64_t graph_captures, graph_replays;
   uint64_t hbm_used, hbm_peak, pinned_reserved, deferred_admissions;
   uint32_t inflight_peak;
-  uint32_t reserved;
+  uint32_t pinned_sync_grows; /* pinned slabs the worker thread had to pin itself */
   double worker_ms[4];     /* worker host time: starting requests, finishing them,
                               making room (spills), waiting for work */
 } mtc_server_stats_t;

@@ -83,10 +83,11 @@ class ServerStats(ctypes.Structure):
         "submitted", "completed", "failed", "checkpoints", "restarts", "bytes_checkpointed", "bytes_restarted",
         "spilled_diffs", "spilled_states", "restored_states", "staged_diffs", "spilled_bytes", "graph_captures",
         "graph_replays", "hbm_used", "hbm_peak", "pinned_reserved", "deferred_admissions")] + \
-        [("inflight_peak", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("worker_ms", ctypes.c_double * 4)]
+        [("inflight_peak", ctypes.c_uint32), ("pinned_sync_grows", ctypes.c_uint32),
+         ("worker_ms", ctypes.c_double * 4)]
 
     def as_dict(self):
-        d = {n: getattr(self, n) for n, _ in self._fields_ if n not in ("reserved", "worker_ms")}
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "worker_ms"}
         d["worker_ms"] = {k: round(self.worker_ms[j], 2) for j, k in enumerate(("start", "finish", "room", "wait"))}
         return d
 

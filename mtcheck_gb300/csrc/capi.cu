@@ -557,6 +557,7 @@ int mtc_server_get_stats(mtc_server_t* s, mtc_server_stats_t* o) {
   o->graph_captures = t.graph_captures; o->graph_replays = t.graph_replays;
   o->hbm_used = t.hbm_used; o->hbm_peak = t.hbm_peak; o->pinned_reserved = t.pinned_reserved;
   o->deferred_admissions = t.deferred_admissions; o->inflight_peak = t.inflight_peak;
+  o->pinned_sync_grows = (uint32_t)t.pinned_sync_grows;
   for (int k = 0; k < 4; k++) o->worker_ms[k] = t.worker_ms[k];
   return MTC_OK;
 }

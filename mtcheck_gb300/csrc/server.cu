@@ -9,17 +9,29 @@
 
 namespace mtc {
 
+// diff bytes the worker copies out ahead of need in one pass of its loop
+constexpr uint64_t kSpillStepBytes = 64ull << 20;
+
 // ---------------------------------------------------------------------------
 // PinnedArena
 // ---------------------------------------------------------------------------
 PinnedArena::~PinnedArena() {
+  {
+    std::lock_guard<std::mutex> g(mu_);
+    stop_ = true;
+  }
+  cv_.notify_all();
+  if (helper_.joinable()) helper_.join();
   for (uint8_t* p : all_) cudaFreeHost(p);
 }
 
 uint64_t PinnedArena::cls(uint64_t n) {
-  uint64_t c = 64ull << 10;
-  while (c < n) c <<= 1;
-  return c;
+  constexpr uint64_t kMin = 64ull << 10;
+  if (n <= kMin) return kMin;
+  uint64_t p = kMin;
+  while (p * 2 <= n) p <<= 1;  // p <= n < 2p
+  const uint64_t q = p / 4;
+  return (n + q - 1) / q * q;
 }
 
 bool PinnedArena::add_slab(uint64_t bytes) {
@@ -28,47 +40,89 @@ bool PinnedArena::add_slab(uint64_t bytes) {
     cudaGetLastError();
     return false;
   }
+  std::lock_guard<std::mutex> g(mu_);
   all_.push_back(static_cast<uint8_t*>(q));
   slabs_.push_back({static_cast<uint8_t*>(q), bytes});
   reserved_ += bytes;
+  spare_ += bytes;
   return true;
 }
 
 bool PinnedArena::reserve(uint64_t bytes) {
   constexpr uint64_t kGiB = 1ull << 30, kMin = 256ull << 20;
-  while (reserved_ < bytes) {
-    const uint64_t left = bytes - reserved_;
+  while (reserved() < bytes) {
+    const uint64_t left = bytes - reserved();
     const uint64_t slab = left < kMin ? kMin : (left < kGiB ? left : kGiB);
     if (!add_slab(slab)) return false;
   }
   return true;
 }
 
-uint8_t* PinnedArena::alloc(uint64_t n) {
-  const uint64_t c = cls(n);
-  auto& fl = free_[c];
-  if (!fl.empty()) {
-    uint8_t* p = fl.back();
-    fl.pop_back();
-    return p;
+void PinnedArena::keep_spare(int device, uint64_t bytes) {
+  std::lock_guard<std::mutex> g(mu_);
+  spare_target_ = bytes;
+  if (!helper_.joinable() && bytes) helper_ = std::thread([this, device] { helper(device); });
+}
+
+void PinnedArena::helper(int device) {
+  cudaSetDevice(device);
+  std::unique_lock<std::mutex> g(mu_);
+  while (!stop_) {
+    cv_.wait(g, [&] { return stop_ || spare_ < spare_target_; });
+    if (stop_) break;
+    g.unlock();
+    const bool ok = add_slab(1ull << 30);
+    g.lock();
+    if (!ok) spare_target_ = 0;  // host memory exhausted: stop trying
   }
+}
+
+uint64_t PinnedArena::reserved() {
+  std::lock_guard<std::mutex> g(mu_);
+  return reserved_;
+}
+
+uint64_t PinnedArena::sync_grows() {
+  std::lock_guard<std::mutex> g(mu_);
+  return sync_grows_;
+}
+
+uint8_t* PinnedArena::carve(uint64_t c) {
   for (Slab& sl : slabs_)
     if (sl.left >= c) {
       uint8_t* p = sl.next;
       sl.next += c;
       sl.left -= c;
+      spare_ -= c;
       return p;
     }
+  return nullptr;
+}
+
+uint8_t* PinnedArena::alloc(uint64_t n) {
+  const uint64_t c = cls(n);
+  {
+    std::lock_guard<std::mutex> g(mu_);
+    auto& fl = free_[c];
+    if (!fl.empty()) {
+      uint8_t* p = fl.back();
+      fl.pop_back();
+      return p;
+    }
+    uint8_t* p = carve(c);
+    if (spare_ < spare_target_) cv_.notify_one();
+    if (p) return p;
+    sync_grows_++;
+  }
   if (!add_slab(std::max<uint64_t>(c, 256ull << 20))) return nullptr;
-  Slab& sl = slabs_.back();
-  uint8_t* p = sl.next;
-  sl.next += c;
-  sl.left -= c;
-  return p;
+  std::lock_guard<std::mutex> g(mu_);
+  return carve(c);
 }
 
 void PinnedArena::free(uint8_t* p, uint64_t n) {
-  if (p) free_[cls(n)].push_back(p);
+  if (!p) return;
+  std::lock_guard<std::mutex> g(mu_);
+  free_[cls(n)].push_back(p);
 }
 
 // ---------------------------------------------------------------------------
@@ -106,7 +160,11 @@ Server::Server(const ServerOptions& o) : opt_(o) {
     cudaStreamDestroy(s);
     cudaGetLastError();
   }
+  cudaStreamCreateWithFlags(&spill_s_, cudaStreamNonBlocking);
   if (opt_.pinned_reserve) arena_.reserve(opt_.pinned_reserve);
+  // with a reserve, a helper thread keeps an eighth of it pinned ahead of
+  // the spills
+  if (opt_.pinned_reserve) arena_.keep_spare(device_, opt_.pinned_reserve / 8);
   thread_ = std::thread([this] { worker(); });
 }
 
@@ -117,6 +175,12 @@ Server::~Server() {
   }
   cv_work_.notify_all();
   if (thread_.joinable()) thread_.join();
+  if (spill_s_) {
+    cudaStreamSynchronize(spill_s_);
+    cudaStreamDestroy(spill_s_);
+  }
+  for (const SpillBatch& sb : spills_) events_.push_back(sb.ev);
+  spills_.clear();
   for (auto& pp : procs_) {
     Proc& p = *pp;
     cudaStreamSynchronize(p.s);
@@ -274,6 +338,7 @@ ServerStats Server::stats() {
   std::lock_guard<std::mutex> g(mu_);
   ServerStats s = st_;
   s.pinned_reserved = arena_.reserved();
+  s.pinned_sync_grows = arena_.sync_grows();
   return s;
 }
 
@@ -331,18 +396,107 @@ void Server::refresh_state_bytes(Proc& p) {
   p.scratch_dev = p.eng->restart_scratch_bytes();
 }
 
-void Server::spill_diff(Proc& p, Archived& a) {
-  uint8_t* h = arena_.alloc(a.len);
-  if (!h) return;
-  cudaMemcpyAsync(h, a.dev, a.len, cudaMemcpyDeviceToHost, p.s);
-  cudaFreeAsync(a.dev, p.s);
-  std::lock_guard<std::mutex> g(mu_);
-  a.host = h;
-  a.dev = nullptr;
-  chain_dev_ -= a.len;
-  p.chain_dev -= a.len;
-  st_.spilled_diffs++;
-  st_.spilled_bytes += a.len;
+uint64_t Server::used_bytes() const {
+  uint64_t u = chain_dev_;
+  for (const Proc* pp : view_) u += pp->state_dev + pp->scratch_dev;
+  return u;
+}
+
+void Server::reap_spills() {
+  for (size_t b = 0; b < spills_.size();) {
+    SpillBatch& sb = spills_[b];
+    if (cudaEventQuery(sb.ev) == cudaErrorNotReady) {
+      b++;
+      continue;
+    }
+    for (size_t i = 0; i < sb.items.size();) {
+      Proc& p = *view_[sb.items[i].first];
+      // a running restart of the process may read the device copy
+      if (p.busy) {
+        i++;
+        continue;
+      }
+      {
+        // under the lock: copy_diff reads the device copy while it holds it
+        std::lock_guard<std::mutex> g(mu_);
+        Archived& a = p.chain[sb.items[i].second];
+        cudaFreeAsync(a.dev, p.s);
+        a.dev = nullptr;
+        a.spilling = false;
+        chain_dev_ -= a.len;
+        p.chain_dev -= a.len;
+        p.chain_moving -= a.len;
+        spilling_bytes_ -= a.len;
+      }
+      sb.items[i] = sb.items.back();
+      sb.items.pop_back();
+    }
+    if (sb.items.empty()) {
+      put_event(sb.ev);
+      spills_.erase(spills_.begin() + (long)b);
+    } else {
+      b++;
+    }
+  }
+}
+
+uint64_t Server::spill_chains(uint64_t target, uint32_t except, uint64_t max_bytes) {
+  SpillBatch sb{nullptr, {}};
+  uint64_t issued = 0;
+  bool out_of_pinned = false;
+  while (!out_of_pinned && issued < max_bytes && used_bytes() - spilling_bytes_ > target) {
+    // the oldest resident archived checkpoints of the least recently used idle process
+    Proc* victim = nullptr;
+    uint32_t vid = 0;
+    for (uint32_t i = 0; i < view_.size(); i++) {
+      Proc& p = *view_[i];
+      if (p.busy || i == except || p.chain_dev == p.chain_moving) continue;
+      if (!victim || p.lru < victim->lru) {
+        victim = &p;
+        vid = i;
+      }
+    }
+    if (!victim) break;
+    {
+      // the spill stream copies after the archive copies on the process's stream
+      cudaEvent_t ev;
+      {
+        std::lock_guard<std::mutex> g(mu_);
+        ev = get_event();
+      }
+      cudaEventRecord(ev, victim->s);
+      cudaStreamWaitEvent(spill_s_, ev, 0);
+      put_event(ev);
+    }
+    for (uint32_t k = 0; k < victim->chain.size() && issued < max_bytes; k++) {
+      Archived& a = victim->chain[k];
+      if (!a.dev || a.spilling) continue;
+      uint8_t* h = arena_.alloc(a.len);
+      if (!h) {
+        out_of_pinned = true;
+        break;
+      }
+      cudaMemcpyAsync(h, a.dev, a.len, cudaMemcpyDeviceToHost, spill_s_);
+      std::lock_guard<std::mutex> g(mu_);
+      a.host = h;
+      a.spilling = true;
+      sb.items.emplace_back(vid, k);
+      spilling_bytes_ += a.len;
+      victim->chain_moving += a.len;
+      st_.spilled_diffs++;
+      st_.spilled_bytes += a.len;
+      issued += a.len;
+    }
+  }
+  if (!sb.items.empty()) {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      sb.ev = get_event();
+    }
+    cudaEventRecord(sb.ev, spill_s_);
+    spills_.push_back(std::move(sb));
+  }
+  return issued;
 }
 
 void Server::spill_state(Proc& p) {
@@ -376,53 +530,50 @@ int Server::restore_state(Proc& p) {
   return ST_OK;
 }
 
-bool Server::make_room(uint64_t need, uint32_t except) {
-  auto used = [&] {
-    uint64_t u = chain_dev_;
-    for (Proc* pp : view_) u += pp->state_dev + pp->scratch_dev;
-    return u;
-  };
-  // spill down to 95% of the budget, so that the next admissions find room
-  const uint64_t target = opt_.hbm_budget - opt_.hbm_budget / 20;
-  while (used() + need > target) {
-    // 0. the restart tables of the least recently used idle process (a
-    //    cache: dropping them costs only its next restart's allocation)
+uint64_t Server::drop_scratch(uint64_t target, uint32_t except) {
+  // the restart tables of the least recently used idle processes (a cache:
+  // dropping them costs only the next restart's allocation)
+  uint64_t dropped = 0;
+  while (used_bytes() > target) {
     Proc* victim = nullptr;
     for (uint32_t i = 0; i < view_.size(); i++) {
       Proc& p = *view_[i];
       if (p.busy || i == except || p.scratch_dev == 0) continue;
       if (!victim || p.lru < victim->lru) victim = &p;
     }
-    if (victim) {
-      victim->eng->release_restart_scratch();
-      victim->scratch_dev = 0;
-      continue;
-    }
-    // 1. every archived checkpoint of the least recently used idle process
-    for (uint32_t i = 0; i < view_.size(); i++) {
-      Proc& p = *view_[i];
-      if (p.busy || i == except || p.chain_dev == 0) continue;
-      if (!victim || p.lru < victim->lru) victim = &p;
-    }
-    if (victim) {
-      const uint64_t before = chain_dev_;
-      for (auto& a : victim->chain)
-        if (a.dev) spill_diff(*victim, a);
-      if (chain_dev_ == before) return used() + need <= opt_.hbm_budget;  // no pinned memory left
-      continue;
-    }
-    // 2. the digest state of the least recently used idle process
+    if (!victim) break;
+    dropped += victim->scratch_dev;
+    victim->eng->release_restart_scratch();
+    victim->scratch_dev = 0;
+  }
+  return dropped;
+}
+
+bool Server::make_room(uint64_t need, uint32_t except) {
+  // free down to 95% of the budget, so that the next admissions find room
+  const uint64_t target = opt_.hbm_budget - opt_.hbm_budget / 20;
+  // 0. restart tables
+  drop_scratch(need >= target ? 0 : target - need, except);
+  if (used_bytes() + need <= target) return true;
+  // 1. archived checkpoints, copied to pinned memory on their processes'
+  //    streams; the request is admitted once enough of the copies have landed
+  spill_chains(need >= target ? 0 : target - need, except, std::numeric_limits<uint64_t>::max());
+  if (used_bytes() + need <= opt_.hbm_budget) return true;
+  if (used_bytes() - spilling_bytes_ + need <= opt_.hbm_budget) return false;
+  // 2. the digest state of the least recently used idle process
+  while (used_bytes() - spilling_bytes_ + need > target) {
+    Proc* victim = nullptr;
     for (uint32_t i = 0; i < view_.size(); i++) {
       Proc& p = *view_[i];
       if (p.busy || i == except || p.state_dev == 0 || p.eng->mode() == MODE_FULL) continue;
       if (!victim || p.lru < victim->lru) victim = &p;
     }
-    if (!victim) return used() + need <= opt_.hbm_budget;
+    if (!victim) break;
     const uint64_t before = victim->state_dev;
     spill_state(*victim);
-    if (victim->state_dev == before) return used() + need <= opt_.hbm_budget;
+    if (victim->state_dev == before) break;  // no pinned memory left
   }
-  return true;
+  return used_bytes() + need <= opt_.hbm_budget;
 }
 
 // ---- request execution -------------------------------------------------------
@@ -521,14 +672,12 @@ int Server::start_restart(Req& r, Proc& p, std::vector<uint8_t*>* temps) {
 bool Server::try_start(Req& r) {
   Proc& p = *view_[r.pid];
   const uint64_t need = need_bytes(r, p);
-  uint64_t used = chain_dev_;
-  for (Proc* pp : view_) used += pp->state_dev + pp->scratch_dev;
   const double t_room = now_ms();
-  const bool over = used + need > opt_.hbm_budget;
+  const bool over = used_bytes() + need > opt_.hbm_budget;
   const bool room = !over || make_room(need, r.pid);
   if (over) st_.worker_ms[2] += now_ms() - t_room;
   if (!room) {
-    if (flights_.empty()) {
+    if (flights_.empty() && spills_.empty()) {
       // nothing in flight will free memory: the request cannot fit
       Completion c{r.ticket, r.pid, r.kind, ST_ENOMEM, 0, 0, r.t_submit, now_ms(), now_ms()};
       put_event(r.ready);
@@ -555,8 +704,7 @@ bool Server::try_start(Req& r) {
   std::lock_guard<std::mutex> g(mu_);
   st_.worker_ms[0] += now_ms() - t_start;
   st_.inflight_peak = std::max<uint32_t>(st_.inflight_peak, (uint32_t)flights_.size());
-  uint64_t u = chain_dev_;
-  for (Proc* pp : view_) u += pp->state_dev + pp->scratch_dev;
+  const uint64_t u = used_bytes();
   st_.hbm_used = u;
   st_.hbm_peak = std::max(st_.hbm_peak, u);
   return true;
@@ -607,10 +755,8 @@ void Server::finish(Flight& f) {
       // its allocations and its graph capture then cost the next request
       // nothing (a new input pointer or baseline still re-prepares)
       // (not under memory pressure: the process may be spilled before then)
-      uint64_t used = chain_dev_;
-      for (Proc* pp : view_) used += pp->state_dev + pp->scratch_dev;
       if (c.status == ST_OK && opt_.use_graph && e.mode() != MODE_FULL &&
-          used < opt_.hbm_budget - opt_.hbm_budget / 10 &&
+          used_bytes() < opt_.hbm_budget - opt_.hbm_budget / 10 &&
           e.prepare(f.r.data, f.r.len, false, opt_.id_headroom) == ST_OK)
         ensure_graph(p, f.r.data, f.r.len);
     } else {
@@ -657,6 +803,12 @@ void Server::worker() {
       }
     }
     bool progress = false;
+    // 0. archived checkpoints whose copy to pinned memory has landed
+    if (!spills_.empty()) {
+      const size_t before = spills_.size();
+      reap_spills();
+      progress = spills_.size() != before;
+    }
     // 1. completions
     for (size_t i = 0; i < flights_.size();) {
       cudaError_t q = cudaEventQuery(flights_[i].done);
@@ -675,7 +827,19 @@ void Server::worker() {
       st_.worker_ms[1] += now_ms() - t_fin;
       progress = true;
     }
-    // 2. admission in submission order; one request per process at a time
+    // 2. past 90% of the budget, make room ahead of need until 87.5% stays
+    //    resident: first the restart tables that idle processes keep, then
+    //    the oldest archived checkpoints of the least recently used
+    //    processes, a bounded amount per pass, between admissions, so that
+    //    neither a request nor the worker waits for the copies
+    if (used_bytes() - spilling_bytes_ > opt_.hbm_budget - opt_.hbm_budget / 10) {
+      const double t_room = now_ms();
+      const uint64_t low = opt_.hbm_budget - opt_.hbm_budget / 8;
+      drop_scratch(low + spilling_bytes_, UINT32_MAX);
+      spill_chains(low, UINT32_MAX, kSpillStepBytes);
+      st_.worker_ms[2] += now_ms() - t_room;
+    }
+    // 3. admission in submission order; one request per process at a time
     std::set<uint32_t> seen;
     for (auto it = pending_.begin(); it != pending_.end() && flights_.size() < opt_.max_inflight;) {
       const uint32_t pid = it->pid;
@@ -696,7 +860,8 @@ void Server::worker() {
       const double t_wait = now_ms();
       std::unique_lock<std::mutex> g(mu_);
       if (inbox_.empty() && !stop_)
-        cv_work_.wait_for(g, flights_.empty() ? std::chrono::microseconds(2000) : std::chrono::microseconds(20));
+        cv_work_.wait_for(g, flights_.empty() && spills_.empty() ? std::chrono::microseconds(2000)
+                                                                 : std::chrono::microseconds(20));
       st_.worker_ms[3] += now_ms() - t_wait;
     }
   }

@@ -44,7 +44,9 @@ struct ServerOptions {
   int use_graph = 0;
   // Allocate the HBM budget from the server's pool once at creation (and
   // keep it there), and pin this much host memory for spills up front:
-  // growing either later costs milliseconds per allocation.
+  // growing either later costs milliseconds per allocation.  With a pinned
+  // reserve, a helper thread also keeps an eighth of it unused and pinned
+  // ahead of the spills.
   int reserve_hbm = 0;
   uint64_t pinned_reserve = 0;
 };
@@ -68,35 +70,51 @@ struct ServerStats {
   uint64_t spilled_bytes = 0;
   uint64_t graph_captures = 0, graph_replays = 0;
   uint64_t hbm_used = 0, hbm_peak = 0, pinned_reserved = 0;
+  uint64_t pinned_sync_grows = 0;  // slabs the worker had to pin itself
   uint64_t deferred_admissions = 0;  // admission attempts refused for memory
   uint32_t inflight_peak = 0;
   double worker_ms[4] = {0, 0, 0, 0};  // host time of the worker: starting requests,
                                        // finishing them, making room, waiting
 };
 
-// Pinned host memory in power-of-two blocks, reused, freed at destruction
-// (cudaFreeHost would wait for the whole device).  Blocks are carved from
-// slabs of at least 256 MiB, so that cudaHostAlloc -- slow -- runs rarely;
-// reserve() pins slabs ahead of use.
+// Pinned host memory for spills, in blocks of quarter-power-of-two classes
+// (64 KiB, then p, 1.25p, 1.5p, 1.75p for each power of two p: at most a
+// quarter of a block is unused), reused, freed at destruction (cudaFreeHost
+// would wait for the whole device).  Blocks are carved from slabs of at least
+// 256 MiB.  Pinning a slab takes tens of milliseconds, so with keep_spare() a
+// helper thread pins the next slabs while the unused slab space is below the
+// given size, and the thread that allocates pins only when the helper has
+// fallen behind.  All members are thread-safe.
 class PinnedArena {
  public:
   ~PinnedArena();
   uint8_t* alloc(uint64_t n);
   void free(uint8_t* p, uint64_t n);
   bool reserve(uint64_t bytes);
-  uint64_t reserved() const { return reserved_; }
+  void keep_spare(int device, uint64_t bytes);
+  uint64_t reserved();
+  uint64_t sync_grows();
+  static uint64_t cls(uint64_t n);
 
  private:
   struct Slab {
     uint8_t* next;
     uint64_t left;
   };
-  static uint64_t cls(uint64_t n);
   bool add_slab(uint64_t bytes);
+  uint8_t* carve(uint64_t c);  // caller holds mu_
+  void helper(int device);
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::thread helper_;
+  bool stop_ = false;
+  uint64_t spare_target_ = 0;
+  uint64_t spare_ = 0;  // unused slab bytes
   std::map<uint64_t, std::vector<uint8_t*>> free_;
   std::vector<uint8_t*> all_;
   std::vector<Slab> slabs_;
   uint64_t reserved_ = 0;
+  uint64_t sync_grows_ = 0;
 };
 
 class Server {
@@ -119,9 +137,19 @@ class Server {
  private:
   struct Archived {
     uint8_t* dev = nullptr;   // pool allocation, or null when spilled
-    uint8_t* host = nullptr;  // pinned copy when spilled
+    uint8_t* host = nullptr;  // pinned copy when spilled (or being spilled)
     uint64_t len = 0;
     HeaderHost hdr{};
+    bool spilling = false;    // host copy in flight; dev stays valid until it lands
+  };
+  // Diffs whose copy to pinned memory is in flight on the spill stream,
+  // and the event recorded after their copies.  Their device blocks are
+  // freed only once the copies have run: freed earlier, the pool could hand
+  // a block to another process's request, which would then wait behind the
+  // whole copy.
+  struct SpillBatch {
+    cudaEvent_t ev;
+    std::vector<std::pair<uint32_t, uint32_t>> items;  // (process, chain index)
   };
   struct Proc {
     std::unique_ptr<Engine> eng;
@@ -136,6 +164,7 @@ class Server {
     cudaGraphExec_t exec = nullptr;
     uint64_t sig = 0;
     uint64_t chain_dev = 0;        // device bytes of archived checkpoints
+    uint64_t chain_moving = 0;     // of which the host copy is in flight
     uint64_t last_diff = 0;        // size of the latest incremental checkpoint
   };
   struct Req {
@@ -166,7 +195,10 @@ class Server {
   void finish(Flight& f);
   uint64_t need_bytes(const Req& r, const Proc& p) const;
   bool make_room(uint64_t need, uint32_t except);
-  void spill_diff(Proc& p, Archived& a);
+  uint64_t used_bytes() const;
+  uint64_t drop_scratch(uint64_t target, uint32_t except);
+  uint64_t spill_chains(uint64_t target, uint32_t except, uint64_t max_bytes);
+  void reap_spills();
   void spill_state(Proc& p);
   int restore_state(Proc& p);
   void refresh_state_bytes(Proc& p);
@@ -183,6 +215,9 @@ class Server {
   std::vector<Proc*> view_;                   // the worker's copy of procs_
   std::deque<Req> inbox_, pending_;
   std::vector<Flight> flights_;
+  std::vector<SpillBatch> spills_;  // worker thread only
+  cudaStream_t spill_s_ = nullptr;  // copies of spilled diffs to pinned memory
+  uint64_t spilling_bytes_ = 0;    // device bytes whose host copy is in flight
   std::deque<Completion> done_;
   std::vector<cudaEvent_t> events_;
   std::mutex mu_;                  // inbox, completions, events, procs vector, chains
