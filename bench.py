@@ -270,13 +270,15 @@ def restart_bench(torch, mc, dev, a, kind, approach=None):
                     "host_chain_value: chain in pageable host memory, copied to HBM inside the call"}
 
 
-def series_bench(torch, mc, dev, states, cs, kind, W, flush=None):
+def series_bench(torch, mc, dev, states, cs, kind, W, flush=None, untimed=False):
     """Incremental checkpoints of resident device states through one handle:
     states[0] is the baseline, the next W are warm-up, the rest are timed.
     With `flush`, each step is timed alone after a write of `flush` (larger
     than L2); without it, the whole loop between two events.  Returns the
     device seconds per step and the per-step counters."""
     d = mc.TreeDeduplicator(cs, kind)
+    if untimed:
+        d.set_tuning(untimed=1)
     d.checkpoint_device(states[0], True)
     for s in states[1:1 + W]:
         d.checkpoint_device(s, False)
@@ -346,21 +348,26 @@ def link_section(torch, dev, nbytes=GIB, reps=3):
 def small_series_section(torch, mc, dev, peak):
     """The 64 MiB / 128 B series (tree, Murmur3, 10 checkpoints: a baseline and
     9 incremental ones, each timed alone after a 256 MiB write that flushes
-    L2), run once untimed and once timed on the same states."""
+    L2): once as a warm-up, once with the phase events (for the leaf time),
+    once replayed as one graph without them (the value)."""
     nbytes, cs = 64 << 20, 128
     N = nbytes // cs
     states = make_states(torch, nbytes, cs, 10, seed=64, device=dev, pattern="64mib")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     series_bench(torch, mc, dev, states, cs, mc.MURMUR3, 0, flush)
-    t, leaf, sd, sm = series_bench(torch, mc, dev, states, cs, mc.MURMUR3, 0, flush)
+    t_timed, leaf, sd, sm = series_bench(torch, mc, dev, states, cs, mc.MURMUR3, 0, flush)
+    t, _, _, _ = series_bench(torch, mc, dev, states, cs, mc.MURMUR3, 0, flush, untimed=True)
     b = nbytes + 32 * N + 2 * sd + sm
     del states, flush
     return {"workload": "tree dedup, Murmur3, 64 MiB buffer, 128 B chunks, 10 checkpoints of the 64 MiB update "
                         "pattern (9 incremental timed, L2 flushed before each)",
             "value": round(nbytes / t / 1e9, 3), "unit": "GB/s", "ms": round(t * 1e3, 4),
+            "ms_with_phase_events": round(t_timed * 1e3, 4),
             "leaf_ms": round(leaf * 1e3, 4),
             "roofline_frac": round(b / t / 1e9 / peak, 4),
-            "note": "roofline_frac: B_dedup = D + 32 N + 2 S_data + S_meta per device-timed checkpoint over the "
+            "note": "value and ms: replayed as one graph (mtc_tune_t.untimed); ms_with_phase_events: the default "
+                    "five graph launches with events between the phases, which the leaf time comes from; "
+                    "roofline_frac: B_dedup = D + 32 N + 2 S_data + S_meta per device-timed checkpoint over the "
                     "measured HBM copy bandwidth"}
 
 
@@ -644,12 +651,23 @@ def serve_bench(torch, mc, dev, a):
         pending_checks.append((p, 1, _digest2(mc, kind, outs[0][:nb])))
     rst_ok, rst_checked = True, 0
 
-    def stream(arr, is_rst, who, trace=None):
+    def stream(arr, is_rst, who, trace=None, stalls=None):
         """Requests arriving at offsets `arr` (ms); returns the latencies,
         (arrival offset, latency) pairs, bytes served and the wall time from
         the first arrival to the last completion.  `trace`, a list, receives
         one row per request: arrival, submission, admission and completion
-        (ms from the start), kind, process, buffer bytes."""
+        (ms from the start), kind, process, buffer bytes; `stalls`, a dict,
+        the longest single call of each kind the client made (ms, at ms)."""
+        def timed_call(name, f, *args):
+            if stalls is None:
+                return f(*args)
+            t = mc.now_ms()
+            r = f(*args)
+            dt = mc.now_ms() - t
+            if dt > stalls.get(name, (0.0, 0.0))[0]:
+                stalls[name] = (round(dt, 3), round(t - t0, 1))
+            return r
+
         n_req = len(arr)
         queues = [deque() for _ in range(P)]
         busy = [None] * P
@@ -677,17 +695,22 @@ def serve_bench(torch, mc, dev, a):
                     slot = free_outs.pop()
                     target = int(rng.integers(0, step[p]))
                     n = mix[p]["nbytes"]
-                    srv.submit_restart(pids[p], target, outs[slot][:n])
+                    timed_call("submit_restart", srv.submit_restart, pids[p], target, outs[slot][:n])
                     busy[p] = ("restart", arrival, target, slot)
                 else:
-                    plans[p].apply(bufs[p], step[p])
-                    srv.submit_checkpoint(pids[p], bufs[p])
+                    timed_call("apply_update", plans[p].apply, bufs[p], step[p])
+                    timed_call("submit_checkpoint", srv.submit_checkpoint, pids[p], bufs[p])
                     busy[p] = ("checkpoint", arrival, step[p], None)
                     step[p] += 1
                 queues[p].popleft()
                 ready.discard(p)
                 outstanding += 1
+            t_poll = mc.now_ms()
             done = srv.poll(0.0 if (ready or (i < n_req and t0 + arr[i] <= mc.now_ms() + 0.05)) else 0.2)
+            if stalls is not None and done:
+                dt = mc.now_ms() - t_poll
+                if dt > stalls.get("poll", (0.0, 0.0))[0]:
+                    stalls["poll"] = (round(dt, 3), round(t_poll - t0, 1))
             for c in done:
                 p = c["pid"]  # this server's process ids are 0..P-1 in order
                 what, arrival, target, slot = busy[p]
@@ -701,7 +724,8 @@ def serve_bench(torch, mc, dev, a):
                 nbytes_done += mix[p]["nbytes"]
                 t_last = max(t_last, c["t_done_ms"])
                 if what == "restart":
-                    pending_checks.append((p, target, _digest2(mc, kind, outs[slot][:mix[p]["nbytes"]])))
+                    pending_checks.append((p, target, timed_call("verify_digest", _digest2, mc, kind,
+                                                                 outs[slot][:mix[p]["nbytes"]])))
                     free_outs.append(slot)
                 busy[p] = None
                 outstanding -= 1
@@ -713,7 +737,9 @@ def serve_bench(torch, mc, dev, a):
     n_req = int(a.serve_rate * a.serve_seconds)
     arr = np.cumsum(rng.exponential(1.0 / a.serve_rate, n_req)) * 1e3
     trace = [] if a.serve_trace else None
-    lat, lat_t, nbytes_done, wall = stream(arr, rng.random(n_req) < 0.05, rng.integers(0, P, n_req), trace)
+    client_max = {}
+    lat, lat_t, nbytes_done, wall = stream(arr, rng.random(n_req) < 0.05, rng.integers(0, P, n_req), trace,
+                                           client_max)
     st_stream = srv.stats()
     if trace is not None:
         with open(a.serve_trace, "w") as f:
@@ -840,10 +866,14 @@ def serve_bench(torch, mc, dev, a):
         "server": {k: st[k] for k in ("inflight_peak", "graph_captures", "graph_replays", "spilled_diffs",
                                       "spilled_bytes", "spilled_states", "restored_states", "staged_diffs",
                                       "hbm_peak", "pinned_reserved", "pinned_sync_grows", "deferred_admissions",
-                                      "failed", "worker_ms")},
+                                      "failed", "worker_ms", "worker_max_ms", "pool_reserved_high",
+                                      "pool_used_high")},
+        "torch_allocator": {k: torch.cuda.memory_stats().get(k) for k in ("num_alloc_retries", "num_device_alloc",
+                                                                         "num_device_free")},
+        "client_max_ms": {k: {"ms": v[0], "at_ms": v[1]} for k, v in sorted(client_max.items())},
         "server_after_stream": {k: st_stream[k] for k in ("spilled_diffs", "spilled_bytes", "spilled_states",
                                                           "restored_states", "staged_diffs", "hbm_peak",
-                                                          "deferred_admissions")},
+                                                          "deferred_admissions", "worker_max_ms")},
         "note": "value: bytes of all completed requests (checkpointed and restarted buffers) / time from the first "
                 "arrival to the last completion; latency: arrival to completion (diff archived in HBM, or "
                 "restarted buffer written)",

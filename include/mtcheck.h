@@ -278,10 +278,13 @@ typedef struct mtc_server_stats {
   uint64_t spilled_diffs, spilled_states, restored_states, staged_diffs, spilled_bytes;
   uint64_t graph_captures, graph_replays;
   uint64_t hbm_used, hbm_peak, pinned_reserved, deferred_admissions;
+  uint64_t pool_reserved_high, pool_used_high; /* device bytes the server's pool mapped and
+                                                  handed out, highest so far */
   uint32_t inflight_peak;
   uint32_t pinned_sync_grows; /* pinned slabs the worker thread had to pin itself */
   double worker_ms[4];     /* worker host time: starting requests, finishing them,
                               making room (spills), waiting for work */
+  double worker_max_ms[3]; /* longest single start, finish and room-making pass */
 } mtc_server_stats_t;
 int mtc_server_create(const mtc_server_options_t* opt, mtc_server_t** out);
 /* waits for every submitted request, then frees everything */
@@ -319,7 +322,9 @@ typedef struct mtc_tune {
   int32_t threads_per_chunk; /* 1 (0 taken as 1): one thread per chunk; 32: one warp
                                 per chunk (chunks of at most 4096 bytes; the warp loads
                                 the chunk, one lane hashes it: the digests are serial) */
-  int32_t reserved;
+  int32_t untimed;      /* 1: replay an incremental checkpoint as one graph, without the
+                           events between its phases (one graph launch instead of five);
+                           the phase times and the log timers then read 0 */
 } mtc_tune_t;
 int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t);
 int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* out);

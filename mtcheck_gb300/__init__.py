@@ -60,11 +60,12 @@ class BatchInfo(ctypes.Structure):
 class Tune(ctypes.Structure):
     _fields_ = [("rows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("direct", ctypes.c_int32),
                 ("eager", ctypes.c_int32), ("max_load", ctypes.c_double), ("threads_per_chunk", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("untimed", ctypes.c_int32)]
 
     def as_dict(self):
         return {"rows": self.rows, "ctas_per_sm": self.ctas_per_sm, "direct": self.direct,
-                "eager": self.eager, "max_load": self.max_load, "threads_per_chunk": self.threads_per_chunk}
+                "eager": self.eager, "max_load": self.max_load, "threads_per_chunk": self.threads_per_chunk,
+                "untimed": self.untimed}
 
 
 class ServerOptions(ctypes.Structure):
@@ -82,13 +83,15 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "submitted", "completed", "failed", "checkpoints", "restarts", "bytes_checkpointed", "bytes_restarted",
         "spilled_diffs", "spilled_states", "restored_states", "staged_diffs", "spilled_bytes", "graph_captures",
-        "graph_replays", "hbm_used", "hbm_peak", "pinned_reserved", "deferred_admissions")] + \
+        "graph_replays", "hbm_used", "hbm_peak", "pinned_reserved", "deferred_admissions", "pool_reserved_high",
+        "pool_used_high")] + \
         [("inflight_peak", ctypes.c_uint32), ("pinned_sync_grows", ctypes.c_uint32),
-         ("worker_ms", ctypes.c_double * 4)]
+         ("worker_ms", ctypes.c_double * 4), ("worker_max_ms", ctypes.c_double * 3)]
 
     def as_dict(self):
-        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "worker_ms"}
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n not in ("worker_ms", "worker_max_ms")}
         d["worker_ms"] = {k: round(self.worker_ms[j], 2) for j, k in enumerate(("start", "finish", "room", "wait"))}
+        d["worker_max_ms"] = {k: round(self.worker_max_ms[j], 2) for j, k in enumerate(("start", "finish", "room"))}
         return d
 
 
@@ -319,12 +322,12 @@ class Deduplicator:
 
     # -- tuning ------------------------------------------------------------
     def set_tuning(self, rows=None, ctas_per_sm=None, direct=None, max_load=None, eager=None,
-                   threads_per_chunk=None):
+                   threads_per_chunk=None, untimed=None):
         """Set the given fields of the launch tuning; the others keep their values."""
         cur = self.tuning()
         pick = lambda v, k: cur[k] if v is None else v
         t = Tune(pick(rows, "rows"), pick(ctas_per_sm, "ctas_per_sm"), pick(direct, "direct"), pick(eager, "eager"),
-                 pick(max_load, "max_load"), pick(threads_per_chunk, "threads_per_chunk"), 0)
+                 pick(max_load, "max_load"), pick(threads_per_chunk, "threads_per_chunk"), pick(untimed, "untimed"))
         _check(load().mtc_set_tuning(self.h, ctypes.byref(t)))
 
     def tuning(self):

@@ -558,7 +558,10 @@ int mtc_server_get_stats(mtc_server_t* s, mtc_server_stats_t* o) {
   o->hbm_used = t.hbm_used; o->hbm_peak = t.hbm_peak; o->pinned_reserved = t.pinned_reserved;
   o->deferred_admissions = t.deferred_admissions; o->inflight_peak = t.inflight_peak;
   o->pinned_sync_grows = (uint32_t)t.pinned_sync_grows;
+  o->pool_reserved_high = t.pool_reserved_high;
+  o->pool_used_high = t.pool_used_high;
   for (int k = 0; k < 4; k++) o->worker_ms[k] = t.worker_ms[k];
+  for (int k = 0; k < 3; k++) o->worker_max_ms[k] = t.worker_max_ms[k];
   return MTC_OK;
 }
 
@@ -576,6 +579,7 @@ int mtc_set_tuning(mtc_dedup_t* h, const mtc_tune_t* t) {
                                       t->threads_per_chunk == 32 ? 32 : 1});
   h->eng->set_max_load(t->max_load);
   h->eng->set_own_graph(t->eager == 0);
+  h->eng->set_untimed(t->untimed != 0);
   return MTC_OK;
 }
 
@@ -588,6 +592,7 @@ int mtc_get_tuning(const mtc_dedup_t* h, mtc_tune_t* o) {
   o->direct = t.direct;
   o->threads_per_chunk = t.threads_per_chunk;
   o->eager = h->eng->own_graph() ? 0 : 1;
+  o->untimed = h->eng->untimed() ? 1 : 0;
   o->max_load = h->eng->max_load();
   return MTC_OK;
 }

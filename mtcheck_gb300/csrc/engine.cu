@@ -76,7 +76,12 @@ Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_); else cudaDeviceSynchronize();
   drop_own_graph();
   if (cap_stream_) cudaStreamDestroy(cap_stream_);
+  if (rside_) {
+    cudaStreamSynchronize(rside_);
+    cudaStreamDestroy(rside_);
+  }
   for (auto& e : ev_) if (e) cudaEventDestroy(e);
+  for (auto& e : rev_) if (e) cudaEventDestroy(e);
   if (lay_host_) cudaFreeHost(lay_host_);
   if (err_host_) cudaFreeHost(err_host_);
   if (sp_host_) cudaFreeHost(sp_host_);
@@ -489,6 +494,11 @@ int Engine::update_own_params() {
   return ST_OK;
 }
 
+void Engine::set_untimed(bool on) {
+  if (on != untimed_) drop_own_graph();
+  untimed_ = on;
+}
+
 void Engine::set_own_graph(bool on) {
   own_graph_ = on;
   if (!on) drop_own_graph();
@@ -503,6 +513,7 @@ int Engine::mark(int i) {
     MTC_CUDA(cudaEventRecord(ev_[i], stream_));
     return ST_OK;
   }
+  if (untimed_) return ST_OK;  // one graph, no phase events
   cudaGraph_t g = nullptr;
   MTC_CUDA(cudaStreamEndCapture(cap_stream_, &g));
   seg_graphs_.emplace_back(seg_mark_, g);
@@ -597,6 +608,7 @@ int Engine::replay_own(const uint8_t* data, uint64_t len) {
     if (sg.mark >= 0) MTC_CUDA(cudaEventRecord(ev_[sg.mark], stream_));
     if (sg.exec) MTC_CUDA(cudaGraphLaunch(sg.exec, stream_));
   }
+  timed_ = !untimed_;
   return ST_OK;
 }
 
@@ -636,6 +648,9 @@ int Engine::complete(uint64_t len, HeaderHost* header) {
     ms[1] = event_ms(ev_[1], ev_[2]);
     ms[2] = event_ms(ev_[2], ev_[3]);
     timers[0] = ms[0] * 1e-3; timers[1] = ms[1] * 1e-3; timers[2] = ms[2] * 1e-3;
+  } else {
+    timers[0] = timers[1] = timers[2] = 0;
+    phase_times[0] = phase_times[1] = phase_times[2] = 0;
   }
   if (mode_ == MODE_FULL) {
     diff_len_ = len;

@@ -116,6 +116,10 @@ class Engine {
   // signature changes (on by default; a Batch never uses it).
   void set_own_graph(bool on);
   bool own_graph() const { return own_graph_; }
+  // Replay an incremental checkpoint as one graph without the phase events
+  // between its segments; its timers and phase times then read 0.
+  void set_untimed(bool on);
+  bool untimed() const { return untimed_; }
   // Batch members read their step values from the pinned block at run time.
   void set_params_from_host(bool on) { params_by_value_ = !on; }
   bool take_stream_work() {
@@ -227,6 +231,7 @@ class Engine {
   LeafTune leaf_tune_{};
   uint32_t N_ = 0, M_ = 0;
   bool own_graph_ = true;
+  bool untimed_ = false;
   // the captured sequence, cut at the timing marks: the event recorded
   // before each segment (or -1) and the segment's graph (null when empty)
   struct OwnSeg {
@@ -287,6 +292,11 @@ class Engine {
   TmaCache tma_;
   cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   RestartScratch* rs_ = nullptr;  // restart buffers, created on first use
+  // restart: a second stream for the work that does not depend on the main
+  // sequence (clears, the chain tables beside the main scatter, the copy of
+  // resolved chunk ranges), and the events that fork and join it
+  cudaStream_t rside_ = nullptr;
+  cudaEvent_t rev_[12] = {};
   DevBuf<uint8_t> hdr_dev_;         // read_headers: gathered headers
   uint8_t* hdr_host_ = nullptr;     // pinned copy of them
   size_t hdr_host_cap_ = 0;

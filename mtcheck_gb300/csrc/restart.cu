@@ -20,6 +20,7 @@
 //   5. one copy pass moves each chunk once from the diff that owns it.
 // A chunk that the reference never writes is not written here either.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "engine.hpp"
@@ -73,6 +74,7 @@ struct RArgs {
   uint64_t *tot;                // [0] dm items, [2] main FO chunks, [3] main shift chunks, [4] [3] + rm items
   uint8_t* out;
   uint32_t* err;
+  uint32_t c_lo, c_hi;           // resolve / copy: chunks [c_lo, c_hi), c_lo a multiple of 32
 };
 
 __device__ __forceinline__ uint32_t rd32(const uint8_t* p) {
@@ -995,7 +997,7 @@ __global__ void __launch_bounds__(256, 6) resolve_kernel(RArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint2* bm = reinterpret_cast<const uint2*>(a.sbm);
-  for (uint64_t cw = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); cw < a.N; cw += stride) {
+  for (uint64_t cw = a.c_lo + (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); cw < a.c_hi; cw += stride) {
     const uint64_t c = cw + lane;
     OwnMasks own;
     own.key = (uint32_t)c;  // chunk c's own key (tree: leaf N-1+c, list: chunk c)
@@ -1005,7 +1007,7 @@ __global__ void __launch_bounds__(256, 6) resolve_kernel(RArgs a) {
       const uint2 v = st < a.nsteps ? bm[(cw >> 5) * a.W * 32 + st] : make_uint2(0, 0);
       own.m = make_uint2(warp_transpose32(v.x), warp_transpose32(v.y));
     }
-    if (c < a.N) {
+    if (c < a.c_hi) {
       const uint8_t* src;
       uint32_t nb;
       chunk_source(a, own, c, src, nb);
@@ -1019,12 +1021,13 @@ __global__ void __launch_bounds__(256, 6) resolve_kernel(RArgs a) {
 __global__ void __launch_bounds__(256, 3) restore_copy_kernel(RArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-  const uint64_t tiles = ((uint64_t)a.N + 31) / 32;
-  for (uint64_t wt = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wt < tiles; wt += warps) {
+  const uint64_t t_hi = ((uint64_t)a.c_hi + 31) / 32;
+  for (uint64_t wt = a.c_lo / 32 + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wt < t_hi;
+       wt += warps) {
     const uint64_t c = wt * 32 + lane;
     const uint8_t* src = nullptr;
     uint32_t nb = 0;
-    if (c < a.N) {
+    if (c < a.c_hi) {
       src = reinterpret_cast<const uint8_t*>(a.srcp[c]);
       nb = a.nbv[c];
     }
@@ -1041,6 +1044,17 @@ inline uint32_t gsz(uint64_t n, int threads = 256, int per_sm = 8) {
 }
 
 }  // namespace
+
+// Chunk ranges the resolve and copy passes are pipelined over
+// (MTCHECK_RESTART_PARTS, 1-7; default 4, one below 2^16 chunks).
+static uint32_t restart_parts(uint32_t N) {
+  static int v = [] {
+    const char* e = std::getenv("MTCHECK_RESTART_PARTS");
+    const int x = e ? std::atoi(e) : 4;
+    return x < 1 ? 1 : x > 7 ? 7 : x;
+  }();
+  return N < (1u << 16) ? 1 : (uint32_t)v;
+}
 
 // Restart scratch owned by the engine between calls.
 struct RestartScratch {
@@ -1297,6 +1311,20 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   a.out = dev_out; a.err = err_.p;
   const bool tree = approach == APPROACH_TREE;
 
+  // The second stream: clears that depend on nothing run there at once; the
+  // chain tables run there beside the main checkpoint's scatter; each range
+  // of resolved chunks is copied there while the next range is resolved.
+  if (!rside_) {
+    MTC_CUDA_R(cudaStreamCreateWithFlags(&rside_, cudaStreamNonBlocking));
+    for (auto& e : rev_) MTC_CUDA_R(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  cudaStream_t side = rside_;
+  MTC_CUDA_R(cudaEventRecord(rev_[0], s));  // after the allocations and the previous restart
+  MTC_CUDA_R(cudaStreamWaitEvent(side, rev_[0], 0));
+  MTC_CUDA_R(cudaMemsetAsync(R.fo_at.p, 0xff, sizeof(uint32_t) * ((size_t)M + 2), side));
+  if (nsteps) MTC_CUDA_R(cudaMemsetAsync(R.sbm.p, 0, sizeof(uint32_t) * (size_t)KW * W * 32 * 2, side));
+  MTC_CUDA_R(cudaEventRecord(rev_[1], side));
+
   // 1-3: decode entries, repeat tables, source checkpoints
   MTC_CUDA_R(cudaMemsetAsync(R.tot.p, 0, sizeof(uint64_t) * 5, s));
   if (nfo + nsh) { load_entries_kernel<<<gsz((uint64_t)nfo + nsh), 256, 0, s>>>(a); note_launch(); }
@@ -1333,8 +1361,16 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     clen_kernel<<<gsz(nfo), 256, 0, s>>>(a);
     note_launch();
   }
-  // main checkpoint
-  MTC_CUDA_R(cudaMemsetAsync(R.fo_at.p, 0xff, sizeof(uint32_t) * ((size_t)M + 2), s));
+  // chain tables on the second stream, after the clears and the entries
+  MTC_CUDA_R(cudaEventRecord(rev_[2], s));
+  if (nsteps) {
+    MTC_CUDA_R(cudaStreamWaitEvent(side, rev_[2], 0));
+    chain_tables_kernel<<<num_sms() * 8, 256, 0, side>>>(a);
+    note_launch();
+  }
+  MTC_CUDA_R(cudaEventRecord(rev_[3], side));
+  // main checkpoint, beside them
+  MTC_CUDA_R(cudaStreamWaitEvent(s, rev_[1], 0));
   if (di[0].F) { fo_at_kernel<<<gsz(di[0].F), 256, 0, s>>>(a); note_launch(); }
   if (di[0].S) {
     main_shift_kernel<<<gsz(di[0].S), 256, 0, s>>>(a);
@@ -1344,16 +1380,31 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     main_cover_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
     note_launch();
   }
-  // chain
-  if (nsteps) {
-    MTC_CUDA_R(cudaMemsetAsync(R.sbm.p, 0, sizeof(uint32_t) * (size_t)KW * W * 32 * 2, s));
-    chain_tables_kernel<<<num_sms() * 8, 256, 0, s>>>(a);
-    note_launch();
+  MTC_CUDA_R(cudaStreamWaitEvent(s, rev_[3], 0));
+  // 4: every chunk's source, 5: the copy; range by range, each range copied
+  // on the second stream while the next is resolved
+  const uint32_t parts = restart_parts(N);
+  const uint64_t per = ((uint64_t)N + parts - 1) / parts;
+  const uint64_t step = (per + 31) / 32 * 32;
+  uint32_t launched = 0;
+  for (uint64_t lo = 0; lo < N; lo += step, launched++) {
+    RArgs r = a;
+    r.c_lo = (uint32_t)lo;
+    r.c_hi = (uint32_t)std::min<uint64_t>(N, lo + step);
+    resolve_kernel<<<gsz(r.c_hi - r.c_lo), 256, 0, s>>>(r);
+    if (parts == 1) {
+      restore_copy_kernel<<<num_sms() * 3, 256, 0, s>>>(r);
+    } else {
+      MTC_CUDA_R(cudaEventRecord(rev_[4 + launched], s));
+      MTC_CUDA_R(cudaStreamWaitEvent(side, rev_[4 + launched], 0));
+      restore_copy_kernel<<<num_sms() * 3, 256, 0, side>>>(r);
+    }
+    note_launch(2);
   }
-  // 4: every chunk's source; 5: the copy
-  resolve_kernel<<<gsz(N), 256, 0, s>>>(a);
-  restore_copy_kernel<<<num_sms() * 3, 256, 0, s>>>(a);
-  note_launch(2);
+  if (parts > 1) {
+    MTC_CUDA_R(cudaEventRecord(rev_[11], side));
+    MTC_CUDA_R(cudaStreamWaitEvent(s, rev_[11], 0));
+  }
   cudaEventRecord(e1, s);
   Readback rb{};
   rb.src[0] = err_.p;

@@ -5,6 +5,9 @@
 #include <limits>
 #include <set>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "server.hpp"
 
 namespace mtc {
@@ -22,7 +25,10 @@ PinnedArena::~PinnedArena() {
   }
   cv_.notify_all();
   if (helper_.joinable()) helper_.join();
-  for (uint8_t* p : all_) cudaFreeHost(p);
+  for (const auto& m : all_) {
+    cudaHostUnregister(m.first);
+    munmap(m.first, m.second);
+  }
 }
 
 uint64_t PinnedArena::cls(uint64_t n) {
@@ -35,13 +41,22 @@ uint64_t PinnedArena::cls(uint64_t n) {
 }
 
 bool PinnedArena::add_slab(uint64_t bytes) {
-  void* q = nullptr;
-  if (cudaHostAlloc(&q, bytes, cudaHostAllocDefault) != cudaSuccess) {
+  // Map and touch the pages first, then register them: cudaHostAlloc holds
+  // the driver for the whole time it takes (about 75 ms per GiB), during
+  // which every CUDA call of every other thread waits; registering pages
+  // already present takes about 2 ms per GiB.
+  void* q = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (q == MAP_FAILED) return false;
+  const long page = sysconf(_SC_PAGESIZE);
+  const uint64_t step = page > 0 ? (uint64_t)page : 4096;
+  for (uint64_t o = 0; o < bytes; o += step) static_cast<volatile uint8_t*>(q)[o] = 0;
+  if (cudaHostRegister(q, bytes, cudaHostRegisterDefault) != cudaSuccess) {
     cudaGetLastError();
+    munmap(q, bytes);
     return false;
   }
   std::lock_guard<std::mutex> g(mu_);
-  all_.push_back(static_cast<uint8_t*>(q));
+  all_.emplace_back(static_cast<uint8_t*>(q), bytes);
   slabs_.push_back({static_cast<uint8_t*>(q), bytes});
   reserved_ += bytes;
   spare_ += bytes;
@@ -339,6 +354,12 @@ ServerStats Server::stats() {
   ServerStats s = st_;
   s.pinned_reserved = arena_.reserved();
   s.pinned_sync_grows = arena_.sync_grows();
+  if (pool_) {
+    cuuint64_t v = 0;
+    if (cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrReservedMemHigh, &v) == cudaSuccess) s.pool_reserved_high = v;
+    if (cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrUsedMemHigh, &v) == cudaSuccess) s.pool_used_high = v;
+    cudaGetLastError();
+  }
   return s;
 }
 
@@ -675,7 +696,11 @@ bool Server::try_start(Req& r) {
   const double t_room = now_ms();
   const bool over = used_bytes() + need > opt_.hbm_budget;
   const bool room = !over || make_room(need, r.pid);
-  if (over) st_.worker_ms[2] += now_ms() - t_room;
+  if (over) {
+    const double dt = now_ms() - t_room;
+    st_.worker_ms[2] += dt;
+    st_.worker_max_ms[2] = std::max(st_.worker_max_ms[2], dt);
+  }
   if (!room) {
     if (flights_.empty() && spills_.empty()) {
       // nothing in flight will free memory: the request cannot fit
@@ -702,7 +727,9 @@ bool Server::try_start(Req& r) {
   cudaEventRecord(f.done, p.s);
   flights_.push_back(f);
   std::lock_guard<std::mutex> g(mu_);
-  st_.worker_ms[0] += now_ms() - t_start;
+  const double dt = now_ms() - t_start;
+  st_.worker_ms[0] += dt;
+  st_.worker_max_ms[0] = std::max(st_.worker_max_ms[0], dt);
   st_.inflight_peak = std::max<uint32_t>(st_.inflight_peak, (uint32_t)flights_.size());
   const uint64_t u = used_bytes();
   st_.hbm_used = u;
@@ -824,7 +851,9 @@ void Server::worker() {
       flights_.erase(flights_.begin() + (long)i);
       const double t_fin = now_ms();
       finish(f);
-      st_.worker_ms[1] += now_ms() - t_fin;
+      const double dt = now_ms() - t_fin;
+      st_.worker_ms[1] += dt;
+      st_.worker_max_ms[1] = std::max(st_.worker_max_ms[1], dt);
       progress = true;
     }
     // 2. past 90% of the budget, make room ahead of need until 87.5% stays
@@ -837,7 +866,9 @@ void Server::worker() {
       const uint64_t low = opt_.hbm_budget - opt_.hbm_budget / 8;
       drop_scratch(low + spilling_bytes_, UINT32_MAX);
       spill_chains(low, UINT32_MAX, kSpillStepBytes);
-      st_.worker_ms[2] += now_ms() - t_room;
+      const double dt = now_ms() - t_room;
+      st_.worker_ms[2] += dt;
+      st_.worker_max_ms[2] = std::max(st_.worker_max_ms[2], dt);
     }
     // 3. admission in submission order; one request per process at a time
     std::set<uint32_t> seen;

@@ -71,20 +71,22 @@ struct ServerStats {
   uint64_t graph_captures = 0, graph_replays = 0;
   uint64_t hbm_used = 0, hbm_peak = 0, pinned_reserved = 0;
   uint64_t pinned_sync_grows = 0;  // slabs the worker had to pin itself
+  uint64_t pool_reserved_high = 0, pool_used_high = 0;  // device bytes the pool mapped / handed out, peaks
   uint64_t deferred_admissions = 0;  // admission attempts refused for memory
   uint32_t inflight_peak = 0;
   double worker_ms[4] = {0, 0, 0, 0};  // host time of the worker: starting requests,
                                        // finishing them, making room, waiting
+  double worker_max_ms[3] = {0, 0, 0};  // longest single start, finish, room-making pass
 };
 
 // Pinned host memory for spills, in blocks of quarter-power-of-two classes
 // (64 KiB, then p, 1.25p, 1.5p, 1.75p for each power of two p: at most a
-// quarter of a block is unused), reused, freed at destruction (cudaFreeHost
-// would wait for the whole device).  Blocks are carved from slabs of at least
-// 256 MiB.  Pinning a slab takes tens of milliseconds, so with keep_spare() a
-// helper thread pins the next slabs while the unused slab space is below the
-// given size, and the thread that allocates pins only when the helper has
-// fallen behind.  All members are thread-safe.
+// quarter of a block is unused), reused, freed at destruction.  Blocks are
+// carved from slabs of at least 256 MiB, mapped, touched and then registered
+// with CUDA.  Touching a slab's pages takes tens of milliseconds, so with
+// keep_spare() a helper thread prepares the next slabs while the unused slab
+// space is below the given size, and the thread that allocates pins only when
+// the helper has fallen behind.  All members are thread-safe.
 class PinnedArena {
  public:
   ~PinnedArena();
@@ -111,7 +113,7 @@ class PinnedArena {
   uint64_t spare_target_ = 0;
   uint64_t spare_ = 0;  // unused slab bytes
   std::map<uint64_t, std::vector<uint8_t*>> free_;
-  std::vector<uint8_t*> all_;
+  std::vector<std::pair<uint8_t*, uint64_t>> all_;  // mapped and registered slabs
   std::vector<Slab> slabs_;
   uint64_t reserved_ = 0;
   uint64_t sync_grows_ = 0;

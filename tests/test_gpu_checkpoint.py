@@ -118,7 +118,7 @@ def test_epochs_rebased_near_their_limit(cuda, mtc, oracle, monkeypatch):
 
 @pytest.mark.parametrize("kind", [0, 1], ids=["murmur3", "md5"])
 @pytest.mark.parametrize("approach", [3, 4], ids=["list", "tree"])
-@pytest.mark.parametrize("issue", ["in_place", "alternating", "eager"])
+@pytest.mark.parametrize("issue", ["in_place", "alternating", "eager", "untimed"])
 def test_graph_replay_matches_oracle(cuda, mtc, oracle, kind, approach, issue):
     # the single-call path replays a captured launch sequence: on the same
     # buffer rewritten in place, on two buffers taking turns (the sequence
@@ -129,12 +129,18 @@ def test_graph_replay_matches_oracle(cuda, mtc, oracle, kind, approach, issue):
     gpu = mtc.Deduplicator(cs, kind, approach=approach)
     if issue == "eager":
         gpu.set_tuning(eager=1)
+    if issue == "untimed":
+        gpu.set_tuning(untimed=1)
     bufs = [cuda.empty(nbytes, dtype=cuda.uint8, device="cuda") for _ in range(2)]
     for i, s in enumerate(seq):
-        buf = bufs[i % 2] if issue == "alternating" else bufs[0]
+        buf = bufs[i % 2] if issue in ("alternating", "untimed") else bufs[0]
         buf.copy_(cuda.from_numpy(s))
         assert gpu.checkpoint(buf, i == 0) == ref.checkpoint(s, i == 0), (issue, i)
+        if issue == "untimed" and i > 0:
+            # one graph without the phase events: no phase times
+            assert list(gpu.info().phase_times) == [0.0, 0.0, 0.0]
     assert gpu.tuning()["eager"] == (1 if issue == "eager" else 0)
+    assert gpu.tuning()["untimed"] == (1 if issue == "untimed" else 0)
     gpu.close()
 
 
