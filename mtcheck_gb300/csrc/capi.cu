@@ -240,9 +240,14 @@ int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* 
     if (rc == MTC_OK) h->eng->restart_timers[0] = 0;  // no staging copy
     return ret_eng(rc, h->eng);
   }
-  uint8_t* dev = nullptr;
-  if (cudaMalloc(&dev, total ? total : 1) != cudaSuccess) return ret(MTC_ENOMEM, "cannot stage the chain");
+  // a staging buffer kept by the handle: no allocation, and no cudaFree
+  // (which would wait for the whole device), per call
   cudaStream_t s = h->eng->stream();
+  if (h->eng->restart_stage.ensure(total ? total : 1, s) != cudaSuccess) {
+    cudaGetLastError();
+    return ret(MTC_ENOMEM, "cannot stage the chain");
+  }
+  uint8_t* dev = h->eng->restart_stage.p;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
@@ -264,7 +269,6 @@ int mtc_restart(mtc_dedup_t* h, void* dev_out, uint64_t len, const void* const* 
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  cudaFree(dev);
   return ret_eng(rc, h->eng);
 }
 
@@ -341,15 +345,22 @@ int mtc_hash_chunks(int hash, const void* dev_data, uint64_t len, uint32_t chunk
   a.epi = mtc::EPI_HASH;
   mtc::TmaCache cache;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
-  // a device error word for the call (a bounded wait that runs out sets it)
-  uint32_t* err = nullptr;
+  // a device error word for the call (a bounded wait that runs out sets it):
+  // one per host thread and device, allocated on the thread's first call and
+  // kept (an allocation per call would go through the default memory pool,
+  // whose release at every synchronisation maps and unmaps device memory)
+  thread_local uint32_t* tl_err[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return ret(MTC_ENOTSUP, "device ordinal above 63");
+  cudaError_t e = cudaSuccess;
+  if (!tl_err[dev]) e = cudaMalloc(reinterpret_cast<void**>(&tl_err[dev]), sizeof(uint32_t));
+  uint32_t* err = e == cudaSuccess ? tl_err[dev] : nullptr;
   uint32_t err_host = 0;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&err), sizeof(uint32_t), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
   a.err = err;
   if (e == cudaSuccess) e = mtc::launch_leaves(a, &cache, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err_host, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-  if (err) cudaFreeAsync(err, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return ret(e == cudaErrorMemoryAllocation ? MTC_ENOMEM : MTC_ECUDA, cudaGetErrorString(e));
   if (err_host & mtc::DERR_SPIN) return ret(MTC_ETIMEOUT, "bounded device wait expired");

@@ -86,6 +86,8 @@ Engine::~Engine() {
   if (err_host_) cudaFreeHost(err_host_);
   if (sp_host_) cudaFreeHost(sp_host_);
   if (hdr_host_) cudaFreeHost(hdr_host_);
+  if (rdi_ev_) cudaEventDestroy(rdi_ev_);
+  if (rdi_host_) cudaFreeHost(rdi_host_);
   release_retired();
   destroy_restart_scratch(rs_);
 }
@@ -733,6 +735,7 @@ void Engine::for_each_buf(F f) {
 void Engine::set_pool(cudaMemPool_t pool) {
   pool_ = pool;
   for_each_buf([&](auto& b) { b.pool = pool; });
+  restart_stage.pool = pool;
 }
 
 uint64_t Engine::spill_bytes() const {
@@ -793,6 +796,7 @@ void Engine::release_restart_scratch() {
     destroy_restart_scratch(rs_);  // stream-ordered frees
     rs_ = nullptr;
   }
+  restart_stage.release(stream_);
 }
 
 uint64_t Engine::device_bytes() const {

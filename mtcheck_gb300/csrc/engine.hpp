@@ -7,6 +7,9 @@
 #include <string>
 #include <vector>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "mtc_common.cuh"
@@ -39,6 +42,30 @@ struct HeaderHost {  // header_t, include/utils.hpp:29-37
   uint32_t chunk_size, num_first_ocur, num_prior_chkpts, num_shift_dupl;
 };
 static_assert(sizeof(HeaderHost) == 32, "header_t is 32 bytes");
+
+// MTCHECK_SERVER_TRACE=1: every host step timed by a StepTimer that takes
+// longer than 20 ms is reported on stderr with its name and duration (the
+// served worker's steps and the parts of a restart's enqueue).
+inline bool trace_on() {
+  static const bool v = [] {
+    const char* e = std::getenv("MTCHECK_SERVER_TRACE");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+struct StepTimer {
+  const char* what;
+  uint32_t id;
+  std::chrono::steady_clock::time_point t0;
+  StepTimer(const char* w, uint32_t i) : what(w), id(i) {
+    if (trace_on()) t0 = std::chrono::steady_clock::now();
+  }
+  ~StepTimer() {
+    if (!trace_on()) return;
+    const double dt = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (dt > 20.0) std::fprintf(stderr, "mtc-trace: %s (%u) took %.1f ms\n", what, id, dt);
+  }
+};
 
 // Grow-only device array.  With a memory pool set, allocation and release
 // are stream-ordered (cudaMallocFromPoolAsync / cudaFreeAsync on the stream
@@ -297,7 +324,18 @@ class Engine {
   // resolved chunk ranges), and the events that fork and join it
   cudaStream_t rside_ = nullptr;
   cudaEvent_t rev_[12] = {};
+  // pinned staging of a restart's chain descriptors (kept when the restart
+  // tables are released: freeing pinned memory waits for the device), and
+  // the event after their last upload
+  void* rdi_host_ = nullptr;
+  size_t rdi_host_bytes_ = 0;
+  cudaEvent_t rdi_ev_ = nullptr;
   DevBuf<uint8_t> hdr_dev_;         // read_headers: gathered headers
+ public:
+  // A host chain copied to device memory for a restart (the staging path of
+  // mtc_restart); kept between restarts, released with the restart tables.
+  DevBuf<uint8_t> restart_stage;
+ private:
   uint8_t* hdr_host_ = nullptr;     // pinned copy of them
   size_t hdr_host_cap_ = 0;
   std::vector<void*> retired_;    // replaced map tables awaiting cudaFree

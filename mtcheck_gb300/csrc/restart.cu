@@ -1094,11 +1094,13 @@ int Engine::read_headers(const std::vector<const uint8_t*>& ptrs, const std::vec
   if (n == 0) return ST_OK;
   MTC_CUDA_R(hdr_dev_.ensure(bytes, stream_));
   if (hdr_host_cap_ < bytes) {
+    // grown geometrically, as the descriptors below
+    const size_t cap = std::max<size_t>({bytes, 2 * hdr_host_cap_, 16u << 10});
     if (hdr_host_) cudaFreeHost(hdr_host_);
     hdr_host_ = nullptr;
     hdr_host_cap_ = 0;
-    MTC_CUDA_R(cudaMallocHost(reinterpret_cast<void**>(&hdr_host_), bytes));
-    hdr_host_cap_ = bytes;
+    MTC_CUDA_R(cudaMallocHost(reinterpret_cast<void**>(&hdr_host_), cap));
+    hdr_host_cap_ = cap;
   }
   for (size_t i0 = 0; i0 < n; i0 += kHeaderBatch) {
     HeaderSrc src{};
@@ -1119,9 +1121,9 @@ int Engine::read_headers(const std::vector<const uint8_t*>& ptrs, const std::vec
 }
 
 uint64_t Engine::restart_scratch_bytes() const {
-  if (!rs_) return 0;
+  if (!rs_) return restart_stage.n;
   const RestartScratch& R = *rs_;
-  uint64_t b = sizeof(DiffInfo) * R.di.n + sizeof(uint4) * R.fo_rng.n;
+  uint64_t b = restart_stage.n + sizeof(DiffInfo) * R.di.n + sizeof(uint4) * R.fo_rng.n;
   for (const auto* x : {&R.fo_node, &R.fo_seg, &R.fo_clen, &R.sh_node, &R.sh_prev, &R.sh_tree, &R.sh_seg, &R.rrs,
                         &R.fo_at, &R.dm_off, &R.sbm, &R.nbv})
     b += sizeof(uint32_t) * x->n;
@@ -1244,8 +1246,27 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     if (pool_) set_scratch_pool(rs_, pool_);
   }
   RestartScratch& R = *rs_;
+  StepTimer t_alloc("restart: table allocations", N);
   MTC_CUDA_R(R.di.ensure(di.size(), s));
-  MTC_CUDA_R(cudaMemcpyAsync(R.di.p, di.data(), sizeof(DiffInfo) * di.size(), cudaMemcpyHostToDevice, s));
+  // the chain descriptors go up from pinned memory: a copy from pageable
+  // memory would first wait for everything already on the stream
+  StepTimer t_up("restart: descriptor upload", N);
+  const size_t di_bytes = sizeof(DiffInfo) * di.size();
+  if (rdi_ev_) MTC_CUDA_R(cudaEventSynchronize(rdi_ev_));  // the previous restart's copy has read it
+  else MTC_CUDA_R(cudaEventCreateWithFlags(&rdi_ev_, cudaEventDisableTiming));
+  if (rdi_host_bytes_ < di_bytes) {
+    // grown geometrically: a chain grows by one diff per checkpoint, and
+    // freeing pinned memory waits for the whole device
+    const size_t cap = std::max<size_t>({di_bytes, 2 * rdi_host_bytes_, 64u << 10});
+    if (rdi_host_) cudaFreeHost(rdi_host_);
+    rdi_host_ = nullptr;
+    rdi_host_bytes_ = 0;
+    MTC_CUDA_R(cudaMallocHost(&rdi_host_, cap));
+    rdi_host_bytes_ = cap;
+  }
+  std::memcpy(rdi_host_, di.data(), di_bytes);
+  MTC_CUDA_R(cudaMemcpyAsync(R.di.p, rdi_host_, di_bytes, cudaMemcpyHostToDevice, s));
+  MTC_CUDA_R(cudaEventRecord(rdi_ev_, s));
   MTC_CUDA_R(R.fo_node.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_seg.ensure(nfo + 1, s));
   MTC_CUDA_R(R.fo_rng.ensure(nfo + 1, s));
@@ -1319,6 +1340,7 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     for (auto& e : rev_) MTC_CUDA_R(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   cudaStream_t side = rside_;
+  StepTimer t_fork("restart: fork and clears", N);
   MTC_CUDA_R(cudaEventRecord(rev_[0], s));  // after the allocations and the previous restart
   MTC_CUDA_R(cudaStreamWaitEvent(side, rev_[0], 0));
   MTC_CUDA_R(cudaMemsetAsync(R.fo_at.p, 0xff, sizeof(uint32_t) * ((size_t)M + 2), side));
@@ -1326,6 +1348,7 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(cudaEventRecord(rev_[1], side));
 
   // 1-3: decode entries, repeat tables, source checkpoints
+  StepTimer t_dec("restart: entry launches", N);
   MTC_CUDA_R(cudaMemsetAsync(R.tot.p, 0, sizeof(uint64_t) * 5, s));
   if (nfo + nsh) { load_entries_kernel<<<gsz((uint64_t)nfo + nsh), 256, 0, s>>>(a); note_launch(); }
   rrs_kernel<<<gsz(di.size(), 1, 4), 256, 0, s>>>(a);
@@ -1383,6 +1406,7 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
   MTC_CUDA_R(cudaStreamWaitEvent(s, rev_[3], 0));
   // 4: every chunk's source, 5: the copy; range by range, each range copied
   // on the second stream while the next is resolved
+  StepTimer t_rc("restart: resolve and copy launches", N);
   const uint32_t parts = restart_parts(N);
   const uint64_t per = ((uint64_t)N + parts - 1) / parts;
   const uint64_t step = (per + 31) / 32 * 32;

@@ -1,6 +1,8 @@
 // server.cu -- the request-serving loop (see server.hpp).
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <set>
@@ -12,8 +14,36 @@
 
 namespace mtc {
 
-// diff bytes the worker copies out ahead of need in one pass of its loop
+// diff bytes the worker copies out ahead of need in one pass of its loop,
+// and at most in flight on the copy engine from those passes: a deeper
+// queue of copies makes every other copy of the process (an archive, a
+// caller's read-back) wait behind it
 constexpr uint64_t kSpillStepBytes = 64ull << 20;
+constexpr uint64_t kSpillInFlightBytes = 512ull << 20;
+
+// Device-to-device copy of an archived diff by the SMs rather than a copy
+// engine (which the spills keep busy).  Sources are 4-byte aligned (a diff
+// starts at its staging buffer's pad, a multiple of 4), destinations are
+// pool allocations.
+__global__ void archive_copy_kernel(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src, uint64_t n) {
+  const uint64_t words = n / 4;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t* s4 = reinterpret_cast<const uint32_t*>(src);
+  uint32_t* d4 = reinterpret_cast<uint32_t*>(dst);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += stride) d4[i] = s4[i];
+  const uint64_t t = words * 4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n && t < words * 4 + 4) dst[t] = src[t];
+}
+static cudaError_t archive_copy(uint8_t* dst, const uint8_t* src, uint64_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  if ((reinterpret_cast<uintptr_t>(src) & 3) || (reinterpret_cast<uintptr_t>(dst) & 3))
+    return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, s);
+  const uint64_t words = n / 4 + 1;
+  const uint64_t blocks = std::min<uint64_t>((words + 255) / 256, 1024);
+  archive_copy_kernel<<<(unsigned)blocks, 256, 0, s>>>(dst, src, n);
+  return cudaGetLastError();
+}
+
 
 // ---------------------------------------------------------------------------
 // PinnedArena
@@ -170,7 +200,11 @@ Server::Server(const ServerOptions& o) : opt_(o) {
     cudaStream_t s = nullptr;
     cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     void* p = nullptr;
-    if (cudaMallocFromPoolAsync(&p, opt_.hbm_budget, pool_, s) == cudaSuccess) cudaFreeAsync(p, s);
+    // the budget and an eighth more: staged restart inputs and the pool's
+    // fragmentation are outside the budget's accounting, and growing the
+    // pool while requests run maps memory under the driver's lock
+    if (cudaMallocFromPoolAsync(&p, opt_.hbm_budget + opt_.hbm_budget / 8, pool_, s) == cudaSuccess)
+      cudaFreeAsync(p, s);
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     cudaGetLastError();
@@ -634,6 +668,7 @@ int Server::start_checkpoint(Req& r, Proc& p) {
     restored = true;
   }
   if (cudaStreamWaitEvent(p.s, r.ready, 0) != cudaSuccess) return ST_ECUDA;
+  StepTimer st_ck("checkpoint start", r.pid);
   int rc = e.prepare(r.data, r.len, r.make_baseline, opt_.id_headroom);
   if (rc) return rc;
   // a restored state has new device addresses: issuing it once costs less
@@ -661,6 +696,7 @@ int Server::start_restart(Req& r, Proc& p, std::vector<uint8_t*>* temps) {
     int rc = restore_state(p);
     if (rc) return rc;
   }
+  StepTimer st_all("restart start", r.pid);
   const size_t n = p.chain.size();
   std::vector<const uint8_t*> ptrs(n, nullptr);
   std::vector<uint64_t> lens(n, 0);
@@ -685,6 +721,7 @@ int Server::start_restart(Req& r, Proc& p, std::vector<uint8_t*>* temps) {
     }
   }
   if (cudaStreamWaitEvent(p.s, r.ready, 0) != cudaSuccess) return ST_ECUDA;
+  StepTimer st_enq("restart_enqueue", r.pid);
   int rc = e.restart_enqueue(r.out, r.len, ptrs, lens, hdrs, r.chkpt_id);
   for (uint8_t* t : *temps) cudaFreeAsync(t, p.s);  // after the restart, in stream order
   return rc;
@@ -746,16 +783,21 @@ void Server::finish(Flight& f) {
     set_error(e.last_error);
   } else if (f.r.kind == REQ_CHECKPOINT) {
     HeaderHost h{};
-    int rc = e.complete(f.r.len, &h);
-    e.release_retired();
+    int rc;
+    {
+      StepTimer t("complete", f.r.pid);
+      rc = e.complete(f.r.len, &h);
+      e.release_retired();
+    }
     c.status = rc;
     if (rc == ST_OK) {
       const uint64_t n = e.diff_len();
       Archived a;
       a.len = n;
       a.hdr = h;
+      StepTimer t_arch("archive", f.r.pid);
       if (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&a.dev), n ? n : 1, pool_, p.s) == cudaSuccess) {
-        cudaMemcpyAsync(a.dev, e.diff_device(), n, cudaMemcpyDeviceToDevice, p.s);
+        archive_copy(a.dev, e.diff_device(), n, p.s);
       } else {
         // no device memory for the archive: keep it in pinned host memory
         cudaGetLastError();
@@ -782,6 +824,7 @@ void Server::finish(Flight& f) {
       // its allocations and its graph capture then cost the next request
       // nothing (a new input pointer or baseline still re-prepares)
       // (not under memory pressure: the process may be spilled before then)
+      StepTimer t_next("next-step prepare", f.r.pid);
       if (c.status == ST_OK && opt_.use_graph && e.mode() != MODE_FULL &&
           used_bytes() < opt_.hbm_budget - opt_.hbm_budget / 10 &&
           e.prepare(f.r.data, f.r.len, false, opt_.id_headroom) == ST_OK)
@@ -790,6 +833,7 @@ void Server::finish(Flight& f) {
       set_error(e.last_error);
     }
   } else {
+    StepTimer t("restart complete", f.r.pid);
     int rc = e.restart_complete();
     c.status = rc;
     c.chkpt_id = f.r.chkpt_id;
@@ -865,7 +909,8 @@ void Server::worker() {
       const double t_room = now_ms();
       const uint64_t low = opt_.hbm_budget - opt_.hbm_budget / 8;
       drop_scratch(low + spilling_bytes_, UINT32_MAX);
-      spill_chains(low, UINT32_MAX, kSpillStepBytes);
+      if (spilling_bytes_ < kSpillInFlightBytes)
+        spill_chains(low, UINT32_MAX, std::min(kSpillStepBytes, kSpillInFlightBytes - spilling_bytes_));
       const double dt = now_ms() - t_room;
       st_.worker_ms[2] += dt;
       st_.worker_max_ms[2] = std::max(st_.worker_max_ms[2], dt);

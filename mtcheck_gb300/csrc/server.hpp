@@ -42,8 +42,9 @@ struct ServerOptions {
   // captures one when a process's buffers move; during that capture a
   // device-wide synchronisation by any thread of the application fails.
   int use_graph = 0;
-  // Allocate the HBM budget from the server's pool once at creation (and
-  // keep it there), and pin this much host memory for spills up front:
+  // Allocate the HBM budget (and an eighth more, for what its accounting
+  // leaves out) from the server's pool once at creation and keep it there,
+  // and pin this much host memory for spills up front:
   // growing either later costs milliseconds per allocation.  With a pinned
   // reserve, a helper thread also keeps an eighth of it unused and pinned
   // ahead of the spills.
