@@ -488,6 +488,12 @@ def batch_bench(torch, mc, dev, a):
         b.autotune(bufs)
     tune_s = time.perf_counter() - t0
     tunes = [m.tuning() for m in b.members]
+    # the members' state reserved in one allocation of their pool; timed and
+    # counted in the batched job (in its baseline step)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reserved = b.reserve(bufs)
+    reserve_s = time.perf_counter() - t0
     per_call, batched, batched_dev, identical, diff_total = [], [], [], True, 0
     per_call_dev, host_parts, mismatches = [], [], []
     all_pc, all_b = [], []
@@ -508,7 +514,9 @@ def batch_bench(torch, mc, dev, a):
         t2 = time.perf_counter()
         info = b.info()
         all_pc.append(t1 - t0)
-        all_b.append(t2 - t1)
+        all_b.append(t2 - t1 + (reserve_s if step == 0 else 0.0))
+        if step == 0:
+            baseline_host = [round(x, 3) for x in info.host_ms]
         if step:
             per_call.append(t1 - t0)
             per_call_dev.append(pdev)
@@ -554,6 +562,10 @@ def batch_bench(torch, mc, dev, a):
         "speedup_incremental": round(pc / bt, 3),
         "speedup_steady": round(pc / steady, 3),
         "job_s": {"per_call": round(sum(all_pc), 4), "batched": round(sum(all_b), 4)},
+        "baseline_s": {"per_call": round(all_pc[0], 4), "batched": round(all_b[0], 4)},
+        "reserve": {"seconds": round(reserve_s, 4), "bytes": reserved,
+                    "note": "mtc_batch_reserve before the first step; counted in the batched baseline step"},
+        "baseline_host_ms": dict(zip(("prepare", "capture", "issue", "wait", "complete"), baseline_host)),
         "per_call_ms": round(pc * 1e3, 3), "batched_ms": round(bt * 1e3, 3),
         "batched_steady_ms": round(steady * 1e3, 3),
         "identical_to_per_call": identical,
@@ -1102,6 +1114,16 @@ def main():
                "step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]}
         del host, pinned_out, out_view, bufs
 
+    # the served stream runs first among the sections: a server created in a
+    # process after the 96-member batch section measured six times slower
+    # worker calls (cause not found), so that order would not be the
+    # server's own figure
+    srvd = None
+    if not a.no_serve and rank == 0:
+        torch.cuda.empty_cache()
+        srvd = serve_bench(torch, mc, dev, a)
+        torch.cuda.empty_cache()
+
     md5 = small = None
     if rank == 0 and not a.no_sections:
         md5 = md5_section(torch, mc, dev, states[:1 + W + K], cs, W, peak)
@@ -1135,12 +1157,6 @@ def main():
     if not a.no_batch and rank == 0:
         torch.cuda.empty_cache()
         bat = batch_bench(torch, mc, dev, a)
-        torch.cuda.empty_cache()
-
-    srvd = None
-    if not a.no_serve and rank == 0:
-        torch.cuda.empty_cache()
-        srvd = serve_bench(torch, mc, dev, a)
         torch.cuda.empty_cache()
 
     cpu = None

@@ -235,6 +235,10 @@ int mtc_batch_get_info(const mtc_batch_t* b, mtc_batch_info_t* out);
  * and power-of-two length; lengths above 64 MiB share one 64 MiB trial) and
  * apply the winners */
 int mtc_batch_autotune(mtc_batch_t* b, const uint64_t* lens);
+/* reserve device memory, now, for every member's state on buffers of these
+ * lengths (the members' pool keeps it), so that the first checkpoint does not
+ * grow the pool; *bytes (may be NULL) receives the amount reserved */
+int mtc_batch_reserve(mtc_batch_t* b, const uint64_t* lens, uint64_t* bytes);
 
 /* ---- request serving (no counterpart in the reference: its MPI driver runs
  * one process per rank, src/dedup_files_mpi.cpp:54-120) ----

@@ -130,6 +130,7 @@ SIGNATURES = {
     "mtc_batch_set_options": (_I, [_VP, _I, _U32]),
     "mtc_batch_get_info": (_I, [_VP, ctypes.POINTER(BatchInfo)]),
     "mtc_batch_autotune": (_I, [_VP, ctypes.POINTER(_U64)]),
+    "mtc_batch_reserve": (_I, [_VP, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "mtc_server_create": (_I, [ctypes.POINTER(ServerOptions), ctypes.POINTER(_VP)]),
     "mtc_server_destroy": (_I, [_VP]),
     "mtc_server_add_process": (_I, [_VP, _I, _I, _U32, ctypes.POINTER(_U32)]),
@@ -411,6 +412,14 @@ class Batch:
     def autotune(self, bufs):
         lens = (_U64 * len(bufs))(*[_dev_ptr(x)[1] for x in bufs])
         _check(load().mtc_batch_autotune(self.b, lens))
+
+    def reserve(self, bufs):
+        """Reserve device memory for every member's state on these buffers;
+        returns the bytes reserved."""
+        lens = (_U64 * len(bufs))(*[_dev_ptr(x)[1] for x in bufs])
+        out = _U64()
+        _check(load().mtc_batch_reserve(self.b, lens, ctypes.byref(out)))
+        return int(out.value)
 
     def checkpoint(self, bufs, make_baseline=False):
         """One checkpoint of every member; returns the list of diff sizes."""

@@ -125,6 +125,19 @@ int Batch::add(int mode, int hash_kind, uint32_t chunk_size) {
                                        std::string(#call) + ": " + cudaGetErrorString(e_));          \
   } while (0)
 
+int Batch::reserve(const uint64_t* lens, uint64_t* bytes) {
+  uint64_t total = 0;
+  for (size_t i = 0; i < engs_.size(); i++)
+    total += estimate_state_bytes(engs_[i]->mode(), lens[i], engs_[i]->chunk_size());
+  if (bytes) *bytes = total;
+  if (!pool_) return fail(ST_ENOTSUP, "the batch allocates without a memory pool (MTCHECK_BATCH_POOL=0)");
+  void* p = nullptr;
+  MTC_BCUDA(cudaMallocFromPoolAsync(&p, total ? total : 1, pool_, origin_));
+  MTC_BCUDA(cudaFreeAsync(p, origin_));
+  MTC_BCUDA(cudaStreamSynchronize(origin_));
+  return ST_OK;
+}
+
 // The member's sequence reaches its leaf pass while being captured: when
 // its leaves can go through the batched launch, keep its record, close the
 // capture there (the part before the leaves) and open the part after it,

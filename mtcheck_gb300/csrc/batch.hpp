@@ -51,6 +51,10 @@ class Batch : public Engine::LeafHook {
   // One checkpoint of every member (the reference's checkpoint(data, len,
   // diff_h, make_baseline) overload per member, current_id advanced).
   int checkpoint(const uint8_t* const* data, const uint64_t* lens, bool make_baseline, uint64_t* diff_lens);
+  // Grow the members' memory pool, now, to hold their state for buffers of
+  // these lengths (allocated once and returned to the pool, which keeps it),
+  // so that the first checkpoint allocates without growing the pool.
+  int reserve(const uint64_t* lens, uint64_t* bytes);
   void set_use_graph(bool g) { use_graph_ = g; }
   void set_id_headroom(uint32_t h) { headroom_ = h ? h : 1; }
   // off: every member launches its own leaf kernels in its graph (no

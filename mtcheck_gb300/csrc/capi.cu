@@ -462,6 +462,13 @@ int mtc_batch_get_info(const mtc_batch_t* b, mtc_batch_info_t* o) {
   return MTC_OK;
 }
 
+int mtc_batch_reserve(mtc_batch_t* b, const uint64_t* lens, uint64_t* bytes) {
+  if (!b || !lens) return ret(MTC_EINVAL, "NULL argument");
+  const int rc = b->b->reserve(lens, bytes);
+  if (rc) return ret(rc, b->b->last_error);
+  return MTC_OK;
+}
+
 int mtc_batch_autotune(mtc_batch_t* b, const uint64_t* lens) {
   if (!b || !lens) return ret(MTC_EINVAL, "NULL argument");
   for (uint32_t i = 0; i < b->b->size(); i++) {

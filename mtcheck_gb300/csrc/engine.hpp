@@ -43,6 +43,20 @@ struct HeaderHost {  // header_t, include/utils.hpp:29-37
 };
 static_assert(sizeof(HeaderHost) == 32, "header_t is 32 bytes");
 
+// Device bytes of an engine's state for a buffer of `len` bytes in chunks of
+// `cs`: digests, labels, lists, digest map at load <= 3/4, staging for the
+// largest diff (the server's admission and a batch's reservation use it).
+inline uint64_t estimate_state_bytes(int mode, uint64_t len, uint32_t cs) {
+  const uint64_t N = (len + cs - 1) / cs, M = 2 * N;
+  if (mode == MODE_FULL) return len + 64;
+  const bool tree = mode == MODE_TREE || mode == MODE_TREE_LOW_OFFSET || mode == MODE_TREE_LOW_OFFSET_REF;
+  const uint64_t nd = tree ? M : N;
+  uint64_t slots = 1;
+  while (slots < nd * 4 / 3 + 1) slots <<= 1;
+  const uint64_t map = mode == MODE_BASIC ? 0 : slots * 2 * sizeof(MapSlot);
+  return nd * (sizeof(Digest) + 2) + N * 64 + map + (N + 1) * (cs + 12) + (1u << 20);
+}
+
 // MTCHECK_SERVER_TRACE=1: every host step timed by a StepTimer that takes
 // longer than 20 ms is reported on stderr with its name and duration (the
 // served worker's steps and the parts of a restart's enqueue).

@@ -409,30 +409,13 @@ void Server::push_completion(const Completion& c) {
 }
 
 // ---- memory accounting -----------------------------------------------------
-static uint64_t pow2_at_least(uint64_t v) {
-  uint64_t c = 1;
-  while (c < v) c <<= 1;
-  return c;
-}
-
-// Device bytes of an engine's state for a buffer of `len` bytes: digests,
-// labels, lists, digest map at load <= 3/4, staging for the largest diff.
-static uint64_t estimate_state(int mode, uint64_t len, uint32_t cs) {
-  const uint64_t N = (len + cs - 1) / cs, M = 2 * N;
-  if (mode == MODE_FULL) return len + 64;
-  const bool tree = mode == MODE_TREE || mode == MODE_TREE_LOW_OFFSET || mode == MODE_TREE_LOW_OFFSET_REF;
-  const uint64_t nd = tree ? M : N;
-  const uint64_t map = mode == MODE_BASIC ? 0 : pow2_at_least(nd * 4 / 3 + 1) * 2 * sizeof(MapSlot);
-  return nd * (sizeof(Digest) + 2) + N * 64 + map + (N + 1) * (cs + 12) + (1u << 20);
-}
-
 uint64_t Server::need_bytes(const Req& r, const Proc& p) const {
   const Engine& e = *p.eng;
   const uint64_t N = (r.len + e.chunk_size() - 1) / e.chunk_size();
   uint64_t need = 0;
-  if (e.spilled()) need += p.spill_len + estimate_state(e.mode(), r.len, e.chunk_size()) / 2;
+  if (e.spilled()) need += p.spill_len + estimate_state_bytes(e.mode(), r.len, e.chunk_size()) / 2;
   if (r.kind == REQ_CHECKPOINT) {
-    if (p.state_dev == 0 && !e.spilled()) need += estimate_state(e.mode(), r.len, e.chunk_size());
+    if (p.state_dev == 0 && !e.spilled()) need += estimate_state_bytes(e.mode(), r.len, e.chunk_size());
     // the archived diff: the worst case is the whole buffer (a baseline);
     // afterwards twice the latest size, at least 1/16 of the buffer -- a
     // larger diff overshoots the budget until the next admission spills

@@ -211,6 +211,22 @@ def test_batch_autotune_keeps_output(cuda, mtc, states, lone):
     b.close()
 
 
+def test_batch_reserve_keeps_output(cuda, mtc, states, lone):
+    # memory reserved for the members' state before the first step: the same
+    # bytes, and at least the state of the largest member reserved
+    b = mtc.Batch([m[:3] for m in MIX])
+    bufs = [cuda.empty(m[3], dtype=cuda.uint8, device="cuda") for m in MIX]
+    reserved = b.reserve(bufs)
+    assert reserved > max(m[3] for m in MIX)
+    for step in range(STEPS):
+        for buf, seq in zip(bufs, states):
+            buf.copy_(cuda.from_numpy(seq[step]))
+        b.checkpoint(bufs, make_baseline=(step == 0))
+        for i, m in enumerate(b.members):
+            assert member_diff(mtc, m) == lone[i][step]
+    b.close()
+
+
 @pytest.mark.parametrize("kind", [0, 1], ids=["murmur3", "md5"])
 @pytest.mark.parametrize("cs", [16, 32, 64, 128, 512])
 @pytest.mark.parametrize("rows,ctas", [(128, 0), (128, 1), (128, 3), (256, 1), (256, 0)])
