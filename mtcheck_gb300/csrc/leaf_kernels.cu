@@ -124,7 +124,7 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
       label = FIRST_OCUR;
       created++;
     } else if (r == INS_EXISTING) {
-      const unsigned long long old = atomicMin(&s->win, win_of(epoch, node));
+      const unsigned long long old = win_min(&s->win, win_of(epoch, node));
       if (old == kWinEmpty || win_epoch(old) == epoch) {
         label = FIRST_OCUR;  // first seen by this launch: the lowest chunk keeps it
         note_dup(a, (uint32_t)k | kCheckCreator);
@@ -134,7 +134,7 @@ __global__ void leaf_insert_kernel(LeafArgs a) {
         // serial level) are fixed, since every insert of this launch carries
         // a larger epoch and leaves them alone, so one atomicMin on the
         // whole word lowers exactly its node
-        if (win_node(old) > node) atomicMin(&s->win, (old & ~0xffffffffull) | node);
+        if (win_node(old) > node) win_min(&s->win, (old & ~0xffffffffull) | node);
         label = FIRST_OCUR;
         note_dup(a, (uint32_t)k);
       }

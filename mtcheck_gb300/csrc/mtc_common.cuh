@@ -370,11 +370,30 @@ __device__ __forceinline__ uint4 claim_key(MapSlot* s, const Digest& k) {
   return make_uint4((uint32_t)olo, (uint32_t)(olo >> 32), (uint32_t)ohi, (uint32_t)(ohi >> 32));
 }
 
+// atomicMin on an entry's win word, read first: win only decreases, so a
+// value read at or below `w` (a stale read can only be higher than the
+// current one) means the atomic would change nothing, and the read stands in
+// for the value it would have returned: its epoch is the current one, and a
+// node read too high only makes a caller lower it once more, which changes
+// nothing either.
+__device__ __forceinline__ unsigned long long win_min(unsigned long long* p, unsigned long long w) {
+  const unsigned long long cur = __ldcg(p);
+  return cur <= w ? cur : atomicMin(p, w);
+}
+
 // The slot of k, claimed if absent: INS_NEW (this thread created the entry),
 // INS_EXISTING, or INS_FAILED (table full, error word set).
+// A key, once claimed, never changes within a launch, so the slot is read
+// before the compare-and-swap: a key that is already there (every duplicate
+// of a digest, thousands of times over in a run of equal chunks) costs a
+// load instead of an atomic on one contended line.  Only a read equal to k
+// is taken as it is; anything else (another key, an empty slot, or a 16-byte
+// read that saw half of a concurrent claim) goes through the atomic.
 __device__ inline int map_claim(const DigestMap& m, const Digest& k, uint64_t* slot, uint32_t* err) {
   uint64_t i = slot_of(k, m.mask);
   for (uint64_t probe = 0; probe <= m.mask; probe++) {
+    const uint4 seen = __ldcg(reinterpret_cast<const uint4*>(m.slots[i].key));
+    if (key_eq(seen, k)) { *slot = i; return INS_EXISTING; }
     const uint4 old = claim_key(&m.slots[i], k);
     if (key_empty(old)) { *slot = i; return INS_NEW; }
     if (key_eq(old, k)) { *slot = i; return INS_EXISTING; }
@@ -396,7 +415,7 @@ __device__ __forceinline__ int map_insert_win(const DigestMap& m, const Digest& 
   if (r == INS_FAILED) return r;
   MapSlot* s = &m.slots[*slot];
   if (r == INS_NEW) s->tree = tree;
-  *old_win = atomicMin(&s->win, win);
+  *old_win = win_min(&s->win, win);
   return r;
 }
 
