@@ -931,6 +931,32 @@ def summary_of(line):
     }
 
 
+def section_in_subprocess(flag, key, a):
+    """Run one section (`--only-serve`, `--only-batch`) in a fresh process of
+    this script with the section's options, and return its object.  The
+    served stream and the batch each measured worse in a process that had
+    run the other first (worker calls six times slower after the batch;
+    the batch's first allocations 35 times slower after the server), so
+    each is measured as a user would run it, in a process of its own."""
+    args = [sys.executable, os.path.abspath(__file__), flag]
+    for name in ("serve_procs", "serve_rate", "serve_seconds", "serve_budget_gb", "serve_inflight",
+                 "serve_verify_procs", "serve_pinned_gb", "serve_sat_procs", "serve_sat_requests",
+                 "batch_count", "batch_median_mib", "batch_steps"):
+        args += ["--" + name.replace("_", "-"), str(getattr(a, name))]
+    if a.batch_no_tune:
+        args.append("--batch-no-tune")
+    if a.serve_trace:
+        args += ["--serve-trace", a.serve_trace]
+    env = dict(os.environ, RANK="0", LOCAL_RANK=os.environ.get("LOCAL_RANK", "0"), WORLD_SIZE="1")
+    r = subprocess.run(args, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        return {"error": "section process exited %d: %s" % (r.returncode, r.stderr.strip().splitlines()[-1:])}
+    for line in reversed(r.stdout.strip().splitlines()):
+        if line.startswith("{"):
+            return json.loads(line).get(key)
+    return {"error": "section process printed no result"}
+
+
 def bind_local_cpus(torch, local):
     """Pin this process to the CPUs next to the GPU (sysfs local_cpulist of
     its PCI function), so that pinned host buffers are allocated on the GPU's
@@ -1114,15 +1140,11 @@ def main():
                "step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]}
         del host, pinned_out, out_view, bufs
 
-    # the served stream runs first among the sections: a server created in a
-    # process after the 96-member batch section measured six times slower
-    # worker calls (cause not found), so that order would not be the
-    # server's own figure
+    # the served stream and the batch run in processes of their own
     srvd = None
     if not a.no_serve and rank == 0:
         torch.cuda.empty_cache()
-        srvd = serve_bench(torch, mc, dev, a)
-        torch.cuda.empty_cache()
+        srvd = section_in_subprocess("--only-serve", "served", a)
 
     md5 = small = None
     if rank == 0 and not a.no_sections:
@@ -1156,8 +1178,7 @@ def main():
     bat = None
     if not a.no_batch and rank == 0:
         torch.cuda.empty_cache()
-        bat = batch_bench(torch, mc, dev, a)
-        torch.cuda.empty_cache()
+        bat = section_in_subprocess("--only-batch", "batched", a)
 
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu:
