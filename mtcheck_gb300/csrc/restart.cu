@@ -1045,6 +1045,21 @@ inline uint32_t gsz(uint64_t n, int threads = 256, int per_sm = 8) {
 
 }  // namespace
 
+// One wave of resolve_kernel: its CTAs do equal work, so a grid of 1.33
+// waves (eight CTAs per SM asked, six resident) would run its last third on
+// a third of the GPU.
+static uint32_t resolve_grid() {
+  static const uint32_t g = [] {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, resolve_kernel, 256, 0) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    return (uint32_t)(num_sms() * per_sm);
+  }();
+  return g;
+}
+
 // Chunk ranges the resolve and copy passes are pipelined over
 // (MTCHECK_RESTART_PARTS, 1-7; default 4, one below 2^16 chunks).
 static uint32_t restart_parts(uint32_t N) {
@@ -1415,7 +1430,7 @@ int Engine::restart_enqueue(uint8_t* dev_out, uint64_t len, const std::vector<co
     RArgs r = a;
     r.c_lo = (uint32_t)lo;
     r.c_hi = (uint32_t)std::min<uint64_t>(N, lo + step);
-    resolve_kernel<<<gsz(r.c_hi - r.c_lo), 256, 0, s>>>(r);
+    resolve_kernel<<<std::min(gsz(r.c_hi - r.c_lo), resolve_grid()), 256, 0, s>>>(r);
     if (parts == 1) {
       restore_copy_kernel<<<num_sms() * 3, 256, 0, s>>>(r);
     } else {
