@@ -1060,12 +1060,14 @@ static uint32_t resolve_grid() {
   return g;
 }
 
-// Chunk ranges the resolve and copy passes are pipelined over
-// (MTCHECK_RESTART_PARTS, 1-7; default 4, one below 2^16 chunks).
+// Chunk ranges the resolve and copy passes can be pipelined over
+// (MTCHECK_RESTART_PARTS, 1-7; one below 2^16 chunks).  One by default: with
+// resolve in one wave, four ranges measured 0.690 ms against 0.683 ms for
+// one at 1 GiB / 256 B (the copy already holds every SM).
 static uint32_t restart_parts(uint32_t N) {
   static int v = [] {
     const char* e = std::getenv("MTCHECK_RESTART_PARTS");
-    const int x = e ? std::atoi(e) : 4;
+    const int x = e ? std::atoi(e) : 1;
     return x < 1 ? 1 : x > 7 ? 7 : x;
   }();
   return N < (1u << 16) ? 1 : (uint32_t)v;
