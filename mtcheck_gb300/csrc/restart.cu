@@ -993,7 +993,7 @@ __device__ __forceinline__ void chunk_source(const RArgs& a, const OwnMasks& own
 // bytes in flight per warp.
 // Whole warps take 32 consecutive chunks at a time: the warp's own keys'
 // step masks come from one coalesced load and a transpose per 32 steps.
-__global__ void __launch_bounds__(256, 6) resolve_kernel(RArgs a) {
+__global__ void __launch_bounds__(256, 8) resolve_kernel(RArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint2* bm = reinterpret_cast<const uint2*>(a.sbm);
