@@ -612,17 +612,21 @@ __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a) {
     const uint64_t t1 = t0 + kChainTile < total ? t0 + kChainTile : total;
     const uint64_t* excl = rm ? a.sh_excl + a.sh_cb : a.dm_excl;
     const uint32_t n = rm ? a.nsh - a.sh_cb : a.nfo - a.fo_cb;
-    expand_stage(T, excl, n, base + t0, base + t1);
+    // list and basic: every chain entry is exactly one item, so an item's
+    // entry is its own index and nothing needs expanding
+    if (tree) expand_stage(T, excl, n, base + t0, base + t1);
     const uint32_t lane = threadIdx.x & 31;
     // whole warps step together (the fast path below is a warp operation)
     for (uint64_t tw = t0 + (threadIdx.x & ~31u); tw < t1; tw += blockDim.x) {
       const uint64_t t = tw + lane;
       const bool in = t < t1;
       uint32_t k = 0, j = 0;
-      if (in) {
+      if (in && tree) {
         uint64_t j64;
         k = expand_entry(T, excl, n, base + t, &j64);
         j = (uint32_t)j64;
+      } else if (in) {
+        k = (uint32_t)t;
       }
       uint32_t lo = 0, hi = 0, k0 = 0;
       if (!rm && tree) {
@@ -712,7 +716,7 @@ __global__ void __launch_bounds__(256) chain_tables_kernel(RArgs a) {
         seg_bits(a, s, 1, k0, lo, hi);
       }
     }
-    __syncthreads();
+    if (tree) __syncthreads();
   }
 }
 
