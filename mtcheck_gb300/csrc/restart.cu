@@ -346,15 +346,18 @@ struct TwoLists {
 // (src/tree_approach.cpp:825-925; ranks: FO entries 1+i, shift entries 2^32+i);
 // the FO regions (prefix fo_excl, total tot[2]) and the shift regions (prefix
 // sh_excl, total tot[3]) in one launch
+// tiles of 256 items: the main checkpoint holds a few percent of the chunks,
+// and tiles of 2048 left most SMs without one
+constexpr uint32_t kCoverTile = 256;
 __global__ void __launch_bounds__(256) main_cover_kernel(RArgs a) {
-  __shared__ ExpandTile<> T;
-  const TwoLists<> L(a.tot[2], a.tot[3]);
+  __shared__ ExpandTile<kCoverTile> T;
+  const TwoLists<kCoverTile> L(a.tot[2], a.tot[3]);
   const bool tree = a.approach == APPROACH_TREE;
   for (uint64_t tile = blockIdx.x; tile < L.tiles(); tile += gridDim.x) {
     const bool sh = tile >= L.nt0;
     const uint64_t total = sh ? L.tot1 : L.tot0;
-    const uint64_t t0 = (sh ? tile - L.nt0 : tile) * kExpandTile;
-    const uint64_t t1 = t0 + kExpandTile < total ? t0 + kExpandTile : total;
+    const uint64_t t0 = (sh ? tile - L.nt0 : tile) * kCoverTile;
+    const uint64_t t1 = t0 + kCoverTile < total ? t0 + kCoverTile : total;
     const uint64_t* excl = sh ? a.sh_excl : a.fo_excl;
     const uint32_t n = sh ? a.S0 : a.F0;
     expand_stage(T, excl, n, t0, t1);
