@@ -612,7 +612,7 @@ def serve_bench(torch, mc, dev, a):
     the arrival time to completion.  Before the timed stream every process
     makes one incremental checkpoint and every buffer size one restart
     (warm-up).  The update steps are drawn before the
-    stream starts (DeviceUpdates) so that the driver keeps up with the rate.
+    stream starts (DeviceUpdates) so that the client loop keeps up with the rate.
     Every restart is verified against a digest of the state it restores; a
     sample of processes is replayed alone through lone handles and compared
     byte for byte with the served chain."""
