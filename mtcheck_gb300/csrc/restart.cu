@@ -536,7 +536,7 @@ __global__ void entry_scan_sums_kernel(EntryScans e, uint64_t* tile_sums) {
   block_excl_scan(sum, sh, &total);
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
-__global__ void entry_scan_emit_kernel(EntryScans e, const uint64_t* tile_sums) {
+__global__ void __launch_bounds__(kScanThreads, 3) entry_scan_emit_kernel(EntryScans e, const uint64_t* tile_sums) {
   __shared__ uint64_t sh[33];
   const int k = entry_scan_seg(e, blockIdx.x);
   uint64_t part = 0;
