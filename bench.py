@@ -943,6 +943,7 @@ def section_in_subprocess(flag, key, a):
                  "serve_verify_procs", "serve_pinned_gb", "serve_sat_procs", "serve_sat_requests",
                  "batch_count", "batch_median_mib", "batch_steps"):
         args += ["--" + name.replace("_", "-"), str(getattr(a, name))]
+    args += ["--hash", a.hash]
     if a.batch_no_tune:
         args.append("--batch-no-tune")
     if a.serve_trace:
